@@ -1,0 +1,195 @@
+"""ctypes front end of the C oracle (oracle/liboracle_sclet.so).
+
+TEST INFRASTRUCTURE: used by tests/, __graft_entry__.smoke() and the bench's
+CPU-baseline leg as the checker; never by the product path.
+
+``load_case(dir, suffix)`` parses a run directory in the reference's formats
+(see oracle/cases.py) with numpy, independently of the product's C parser, and
+``Oracle`` holds a state and calls the C restatement.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Dict
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle_sclet.so")
+
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+class OrcCfg(ctypes.Structure):
+    _fields_ = [
+        ("n", ctypes.c_int), ("nac", ctypes.c_int), ("nch", ctypes.c_int),
+        ("etd2", ctypes.c_int), ("elastic", ctypes.c_int), ("anisotropic", ctypes.c_int),
+        ("dt", ctypes.c_double), ("epn2", ctypes.c_double),
+        ("h", ctypes.c_double * 3), ("kk", ctypes.c_double * 3),
+        ("lam", ctypes.c_double * 36),
+        ("elastic_scale", ctypes.c_double),
+        ("a2", ctypes.c_double), ("a4", ctypes.c_double), ("a6", ctypes.c_double),
+        ("g", ctypes.c_double), ("th", ctypes.c_double), ("c0", ctypes.c_double),
+        ("A", ctypes.c_double), ("LE", ctypes.c_double), ("KE", ctypes.c_double),
+        ("LCI", ctypes.c_double), ("KCI", ctypes.c_double),
+        ("mp", _dp * 3), ("mpi", _dp * 3), ("dd", _dp * 3),
+        ("bn", _dp),
+        ("elam", ctypes.c_double * 36),
+        ("energy_form", ctypes.c_int),
+    ]
+
+
+def build(out_dir: str = HERE) -> str:
+    """Compiles the C oracle (gcc, OpenMP when available) into out_dir."""
+    import subprocess
+    srcs = [os.path.join(HERE, "sclet_oracle.c"), os.path.join(HERE, "ref_shims", "oracle_fft.c")]
+    out = os.path.join(out_dir, "liboracle_sclet.so")
+    base = ["gcc", "-std=gnu99", "-O2", "-fPIC", "-shared", "-I" + HERE, "-o", out] + srcs + ["-lm"]
+    try:
+        subprocess.run(base[:4] + ["-fopenmp"] + base[4:], check=True, capture_output=True)
+    except subprocess.CalledProcessError:
+        subprocess.run(base, check=True)
+    return out
+
+
+def _lib():
+    lib = ctypes.CDLL(LIB_PATH)
+    lib.orc_threads.restype = ctypes.c_int
+    return lib
+
+
+def _ptr(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_dp)
+
+
+def _read_numbers(path: str):
+    with open(path) as fp:
+        return [float(t) for t in fp.read().replace(",", " ").split()]
+
+
+def load_case(case_dir: str, suffix: str) -> Dict:
+    """Parses a run directory (ini: source_beta_to_omega/src/ScLETD.c:16-34)."""
+    with open(os.path.join(case_dir, f"input{suffix}.ini")) as fp:
+        lines = [ln.strip() for ln in fp if ln.strip()]
+    nums = lambda s: [float(t) for t in s.replace(",", " ").split()]
+    p = {}
+    p["n"] = int(nums(lines[0])[0])
+    p["dt"], p["t_total"] = nums(lines[5])
+    p["epn2"] = nums(lines[6])[0]
+    p["nac"], p["nch"] = [int(v) for v in nums(lines[8])]
+    lo, hi = nums(lines[10]), nums(lines[11])
+    p["etd2"] = int(nums(lines[12])[0])
+    p["elastic"] = int(nums(lines[13])[0])
+    p["anisotropic"] = int(nums(lines[14])[0])
+    p["kk"] = nums(lines[15])
+    n = p["n"]
+    big_n = n - 4
+    p["h"] = [(hi[d] - lo[d]) / big_n for d in range(3)]
+    el = _read_numbers(os.path.join(case_dir, "elastic_input.txt"))
+    p["elastic_scale"] = el[0]
+    p["voigt"] = np.array(el[1:37]).reshape(6, 6)
+    p["eps"] = np.array(el[37:73]).reshape(4, 3, 3)
+    lam_file = np.zeros((4, 3, 3))
+    if p["anisotropic"]:
+        an = _read_numbers(os.path.join(case_dir, "anisotropic_input.txt"))
+        lam_file[: p["nac"]] = np.array(an[: 9 * p["nac"]]).reshape(p["nac"], 3, 3)
+    p["lam_file"] = lam_file
+    p["landau"] = _read_numbers(os.path.join(case_dir, "landau_input.txt"))
+    # eigen data of the Dirichlet-Dirichlet variant (id 3, src/vars.c:488-582)
+    d = np.loadtxt(os.path.join(case_dir, f"d3{n}.dat"))
+    v = np.loadtxt(os.path.join(case_dir, f"v3{n}.dat"))
+    vi = np.loadtxt(os.path.join(case_dir, f"vi3{n}.dat"))
+    p["d"], p["v"], p["vi"] = d, v, vi
+    fields = []
+    for kind, cnt in (("ac", p["nac"]), ("ch", p["nch"])):
+        for m in range(cnt):
+            vals = np.loadtxt(os.path.join(case_dir, "input", f"field_iter0_{kind}{m}_000.txt"))
+            blk = np.zeros((n, n, n))
+            blk[2:-2, 2:-2, 2:-2] = vals.reshape(big_n, big_n, big_n)
+            fields.append(blk)
+    p["fields"] = np.stack(fields)
+    return p
+
+
+class Oracle:
+    """C oracle state for one case.  ``u`` is (F, n, n, n) incl. ghosts."""
+
+    def __init__(self, p: Dict, energy_form: int = 1):
+        self.lib = _lib()
+        self.p = p
+        n = p["n"]
+        self.n = n
+        self.F = p["nac"] + p["nch"]
+        c = OrcCfg()
+        c.n, c.nac, c.nch = n, p["nac"], p["nch"]
+        c.etd2, c.elastic, c.anisotropic = p["etd2"], p["elastic"], p["anisotropic"]
+        c.dt, c.epn2 = p["dt"], p["epn2"]
+        for d in range(3):
+            c.h[d] = p["h"][d]
+            c.kk[d] = p["kk"][d]
+        lam = np.zeros((4, 3, 3))
+        for m in range(p["nac"]):
+            lam[m] = np.diag(p["kk"]) - p["lam_file"][m]
+        self.lam = lam
+        for i, v in enumerate(lam.reshape(-1)):
+            c.lam[i] = v
+        c.elastic_scale = p["elastic_scale"]
+        (c.a2, c.a4, c.a6, c.g, c.th, c.c0, c.A, c.LE, c.KE, c.LCI, c.KCI) = p["landau"]
+        # matrices column-major like the reference (element (r, c) at c*n + r)
+        self._keep = []
+        for d in range(3):
+            mp = np.ascontiguousarray(p["v"].T.reshape(-1))
+            mpi = np.ascontiguousarray(p["vi"].T.reshape(-1))
+            dd = np.ascontiguousarray(p["d"] / p["h"][d] ** 2)
+            self._keep += [mp, mpi, dd]
+            c.mp[d], c.mpi[d], c.dd[d] = _ptr(mp), _ptr(mpi), _ptr(dd)
+        big_n = n - 4
+        if p["elastic"]:
+            self.bn = np.zeros(16 * big_n ** 3)
+            self.lib.orc_compute_bn(ctypes.c_int(big_n), _ptr(np.ascontiguousarray(p["voigt"].reshape(-1))),
+                                    _ptr(np.ascontiguousarray(p["eps"].reshape(-1))), _ptr(self.bn))
+            c.bn = _ptr(self.bn)
+        elam = lam.copy() if p["anisotropic"] else np.zeros((4, 3, 3))
+        for i, v in enumerate(elam.reshape(-1)):
+            c.elam[i] = v
+        c.energy_form = energy_form
+        self.cfg = c
+        self.u = np.ascontiguousarray(p["fields"].copy())
+        self.felas = np.zeros((max(p["nac"], 1), n, n, n))
+        self.fstate = np.zeros((n, n, n))
+
+    def set_energy_tensors(self, elam: np.ndarray, form: int) -> None:
+        for i, v in enumerate(np.asarray(elam, dtype=np.float64).reshape(-1)):
+            self.cfg.elam[i] = v
+        self.cfg.energy_form = form
+
+    def step(self, k: int = 1) -> None:
+        for _ in range(k):
+            self.lib.orc_step(ctypes.byref(self.cfg), _ptr(self.u), _ptr(self.felas), _ptr(self.fstate))
+
+    def rhs(self) -> np.ndarray:
+        """Fill + elastic + right-hand sides on the current state (modifies
+        ghosts and elastic scratch like the reference's first half-pass)."""
+        for m in range(self.F):
+            self.lib.orc_ghost_fill(ctypes.c_int(self.n), _ptr(self.u[m]))
+        if self.p["elastic"]:
+            self.lib.orc_elastic(ctypes.byref(self.cfg), _ptr(self.u), _ptr(self.felas), _ptr(self.fstate))
+        out = np.zeros_like(self.u)
+        self.lib.orc_rhs(ctypes.byref(self.cfg), _ptr(self.u), _ptr(self.felas), _ptr(out))
+        return out
+
+    def check_soln(self) -> np.ndarray:
+        out = np.zeros(self.F * 4)
+        self.lib.orc_check_soln(ctypes.byref(self.cfg), _ptr(self.u), _ptr(out))
+        return out.reshape(self.F, 4)
+
+    def mode_product(self, mat_colmajor: np.ndarray, a: np.ndarray) -> np.ndarray:
+        out = np.zeros_like(a)
+        self.lib.orc_mode_product(ctypes.c_int(self.n), _ptr(np.ascontiguousarray(mat_colmajor)),
+                                  _ptr(np.ascontiguousarray(a)), _ptr(out))
+        return out
+
+    def threads(self) -> int:
+        return self.lib.orc_threads()
