@@ -1,0 +1,213 @@
+// Diagnostics of the state: check_soln_new (source_beta_to_omega/src/field.c:
+// 407-678) as a device reduction.  Per field: max, min and vol = sum(u + 1) h^3
+// over the owned cells; energy over the owned cells' corner cubes from the
+// 8-corner averages and corner-difference gradients (field.c:487-511):
+//   sum_m epn2/2 grad(eta_m).lambda_m.grad(eta_m)  [+ epn2/2 |grad c|^2]
+//   + Landau energy of the averages.
+// form 0 reproduces the reference's hard-coded 2-3-4 polynomial and its
+// separate CH energy ((c^2-1)^2/4); form 1 is the plugin's total free energy.
+// Sums are compensated (TwoSum pairs) in FP64 and reduced in a fixed order,
+// so the result is deterministic.
+#include "sclet_internal.cuh"
+
+namespace sclet {
+
+struct KS {
+  double s, c;
+};
+__device__ inline void two_sum(double a, double b, double &s, double &e) {
+  s = a + b;
+  double bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+__device__ inline void ks_add(KS &k, double v) {
+  double s, e;
+  two_sum(k.s, v, s, e);
+  k.s = s;
+  k.c += e;
+}
+__device__ inline KS ks_merge(KS a, KS b) {
+  KS r;
+  double e;
+  two_sum(a.s, b.s, r.s, e);
+  r.c = a.c + b.c + e;
+  return r;
+}
+
+constexpr int EB = 256;  // threads per block
+constexpr int MAXF = 5;
+
+// partial record per block: for f < F: max, min, vol.s, vol.c; then
+// eng_ac.s, eng_ac.c, eng_ch.s, eng_ch.c
+__host__ __device__ inline int rec_len(int F) { return 4 * F + 4; }
+
+template <typename T>
+__global__ void __launch_bounds__(EB) energy_partial_kernel(Phys ph, const T *__restrict__ u, const double *__restrict__ elam,
+                                                            int form, double *__restrict__ part) {
+  const int n = ph.n, N = n - 4, F = ph.F, nac = ph.nac;
+  const long long n3 = (long long)n * n * n, N3 = (long long)N * N * N;
+  const double hx = ph.h[0], hy = ph.h[1], hz = ph.h[2];
+  double mx[MAXF], mn[MAXF];
+  KS vol[MAXF], eac = {0, 0}, ech = {0, 0};
+  for (int f = 0; f < F; f++) {
+    mx[f] = -1.0e30;
+    mn[f] = 1.0e30;
+    vol[f].s = 0;
+    vol[f].c = 0;
+  }
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < N3; g += (long long)gridDim.x * blockDim.x) {
+    int i = 2 + (int)(g % N), j = 2 + (int)((g / N) % N), k = 2 + (int)(g / ((long long)N * N));
+    long long l = ((long long)k * n + j) * n + i;
+    for (int f = 0; f < F; f++) {
+      double t = (double)u[f * n3 + l];
+      mx[f] = fmax(mx[f], t);
+      mn[f] = fmin(mn[f], t);
+      ks_add(vol[f], t + 1.0);
+    }
+    if (i >= n - 3 || j >= n - 3 || k >= n - 3) continue;
+    double avg[MAXF];
+    double cbar = 0.0;
+    for (int f = 0; f < F; f++) {
+      const T *q = u + f * n3;
+      double v0 = q[l], v1 = q[l + 1], v2 = q[l + n], v3 = q[l + n + 1];
+      double v4 = q[l + n * n], v5 = q[l + n * n + 1], v6 = q[l + n * n + n], v7 = q[l + n * n + n + 1];
+      avg[f] = (v0 + v1 + v2 + v3 + v4 + v5 + v6 + v7) / 8;
+      double ux = ((v1 - v0) + (v3 - v2) + (v5 - v4) + (v7 - v6)) / 4 / hx;
+      double uy = ((v2 - v0) + (v3 - v1) + (v6 - v4) + (v7 - v5)) / 4 / hy;
+      double uz = ((v4 - v0) + (v5 - v1) + (v6 - v2) + (v7 - v3)) / 4 / hz;
+      if (f < nac) {
+        const double *L = elam + 9 * f;
+        double fx = ux * L[0] + uy * L[3] + uz * L[6];
+        double fy = ux * L[1] + uy * L[4] + uz * L[7];
+        double fz = ux * L[2] + uy * L[5] + uz * L[8];
+        ks_add(eac, ph.epn2 * (fx * ux + fy * uy + fz * uz) / 2);
+      } else {
+        double gr = ph.epn2 * (ux * ux + uy * uy + uz * uz) / 2;
+        if (form == 0) ks_add(ech, gr); else ks_add(eac, gr);
+        cbar = avg[f];
+      }
+    }
+    if (form == 0) {
+      double e[4] = {0, 0, 0, 0};
+      for (int f = 0; f < nac && f < 4; f++) e[f] = avg[f];
+      double s2 = e[0] * e[0] + e[1] * e[1] + e[2] * e[2] + e[3] * e[3];
+      double s3 = e[0] * e[0] * e[0] + e[1] * e[1] * e[1] + e[2] * e[2] * e[2] + e[3] * e[3] * e[3];
+      if (nac > 0)
+        ks_add(eac, (2376.0 / 2372.0 / 2.0) * s2 - ((7128.0 + 12.0 * 2372.0) / 2372.0 / 3.0) * s3 +
+                        ((4752.0 + 12.0 * 2372.0) / 2372.0 / 4.0) * s2 * s2);
+      if (ph.nch > 0) ks_add(ech, (cbar * cbar - 1) * (cbar * cbar - 1) / 4);
+    } else {
+      double fl = 0.0, s2 = 0.0;
+      for (int m = 0; m < nac; m++) {
+        double u2 = avg[m] * avg[m];
+        s2 += u2;
+        fl += ph.a2 / 2.0 * u2 + ph.a4 / 4.0 * u2 * u2 + ph.a6 / 6.0 * u2 * u2 * u2;
+        for (int q = m + 1; q < nac; q++) fl += ph.g * u2 * avg[q] * avg[q];
+      }
+      if (ph.nch > 0) fl += ph.A / 2.0 * (cbar - ph.c0) * (cbar - ph.c0) - ph.th * (cbar - ph.c0) * s2;
+      ks_add(eac, fl);
+    }
+  }
+  // block reduction through shared memory
+  __shared__ double sh[EB];
+  __shared__ double out_rec[4 * MAXF + 4];
+  auto reduce_max = [&](double v, bool is_max) -> double {
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int w = EB / 2; w > 0; w >>= 1) {
+      if (threadIdx.x < w) sh[threadIdx.x] = is_max ? fmax(sh[threadIdx.x], sh[threadIdx.x + w]) : fmin(sh[threadIdx.x], sh[threadIdx.x + w]);
+      __syncthreads();
+    }
+    double r = sh[0];
+    __syncthreads();
+    return r;
+  };
+  __shared__ double shc[EB];
+  auto reduce_ks = [&](KS v) -> KS {
+    sh[threadIdx.x] = v.s;
+    shc[threadIdx.x] = v.c;
+    __syncthreads();
+    for (int w = EB / 2; w > 0; w >>= 1) {
+      if (threadIdx.x < w) {
+        KS a = {sh[threadIdx.x], shc[threadIdx.x]}, b = {sh[threadIdx.x + w], shc[threadIdx.x + w]};
+        KS r = ks_merge(a, b);
+        sh[threadIdx.x] = r.s;
+        shc[threadIdx.x] = r.c;
+      }
+      __syncthreads();
+    }
+    KS r = {sh[0], shc[0]};
+    __syncthreads();
+    return r;
+  };
+  for (int f = 0; f < F; f++) {
+    double a = reduce_max(mx[f], true);
+    double b = reduce_max(mn[f], false);
+    KS v = reduce_ks(vol[f]);
+    if (threadIdx.x == 0) {
+      out_rec[4 * f] = a;
+      out_rec[4 * f + 1] = b;
+      out_rec[4 * f + 2] = v.s;
+      out_rec[4 * f + 3] = v.c;
+    }
+  }
+  KS a = reduce_ks(eac), b = reduce_ks(ech);
+  if (threadIdx.x == 0) {
+    double *dst = part + (long long)blockIdx.x * rec_len(F);
+    for (int q = 0; q < 4 * F; q++) dst[q] = out_rec[q];
+    dst[4 * F] = a.s;
+    dst[4 * F + 1] = a.c;
+    dst[4 * F + 2] = b.s;
+    dst[4 * F + 3] = b.c;
+  }
+}
+
+__global__ void energy_final_kernel(Phys ph, int form, const double *__restrict__ part, int npart, double *__restrict__ out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int F = ph.F;
+  const double h3 = ph.h[0] * ph.h[1] * ph.h[2];
+  KS eac = {0, 0}, ech = {0, 0};
+  for (int b = 0; b < npart; b++) {
+    const double *r = part + (long long)b * rec_len(F);
+    eac = ks_merge(eac, KS{r[4 * F], r[4 * F + 1]});
+    ech = ks_merge(ech, KS{r[4 * F + 2], r[4 * F + 3]});
+  }
+  for (int f = 0; f < F; f++) {
+    double mx = -1.0e30, mn = 1.0e30;
+    KS vol = {0, 0};
+    for (int b = 0; b < npart; b++) {
+      const double *r = part + (long long)b * rec_len(F);
+      mx = fmax(mx, r[4 * f]);
+      mn = fmin(mn, r[4 * f + 1]);
+      vol = ks_merge(vol, KS{r[4 * f + 2], r[4 * f + 3]});
+    }
+    out[4 * f] = mx;
+    out[4 * f + 1] = mn;
+    out[4 * f + 2] = (vol.s + vol.c) * h3;
+    double e = (form == 0 && f >= ph.nac) ? (ech.s + ech.c) : (eac.s + eac.c);
+    out[4 * f + 3] = e * h3;
+  }
+}
+
+int check_soln_partials(int n) {
+  long long N3 = (long long)(n - 4) * (n - 4) * (n - 4);
+  long long b = (N3 + EB - 1) / EB;
+  return (int)(b > 152 * 8 ? 152 * 8 : b);
+}
+
+template <typename T>
+cudaError_t launch_check_soln(const Phys &ph, const T *u, const double *elam, int form, double *partials, int npart,
+                              double *out, cudaStream_t s) {
+  if (ph.F > MAXF) return cudaErrorInvalidValue;
+  energy_partial_kernel<T><<<npart, EB, 0, s>>>(ph, u, elam, form, partials);
+  energy_final_kernel<<<1, 32, 0, s>>>(ph, form, partials, npart, out);
+  launch_counter() += 2;
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_check_soln<double>(const Phys &, const double *, const double *, int, double *, int, double *,
+                                               cudaStream_t);
+template cudaError_t launch_check_soln<float>(const Phys &, const float *, const double *, int, double *, int, double *,
+                                              cudaStream_t);
+
+}  // namespace sclet

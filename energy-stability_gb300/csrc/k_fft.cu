@@ -1,0 +1,507 @@
+// Khachaturyan elastic driving force on one periodic block (the reference's
+// elastic_calculate, source_beta_to_omega/src/elastic.c:617-763, with the
+// distributed fftMPI transform of src/fft3d.c:98-138 replaced by a
+// single-GPU mixed-radix FFT).
+//
+//   felas_p = Re IFFT( sum_q B_pq(k) FFT(eta_q) )       on the N^3 owned cells
+//   B_pq(n) = C:e0_p:e0_q - (s0_p n) . Om(n) . (s0_q n), Om = (C n n)^-1,
+//   n = k/|k| with the reference's wave-number convention (0..N/2-1, -N/2..-1),
+//   n = (0,1,0) at k = 0 (elastic_calculate_BN, elastic.c:460-605).
+//
+// GB300 design: two real fields travel as one complex field (eta_0 + i eta_1,
+// eta_2 + i eta_3), so the reference's 2 nac^2 transforms become 2 forward and
+// 2 inverse complex transforms.  The reference keeps only the real part of
+// each inverse transform; the contraction therefore builds the Hermitian part
+// G_p(k) = (F_p(k) + conj F_p(-k)) / 2 of each product spectrum
+// F_p = sum_q B_pq H_q (B is not even at the Nyquist planes), whose inverse
+// transform is exactly that real part, before packing G_0 + i G_1.
+// Each 1D pass keeps tiles of lines in shared memory (Stockham autosort,
+// radices 4, 2, 3, 5); lines along y and z are loaded as runs of adjacent x.
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <vector>
+
+#include "sclet_internal.cuh"
+
+namespace sclet {
+
+template <typename T>
+struct Cx;
+template <>
+struct Cx<double> {
+  typedef double2 t;
+};
+template <>
+struct Cx<float> {
+  typedef float2 t;
+};
+
+template <typename C>
+__device__ inline C cmul(C a, C b) {
+  C r;
+  r.x = a.x * b.x - a.y * b.y;
+  r.y = a.x * b.y + a.y * b.x;
+  return r;
+}
+template <typename C>
+__device__ inline C cadd(C a, C b) {
+  C r;
+  r.x = a.x + b.x;
+  r.y = a.y + b.y;
+  return r;
+}
+template <typename C>
+__device__ inline C csub(C a, C b) {
+  C r;
+  r.x = a.x - b.x;
+  r.y = a.y - b.y;
+  return r;
+}
+template <typename C>
+__device__ inline C cconj(C a) {
+  a.y = -a.y;
+  return a;
+}
+
+struct Radices {
+  int count;
+  int r[16];
+};
+
+static Radices factor(int n) {
+  Radices f;
+  f.count = 0;
+  while (n % 4 == 0) { f.r[f.count++] = 4; n /= 4; }
+  while (n % 2 == 0) { f.r[f.count++] = 2; n /= 2; }
+  while (n % 3 == 0) { f.r[f.count++] = 3; n /= 3; }
+  while (n % 5 == 0) { f.r[f.count++] = 5; n /= 5; }
+  if (n != 1) f.count = -1;
+  return f;
+}
+
+// One batch of line FFTs.  axis 0: lines along x (contiguous); 1: along y;
+// 2: along z.  sign -1 forward, +1 backward (unscaled).  tw[j] = exp(-2 pi i j / N).
+template <typename T>
+__global__ void __launch_bounds__(256) fft_lines_kernel(typename Cx<T>::t *data, int N, int axis, int tile,
+                                                        const typename Cx<T>::t *__restrict__ tw, int sign,
+                                                        Radices rad) {
+  typedef typename Cx<T>::t C;
+  extern __shared__ unsigned char smem_raw[];
+  C *buf0 = reinterpret_cast<C *>(smem_raw);
+  C *buf1 = buf0 + (size_t)tile * N;
+  const long long NN = (long long)N * N;
+  // Line set of this CTA
+  long long base;
+  long long stride, lstride;
+  if (axis == 0) {
+    long long line0 = (long long)blockIdx.x * tile;  // lines indexed by (z*N + y)
+    base = line0 * N;
+    stride = 1;
+    lstride = N;
+  } else if (axis == 1) {
+    int xt = blockIdx.x % (N / tile);
+    int z = blockIdx.x / (N / tile);
+    base = (long long)z * NN + (long long)xt * tile;
+    stride = N;
+    lstride = 1;
+  } else {
+    int xt = blockIdx.x % (N / tile);
+    int y = blockIdx.x / (N / tile);
+    base = (long long)y * N + (long long)xt * tile;
+    stride = NN;
+    lstride = 1;
+  }
+  const int total = tile * N;
+  for (int e = threadIdx.x; e < total; e += blockDim.x) {
+    int line, pos;
+    if (axis == 0) { line = e / N; pos = e % N; }
+    else { line = e % tile; pos = e / tile; }
+    buf0[line * N + pos] = data[base + line * lstride + pos * stride];
+  }
+  __syncthreads();
+  C *src = buf0, *dst = buf1;
+  int Ns = 1;
+  for (int st = 0; st < rad.count; st++) {
+    const int R = rad.r[st];
+    const int nb = N / R;
+    for (int e = threadIdx.x; e < tile * nb; e += blockDim.x) {
+      int line = e / nb, j = e % nb;
+      const C *s = src + line * N;
+      C *d = dst + line * N;
+      int k = j % Ns;
+      C v[5];
+      for (int r = 0; r < R; r++) {
+        v[r] = s[j + r * nb];
+        if (r > 0 && k > 0) {
+          int idx = (int)(((long long)r * k * (N / (Ns * R))) % N);
+          C w = tw[idx];
+          if (sign > 0) w.y = -w.y;
+          v[r] = cmul(v[r], w);
+        }
+      }
+      C o[5];
+      if (R == 2) {
+        o[0] = cadd(v[0], v[1]);
+        o[1] = csub(v[0], v[1]);
+      } else if (R == 4) {
+        C a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
+        C c = cadd(v[1], v[3]), d2 = csub(v[1], v[3]);
+        // multiply d2 by -i (forward) or +i (backward)
+        C dj;
+        if (sign < 0) { dj.x = d2.y; dj.y = -d2.x; }
+        else { dj.x = -d2.y; dj.y = d2.x; }
+        o[0] = cadd(a, c);
+        o[2] = csub(a, c);
+        o[1] = cadd(b, dj);
+        o[3] = csub(b, dj);
+      } else {
+        for (int q = 0; q < R; q++) {
+          C acc = v[0];
+          for (int r = 1; r < R; r++) {
+            int idx = (int)(((long long)r * q * nb) % N);
+            C w = tw[idx];
+            if (sign > 0) w.y = -w.y;
+            acc = cadd(acc, cmul(v[r], w));
+          }
+          o[q] = acc;
+        }
+      }
+      int idxD = (j / Ns) * Ns * R + k;
+      for (int r = 0; r < R; r++) d[idxD + r * Ns] = o[r];
+    }
+    __syncthreads();
+    C *t = src;
+    src = dst;
+    dst = t;
+    Ns *= R;
+  }
+  for (int e = threadIdx.x; e < total; e += blockDim.x) {
+    int line, pos;
+    if (axis == 0) { line = e / N; pos = e % N; }
+    else { line = e % tile; pos = e / tile; }
+    data[base + line * lstride + pos * stride] = src[line * N + pos];
+  }
+}
+
+// eta pairs -> complex grids (owned cells of the n^3 blocks, n = N + 4).
+template <typename T>
+__global__ void pack_kernel(const T *__restrict__ u, typename Cx<T>::t *__restrict__ z01,
+                            typename Cx<T>::t *__restrict__ z23, int N, int nac) {
+  const int n = N + 4;
+  const long long n3 = (long long)n * n * n, N3 = (long long)N * N * N;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < N3; g += (long long)gridDim.x * blockDim.x) {
+    int x = (int)(g % N), y = (int)((g / N) % N), z = (int)(g / ((long long)N * N));
+    long long l = ((long long)(z + 2) * n + (y + 2)) * n + (x + 2);
+    T v[4];
+    for (int q = 0; q < 4; q++) v[q] = q < nac ? u[q * n3 + l] : (T)0;
+    typename Cx<T>::t a, b;
+    a.x = v[0]; a.y = v[1];
+    b.x = v[2]; b.y = v[3];
+    z01[g] = a;
+    if (z23) z23[g] = b;
+  }
+}
+
+__host__ __device__ inline int pq_slot(int p, int q) {
+  if (p > q) { int t = p; p = q; q = t; }
+  // (0,0)0 (0,1)1 (0,2)2 (0,3)3 (1,1)4 (1,2)5 (1,3)6 (2,2)7 (2,3)8 (3,3)9
+  return p * 4 - p * (p - 1) / 2 + (q - p);
+}
+
+// Green-tensor kernel on the full grid, 10 symmetric slots (FP64, once).
+struct BnConst {
+  double C[81];
+  double sig[4][9];
+  double t0[10];
+};
+
+__global__ void bn_kernel(double *__restrict__ bn, int N, BnConst bc) {
+  const long long N3 = (long long)N * N * N;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < N3; g += (long long)gridDim.x * blockDim.x) {
+    int x = (int)(g % N), y = (int)((g / N) % N), z = (int)(g / ((long long)N * N));
+    double kx = x < N / 2 ? (double)x : -(double)(N - x);
+    double ky = y < N / 2 ? (double)y : -(double)(N - y);
+    double kz = z < N / 2 ? (double)z : -(double)(N - z);
+    double nv[3];
+    if (x == 0 && y == 0 && z == 0) {
+      nv[0] = 0.0; nv[1] = 1.0; nv[2] = 0.0;
+    } else {
+      double r = sqrt(kx * kx + ky * ky + kz * kz);
+      nv[0] = kx / r; nv[1] = ky / r; nv[2] = kz / r;
+    }
+    double a[9];
+    for (int i = 0; i < 3; i++)
+      for (int k = 0; k < 3; k++) {
+        double s = 0.0;
+        for (int j = 0; j < 3; j++)
+          for (int l = 0; l < 3; l++) s += bc.C[((i * 3 + j) * 3 + k) * 3 + l] * nv[j] * nv[l];
+        a[i * 3 + k] = s;
+      }
+    double det = a[0] * (a[4] * a[8] - a[5] * a[7]) - a[1] * (a[3] * a[8] - a[5] * a[6]) +
+                 a[2] * (a[3] * a[7] - a[4] * a[6]);
+    double om[9];
+    om[0] = (a[4] * a[8] - a[5] * a[7]) / det;
+    om[1] = -(a[3] * a[8] - a[6] * a[5]) / det;
+    om[2] = (a[3] * a[7] - a[6] * a[4]) / det;
+    om[3] = -(a[1] * a[8] - a[7] * a[2]) / det;
+    om[4] = (a[0] * a[8] - a[2] * a[6]) / det;
+    om[5] = -(a[0] * a[7] - a[6] * a[1]) / det;
+    om[6] = (a[1] * a[5] - a[4] * a[2]) / det;
+    om[7] = -(a[0] * a[5] - a[3] * a[2]) / det;
+    om[8] = (a[0] * a[4] - a[1] * a[3]) / det;
+    double v[4][3];
+    for (int p = 0; p < 4; p++)
+      for (int i = 0; i < 3; i++)
+        v[p][i] = bc.sig[p][i * 3 + 0] * nv[0] + bc.sig[p][i * 3 + 1] * nv[1] + bc.sig[p][i * 3 + 2] * nv[2];
+    for (int p = 0; p < 4; p++)
+      for (int q = p; q < 4; q++) {
+        double t1 = 0.0;
+        for (int j = 0; j < 3; j++)
+          for (int k = 0; k < 3; k++) t1 += v[p][j] * om[j * 3 + k] * v[q][k];
+        bn[(long long)pq_slot(p, q) * N3 + g] = bc.t0[pq_slot(p, q)] - t1;
+      }
+  }
+}
+
+// Contraction on pairs {k, -k}; see the file comment.
+template <typename T>
+__global__ void contract_kernel(typename Cx<T>::t *z01, typename Cx<T>::t *z23, const double *__restrict__ bn, int N,
+                                int nac) {
+  typedef typename Cx<T>::t C;
+  const long long N3 = (long long)N * N * N;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < N3; g += (long long)gridDim.x * blockDim.x) {
+    int x = (int)(g % N), y = (int)((g / N) % N), z = (int)(g / ((long long)N * N));
+    int xm = (N - x) % N, ym = (N - y) % N, zm = (N - z) % N;
+    long long gm = ((long long)zm * N + ym) * N + xm;
+    if (gm < g) continue;  // the pair is handled by its lower index
+    C H[4], Hm[4];
+    C a = z01[g], am = z01[gm];
+    C b, bm;
+    b.x = 0; b.y = 0; bm = b;
+    if (z23) { b = z23[g]; bm = z23[gm]; }
+    // split Z = A + iB into the two real fields' spectra
+    H[0].x = (T)0.5 * (a.x + am.x); H[0].y = (T)0.5 * (a.y - am.y);
+    H[1].x = (T)0.5 * (a.y + am.y); H[1].y = (T)0.5 * (am.x - a.x);
+    H[2].x = (T)0.5 * (b.x + bm.x); H[2].y = (T)0.5 * (b.y - bm.y);
+    H[3].x = (T)0.5 * (b.y + bm.y); H[3].y = (T)0.5 * (bm.x - b.x);
+    for (int q = 0; q < 4; q++) {
+      if (q >= nac) { H[q].x = 0; H[q].y = 0; }
+      Hm[q] = cconj(H[q]);
+    }
+    C G[4];
+    for (int p = 0; p < 4; p++) {
+      C f, fm;
+      f.x = 0; f.y = 0; fm = f;
+      for (int q = 0; q < 4; q++) {
+        T bk = (T)bn[(long long)pq_slot(p, q) * N3 + g];
+        T bkm = (T)bn[(long long)pq_slot(p, q) * N3 + gm];
+        f.x += bk * H[q].x; f.y += bk * H[q].y;
+        fm.x += bkm * Hm[q].x; fm.y += bkm * Hm[q].y;
+      }
+      // Hermitian part: its inverse transform is Re(IFFT(F_p))
+      G[p].x = (T)0.5 * (f.x + fm.x);
+      G[p].y = (T)0.5 * (f.y - fm.y);
+      if (p >= nac) { G[p].x = 0; G[p].y = 0; }
+    }
+    C w01, w23, w01m, w23m;
+    w01.x = G[0].x - G[1].y; w01.y = G[0].y + G[1].x;    // G0 + i G1
+    w01m.x = G[0].x + G[1].y; w01m.y = -G[0].y + G[1].x; // conj(G0) + i conj(G1)
+    w23.x = G[2].x - G[3].y; w23.y = G[2].y + G[3].x;
+    w23m.x = G[2].x + G[3].y; w23m.y = -G[2].y + G[3].x;
+    z01[g] = w01;
+    if (gm != g) z01[gm] = w01m;
+    if (z23) {
+      z23[g] = w23;
+      if (gm != g) z23[gm] = w23m;
+    }
+  }
+}
+
+// Interior of felas_p from the inverse transforms, scaled by 1/N^3.
+template <typename T>
+__global__ void unpack_kernel(const typename Cx<T>::t *__restrict__ w01, const typename Cx<T>::t *__restrict__ w23,
+                              T *__restrict__ felas, int N, int nac) {
+  const int n = N + 4;
+  const long long n3 = (long long)n * n * n, N3 = (long long)N * N * N;
+  const double s = 1.0 / (double)N3;
+  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < N3; g += (long long)gridDim.x * blockDim.x) {
+    int x = (int)(g % N), y = (int)((g / N) % N), z = (int)(g / ((long long)N * N));
+    long long l = ((long long)(z + 2) * n + (y + 2)) * n + (x + 2);
+    typename Cx<T>::t a = w01[g];
+    felas[l] = (T)(a.x * s);
+    if (nac > 1) felas[n3 + l] = (T)(a.y * s);
+    if (nac > 2) {
+      typename Cx<T>::t b = w23[g];
+      felas[2 * n3 + l] = (T)(b.x * s);
+      if (nac > 3) felas[3 * n3 + l] = (T)(b.y * s);
+    }
+  }
+}
+
+struct ElasticPlan {
+  int N, nac, fp32;
+  Radices rad;
+  void *tw;       // twiddles, complex of the working precision
+  void *z01, *z23;
+  double *bn;     // 10 * N^3
+  int tile;
+  size_t smem;
+  bool first;     // no previous elastic call: scratch ghosts are zero
+};
+
+static int grid1(long long total) {
+  long long b = (total + 255) / 256;
+  return (int)(b > 152LL * 32 ? 152LL * 32 : (b < 1 ? 1 : b));
+}
+
+cudaError_t elastic_plan_create(ElasticPlan **out, int N, int nac, const double *voigt, const double *eps, int fp32,
+                                cudaStream_t s) {
+  ElasticPlan *p = new ElasticPlan();
+  memset(p, 0, sizeof *p);
+  p->N = N;
+  p->nac = nac;
+  p->fp32 = fp32;
+  p->first = true;
+  p->rad = factor(N);
+  if (p->rad.count < 0 || nac < 1 || nac > 4) {
+    delete p;
+    return cudaErrorInvalidValue;
+  }
+  const long long N3 = (long long)N * N * N;
+  size_t csz = fp32 ? sizeof(float2) : sizeof(double2);
+  cudaError_t e;
+  if ((e = cudaMalloc(&p->tw, csz * N)) != cudaSuccess) goto fail;
+  if ((e = cudaMalloc(&p->z01, csz * N3)) != cudaSuccess) goto fail;
+  if (nac > 2 && (e = cudaMalloc(&p->z23, csz * N3)) != cudaSuccess) goto fail;
+  if ((e = cudaMalloc(&p->bn, sizeof(double) * 10 * N3)) != cudaSuccess) goto fail;
+  {
+    std::vector<double> twd(2 * N);
+    for (int j = 0; j < N; j++) {
+      double a = -2.0 * 3.14159265358979323846 * (double)j / (double)N;
+      twd[2 * j] = cos(a);
+      twd[2 * j + 1] = sin(a);
+    }
+    if (fp32) {
+      std::vector<float> twf(2 * N);
+      for (int j = 0; j < 2 * N; j++) twf[j] = (float)twd[j];
+      e = cudaMemcpyAsync(p->tw, twf.data(), sizeof(float) * 2 * N, cudaMemcpyHostToDevice, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    } else {
+      e = cudaMemcpyAsync(p->tw, twd.data(), sizeof(double) * 2 * N, cudaMemcpyHostToDevice, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    }
+    if (e != cudaSuccess) goto fail;
+  }
+  {
+    // stiffness (elastic_input, elastic.c:378-398) and s0 = C : e0
+    static const int vi[3][3] = {{0, 5, 4}, {5, 1, 3}, {4, 3, 2}};
+    BnConst bc;
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++)
+        for (int k = 0; k < 3; k++)
+          for (int l = 0; l < 3; l++) bc.C[((i * 3 + j) * 3 + k) * 3 + l] = voigt[vi[i][j] * 6 + vi[k][l]];
+    for (int q = 0; q < 4; q++)
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+          double acc = 0.0;
+          for (int k = 0; k < 3; k++)
+            for (int l = 0; l < 3; l++) acc += bc.C[((i * 3 + j) * 3 + k) * 3 + l] * eps[q * 9 + k * 3 + l];
+          bc.sig[q][i * 3 + j] = acc;
+        }
+    for (int a = 0; a < 4; a++)
+      for (int b = a; b < 4; b++) {
+        double t0 = 0.0;
+        for (int i = 0; i < 3; i++)
+          for (int j = 0; j < 3; j++)
+            for (int k = 0; k < 3; k++)
+              for (int l = 0; l < 3; l++)
+                t0 += bc.C[((i * 3 + j) * 3 + k) * 3 + l] * eps[a * 9 + i * 3 + j] * eps[b * 9 + k * 3 + l];
+        bc.t0[pq_slot(a, b)] = t0;
+      }
+    bn_kernel<<<grid1(N3), 256, 0, s>>>(p->bn, N, bc);
+    launch_counter()++;
+    if ((e = cudaGetLastError()) != cudaSuccess) goto fail;
+  }
+  {
+    // tile of lines per CTA: two ping-pong buffers within ~96 KB
+    int tile = 16;
+    while (tile > 1 && 2 * (size_t)tile * N * csz > 96 * 1024) tile /= 2;
+    while (N % tile) tile /= 2;
+    p->tile = tile;
+    p->smem = 2 * (size_t)tile * N * csz;
+  }
+  *out = p;
+  return cudaSuccess;
+fail:
+  elastic_plan_destroy(p);
+  return e;
+}
+
+void elastic_plan_destroy(ElasticPlan *p) {
+  if (!p) return;
+  cudaFree(p->tw);
+  cudaFree(p->z01);
+  cudaFree(p->z23);
+  cudaFree(p->bn);
+  delete p;
+}
+
+template <typename T>
+static cudaError_t fft3d(ElasticPlan *p, typename Cx<T>::t *z, int sign, cudaStream_t s) {
+  const int N = p->N;
+  static bool attr_set[2] = {false, false};
+  int which = sizeof(T) == 4 ? 1 : 0;
+  if (!attr_set[which]) {
+    cudaFuncSetAttribute(fft_lines_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr_set[which] = true;
+  }
+  const int lines_blocks = (int)((long long)N * N / p->tile);
+  const typename Cx<T>::t *tw = (const typename Cx<T>::t *)p->tw;
+  int order[3] = {0, 1, 2};
+  if (sign > 0) { order[0] = 2; order[2] = 0; }
+  for (int k = 0; k < 3; k++) {
+    fft_lines_kernel<T><<<lines_blocks, 256, p->smem, s>>>(z, N, order[k], p->tile, tw, sign, p->rad);
+    launch_counter()++;
+  }
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t elastic_compute(ElasticPlan *p, const T *u, T *felas, int n, T *shell, cudaStream_t s) {
+  typedef typename Cx<T>::t C;
+  const int N = p->N;
+  const long long N3 = (long long)N * N * N, n3 = (long long)n * n * n;
+  C *z01 = (C *)p->z01, *z23 = (C *)p->z23;
+  pack_kernel<T><<<grid1(N3), 256, 0, s>>>(u, z01, z23, N, p->nac);
+  launch_counter()++;
+  fft3d<T>(p, z01, -1, s);
+  if (z23) fft3d<T>(p, z23, -1, s);
+  contract_kernel<T><<<grid1(N3), 256, 0, s>>>(z01, z23, p->bn, N, p->nac);
+  launch_counter()++;
+  fft3d<T>(p, z01, +1, s);
+  if (z23) fft3d<T>(p, z23, +1, s);
+  unpack_kernel<T><<<grid1(N3), 256, 0, s>>>(z01, z23, felas, N, p->nac);
+  launch_counter()++;
+  // ghost cells: the shared-scratch semantics, field by field in order
+  for (int q = 0; q < p->nac; q++) {
+    const T *prev = felas + (long long)((q + p->nac - 1) % p->nac) * n3;
+    if (p->first && q == 0) {
+      // before the first call the scratch block is all zero
+      cudaMemsetAsync(shell, 0, sizeof(T) * n3, s);
+      prev = shell;
+      cudaError_t e = launch_elastic_shell<T>(felas, prev, n, shell + n3, s);
+      if (e != cudaSuccess) return e;
+      continue;
+    }
+    cudaError_t e = launch_elastic_shell<T>(felas + q * n3, prev, n, shell, s);
+    if (e != cudaSuccess) return e;
+  }
+  p->first = false;
+  return cudaGetLastError();
+}
+
+template cudaError_t elastic_compute<double>(ElasticPlan *, const double *, double *, int, double *, cudaStream_t);
+template cudaError_t elastic_compute<float>(ElasticPlan *, const float *, float *, int, float *, cudaStream_t);
+
+}  // namespace sclet

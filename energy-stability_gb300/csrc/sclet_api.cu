@@ -1,0 +1,563 @@
+// C ABI of sclet_gb300: context, device state and the step sequence of the
+// reference's time loop (source_beta_to_omega/src/ScLETD.c:84-191) on one GPU.
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "sclet_gb300.h"
+#include "sclet_internal.cuh"
+
+namespace sclet {
+void set_phi_tables(const double *phi1_ac, const double *phi1_ch, const double *phi2_ac, const double *phi2_ch);
+}
+
+using namespace sclet;
+
+struct StageEv {
+  int cls;
+  cudaEvent_t a, b;
+};
+
+struct sclet_ctx {
+  sclet_params p;
+  int precision = SCLET_FP64, device = 0;
+  int n = 0, F = 0, nac = 0, nch = 0;
+  long long n3 = 0;
+  Phys ph;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  // FP64 state: state2 = [u (F blocks) | rhs1 (F blocks)]
+  double *state2 = nullptr, *rhs2 = nullptr, *A = nullptr, *B = nullptr;
+  double *felas = nullptr, *scratch = nullptr, *shell = nullptr;
+  double *V[3] = {nullptr, nullptr, nullptr}, *Vi[3] = {nullptr, nullptr, nullptr}, *dd[3] = {nullptr, nullptr, nullptr};
+  double *phi1[2] = {nullptr, nullptr}, *phi2[2] = {nullptr, nullptr};
+  double *elam = nullptr, *partials = nullptr, *diag = nullptr;
+  int npart = 0;
+  ElasticPlan *elastic = nullptr;
+  bool profiling = false;
+  std::vector<StageEv> evs;
+  float stage_ms[8] = {0};
+  int stage_launches[8] = {0};
+  long long launches0 = 0;
+};
+
+static std::string g_create_error;
+
+#define CK(call)                                                                  \
+  do {                                                                            \
+    cudaError_t e_ = (call);                                                      \
+    if (e_ != cudaSuccess) {                                                      \
+      ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);              \
+      return e_ == cudaErrorMemoryAllocation ? SCLET_ERR_NOMEM : SCLET_ERR_CUDA;  \
+    }                                                                             \
+  } while (0)
+
+namespace {
+
+double *u_of(sclet_ctx *ctx) { return ctx->state2; }
+double *rhs1_of(sclet_ctx *ctx) { return ctx->state2 + (long long)ctx->F * ctx->n3; }
+
+// phi1, phi2 of each field kind at eigen-mode (i, j, k), layout [k][j][i]
+// (ac_init_phi / ch_init_phi, vars.c:302-359).
+__global__ void phi_kernel(double *phi1, double *phi2, int n, int kind, const double *dx, const double *dy,
+                           const double *dz, double kkx, double kky, double kkz, double epn2, double dt, double L,
+                           double K) {
+  long long n3 = (long long)n * n * n;
+  for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < n3; o += (long long)gridDim.x * blockDim.x) {
+    int i = (int)(o % n), j = (int)((o / n) % n), k = (int)(o / ((long long)n * n));
+    double tmp, H;
+    if (kind == 0) {
+      tmp = kkz * dz[k] + kky * dy[j] + kkx * dx[i];
+      H = -L * (tmp * epn2 - K);
+    } else {
+      tmp = dz[k] + dy[j] + dx[i];
+      H = L * (tmp * tmp * epn2 - K * tmp);
+    }
+    double p1, p2;
+    if (fabs(H) > 1.0e-8) {
+      double e = exp(-dt * H);
+      p1 = (1.0 - e) / H;
+      p2 = (1.0 - p1 / dt) / H;
+    } else {
+      p1 = dt;
+      p2 = dt / 2;
+    }
+    phi1[o] = p1;
+    phi2[o] = p2;
+  }
+}
+
+int grid_of(long long total) {
+  long long b = (total + 255) / 256;
+  return (int)(b > 152LL * 16 ? 152LL * 16 : (b < 1 ? 1 : b));
+}
+
+int fail(sclet_ctx *ctx, int code, const std::string &msg) {
+  ctx->err = msg;
+  return code;
+}
+
+int upload_eigen(sclet_ctx *ctx, const double *d, const double *v, const double *vi) {
+  const int n = ctx->n;
+  std::vector<double> ds(n);
+  for (int ax = 0; ax < 3; ax++) {
+    double h = ctx->ph.h[ax];
+    // DDX[l] = DDX_b[l] / hx / hx (vars.c:510-513)
+    for (int l = 0; l < n; l++) ds[l] = d[l] / h / h;
+    CK(cudaMemcpyAsync(ctx->dd[ax], ds.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->V[ax], v, sizeof(double) * n * n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->Vi[ax], vi, sizeof(double) * n * n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  const sclet_params &p = ctx->p;
+  const double *lan = p.landau;
+  phi_kernel<<<grid_of(ctx->n3), 256, 0, ctx->stream>>>(ctx->phi1[0], ctx->phi2[0], n, 0, ctx->dd[0], ctx->dd[1],
+                                                        ctx->dd[2], p.kkx, p.kky, p.kkz, p.epn2, p.dt, lan[7], lan[8]);
+  phi_kernel<<<grid_of(ctx->n3), 256, 0, ctx->stream>>>(ctx->phi1[1], ctx->phi2[1], n, 1, ctx->dd[0], ctx->dd[1],
+                                                        ctx->dd[2], p.kkx, p.kky, p.kkz, p.epn2, p.dt, lan[9], lan[10]);
+  launch_counter() += 2;
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  return SCLET_OK;
+}
+
+EtdCoef etd_coef(sclet_ctx *ctx) {
+  EtdCoef ec;
+  for (int a = 0; a < 3; a++) ec.dd[a] = ctx->dd[a];
+  ec.kk[0] = ctx->p.kkx;
+  ec.kk[1] = ctx->p.kky;
+  ec.kk[2] = ctx->p.kkz;
+  ec.epn2 = ctx->p.epn2;
+  ec.dt = ctx->p.dt;
+  ec.LE = ctx->ph.LE;
+  ec.KE = ctx->ph.KE;
+  ec.LCI = ctx->ph.LCI;
+  ec.KCI = ctx->ph.KCI;
+  ec.nac = ctx->nac;
+  ec.F = ctx->F;
+  return ec;
+}
+
+void stage_begin(sclet_ctx *ctx, int cls, StageEv &ev) {
+  if (!ctx->profiling) return;
+  ev.cls = cls;
+  cudaEventCreate(&ev.a);
+  cudaEventCreate(&ev.b);
+  cudaEventRecord(ev.a, ctx->stream);
+}
+void stage_end(sclet_ctx *ctx, StageEv &ev, long long l0) {
+  if (!ctx->profiling) return;
+  cudaEventRecord(ev.b, ctx->stream);
+  ctx->evs.push_back(ev);
+  ctx->stage_launches[ev.cls] += (int)(launch_counter() - l0);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *sclet_last_error(const sclet_ctx *ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
+
+int sclet_block_edge(const sclet_ctx *ctx) { return ctx->n; }
+int sclet_field_count(const sclet_ctx *ctx) { return ctx->F; }
+void *sclet_stream(const sclet_ctx *ctx) { return (void *)ctx->stream; }
+long long sclet_launch_count(const sclet_ctx *ctx) { return launch_counter() - ctx->launches0; }
+
+void sclet_destroy(sclet_ctx *ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  double *bufs[] = {ctx->state2, ctx->rhs2, ctx->A, ctx->B, ctx->felas, ctx->scratch, ctx->shell, ctx->elam,
+                    ctx->partials, ctx->diag, ctx->phi1[0], ctx->phi1[1], ctx->phi2[0], ctx->phi2[1]};
+  for (double *b : bufs) cudaFree(b);
+  for (int a = 0; a < 3; a++) {
+    cudaFree(ctx->V[a]);
+    cudaFree(ctx->Vi[a]);
+    cudaFree(ctx->dd[a]);
+  }
+  for (auto &e : ctx->evs) {
+    cudaEventDestroy(e.a);
+    cudaEventDestroy(e.b);
+  }
+  elastic_plan_destroy(ctx->elastic);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+int sclet_create(const sclet_params *p, int precision, int device, sclet_ctx **out) {
+  *out = nullptr;
+  g_create_error.clear();
+  auto bad = [&](const char *m) {
+    g_create_error = m;
+    return SCLET_ERR_ARG;
+  };
+  if (p->nx != p->ny || p->nx != p->nz) return bad("nx, ny, nz must be equal (one cubic block)");
+  if (p->px != 1 || p->py != 1 || p->pz != 1) return bad("one block per GPU: px = py = pz = 1");
+  if (p->nghost != 2) return bad("nghost must be 2");
+  if (p->periodic != 1) return bad("periodic must be 1 (single block with self-neighbours)");
+  if (p->nx < 8 || p->nx > 1028) return bad("block edge out of range [8, 1028]");
+  if (p->nac < 0 || p->nac > 4 || p->nch < 0 || p->nch > 1 || p->nac + p->nch < 1)
+    return bad("supported: 0..4 Allen-Cahn fields and 0..1 Cahn-Hilliard field");
+  if (p->variable_mobility != 0) {
+    g_create_error = "VariableMobility = 1 is not supported (constant-mobility CH only)";
+    return SCLET_ERR_UNSUPPORTED;
+  }
+  if (p->elastic != 0 && p->elastic != 1) {
+    g_create_error = "ELASTIC must be 0 or 1 (elastic force on the Allen-Cahn fields)";
+    return SCLET_ERR_UNSUPPORTED;
+  }
+  if (p->elastic == 1 && p->nac < 1) return bad("ELASTIC = 1 needs Allen-Cahn fields");
+  if (precision != SCLET_FP64 && precision != SCLET_MIXED) return bad("precision must be SCLET_FP64 or SCLET_MIXED");
+  if (precision == SCLET_MIXED) {
+    g_create_error = "SCLET_MIXED is not available in this build";
+    return SCLET_ERR_UNSUPPORTED;
+  }
+  sclet_ctx *ctx = new sclet_ctx();
+  ctx->p = *p;
+  ctx->precision = precision;
+  ctx->device = device;
+  ctx->n = p->nx;
+  ctx->nac = p->nac;
+  ctx->nch = p->nch;
+  ctx->F = p->nac + p->nch;
+  ctx->n3 = (long long)ctx->n * ctx->n * ctx->n;
+  ctx->launches0 = launch_counter();
+  const int n = ctx->n, F = ctx->F, N = n - 4;
+  Phys &ph = ctx->ph;
+  memset(&ph, 0, sizeof ph);
+  ph.n = n;
+  ph.nac = ctx->nac;
+  ph.nch = ctx->nch;
+  ph.F = F;
+  ph.anisotropic = p->anisotropic;
+  ph.elastic = p->elastic;
+  ph.dt = p->dt;
+  ph.epn2 = p->epn2;
+  // h = (max - min) / gN with gN = n - 2 nghost on one periodic block (vars.c:58-157)
+  ph.h[0] = (p->xmax - p->xmin) / N;
+  ph.h[1] = (p->ymax - p->ymin) / N;
+  ph.h[2] = (p->zmax - p->zmin) / N;
+  ph.kk[0] = p->kkx;
+  ph.kk[1] = p->kky;
+  ph.kk[2] = p->kkz;
+  // lambda = diag(kk) - file tensor (anisotropic_input, anisotropic.c:653-672)
+  for (int m = 0; m < 4; m++)
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) ph.lam[m][i * 3 + j] = (i == j ? ph.kk[i] : 0.0) - p->lambda_file[m][i * 3 + j];
+  ph.elastic_scale = p->elastic_scale;
+  ph.a2 = p->landau[0];
+  ph.a4 = p->landau[1];
+  ph.a6 = p->landau[2];
+  ph.g = p->landau[3];
+  ph.th = p->landau[4];
+  ph.c0 = p->landau[5];
+  ph.A = p->landau[6];
+  ph.LE = p->landau[7];
+  ph.KE = p->landau[8];
+  ph.LCI = p->landau[9];
+  ph.KCI = p->landau[10];
+
+  int rc = SCLET_OK;
+  auto cfail = [&](cudaError_t e, const char *what) {
+    ctx->err = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? SCLET_ERR_NOMEM : SCLET_ERR_CUDA;
+  };
+  cudaError_t e;
+#define CC(call)                       \
+  if ((e = (call)) != cudaSuccess) {   \
+    rc = cfail(e, #call);              \
+    g_create_error = ctx->err;         \
+    sclet_destroy(ctx);                \
+    return rc;                         \
+  }
+  CC(cudaSetDevice(device));
+  CC(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+  const size_t blk = sizeof(double) * ctx->n3;
+  CC(cudaMalloc(&ctx->state2, 2 * F * blk));
+  CC(cudaMemsetAsync(ctx->state2, 0, 2 * F * blk, ctx->stream));
+  if (p->etd2) CC(cudaMalloc(&ctx->rhs2, F * blk));
+  CC(cudaMalloc(&ctx->A, 2 * F * blk));
+  CC(cudaMalloc(&ctx->B, 2 * F * blk));
+  CC(cudaMalloc(&ctx->felas, (ctx->nac > 0 ? ctx->nac : 1) * blk));
+  CC(cudaMemsetAsync(ctx->felas, 0, (ctx->nac > 0 ? ctx->nac : 1) * blk, ctx->stream));
+  CC(cudaMalloc(&ctx->scratch, 2 * blk));
+  CC(cudaMalloc(&ctx->shell, sizeof(double) * F * shell_count(n)));
+  for (int a = 0; a < 3; a++) {
+    CC(cudaMalloc(&ctx->V[a], sizeof(double) * n * n));
+    CC(cudaMalloc(&ctx->Vi[a], sizeof(double) * n * n));
+    CC(cudaMalloc(&ctx->dd[a], sizeof(double) * n));
+  }
+  for (int k = 0; k < 2; k++) {
+    CC(cudaMalloc(&ctx->phi1[k], blk));
+    CC(cudaMalloc(&ctx->phi2[k], blk));
+  }
+  CC(cudaMalloc(&ctx->elam, sizeof(double) * 36));
+  ctx->npart = check_soln_partials(n);
+  CC(cudaMalloc(&ctx->partials, sizeof(double) * ctx->npart * (4 * F + 4)));
+  CC(cudaMalloc(&ctx->diag, sizeof(double) * 4 * F));
+  {
+    // energy tensors: the gradient operator of the dynamics
+    double el[36] = {0};
+    for (int m = 0; m < 4; m++)
+      for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++)
+          el[m * 9 + i * 3 + j] = p->anisotropic ? p->lambda_file[m][i * 3 + j] : (i == j ? ph.kk[i] : 0.0);
+    CC(cudaMemcpyAsync(ctx->elam, el, sizeof el, cudaMemcpyHostToDevice, ctx->stream));
+    CC(cudaStreamSynchronize(ctx->stream));
+  }
+  {
+    std::vector<double> d(n), v((size_t)n * n), vi((size_t)n * n);
+    sclet_eigen_dirichlet(n, d.data(), v.data(), vi.data());
+    rc = upload_eigen(ctx, d.data(), v.data(), vi.data());
+    if (rc != SCLET_OK) {
+      g_create_error = ctx->err;
+      sclet_destroy(ctx);
+      return rc;
+    }
+  }
+  if (p->elastic == 1) {
+    CC(elastic_plan_create(&ctx->elastic, N, ctx->nac, p->voigt, &p->eigenstrain[0][0], 0, ctx->stream));
+  }
+  CC(cudaStreamSynchronize(ctx->stream));
+#undef CC
+  *out = ctx;
+  return SCLET_OK;
+}
+
+int sclet_set_eigen(sclet_ctx *ctx, const double *d, const double *v, const double *vi) {
+  CK(cudaSetDevice(ctx->device));
+  return upload_eigen(ctx, d, v, vi);
+}
+
+int sclet_set_energy_tensors(sclet_ctx *ctx, const double *lam) {
+  double el[36] = {0};
+  memcpy(el, lam, sizeof(double) * 9 * ctx->nac);
+  CK(cudaMemcpyAsync(ctx->elam, el, sizeof el, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return SCLET_OK;
+}
+
+static int field_index(sclet_ctx *ctx, int kind, int m) {
+  if (kind == SCLET_AC && m >= 0 && m < ctx->nac) return m;
+  if (kind == SCLET_CH && m >= 0 && m < ctx->nch) return ctx->nac + m;
+  return -1;
+}
+
+int sclet_set_field(sclet_ctx *ctx, int kind, int m, const double *block) {
+  int f = field_index(ctx, kind, m);
+  if (f < 0) return fail(ctx, SCLET_ERR_ARG, "no such field");
+  CK(cudaMemcpyAsync(u_of(ctx) + f * ctx->n3, block, sizeof(double) * ctx->n3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return SCLET_OK;
+}
+
+int sclet_get_field(sclet_ctx *ctx, int kind, int m, double *block) {
+  int f = field_index(ctx, kind, m);
+  if (f < 0) return fail(ctx, SCLET_ERR_ARG, "no such field");
+  CK(cudaMemcpyAsync(block, u_of(ctx) + f * ctx->n3, sizeof(double) * ctx->n3, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return SCLET_OK;
+}
+
+int sclet_load_restart(sclet_ctx *ctx, int kind, int m, const char *path) {
+  std::vector<double> blk(ctx->n3, 0.0);
+  int f = field_index(ctx, kind, m);
+  if (f < 0) return fail(ctx, SCLET_ERR_ARG, "no such field");
+  CK(cudaMemcpyAsync(blk.data(), u_of(ctx) + f * ctx->n3, sizeof(double) * ctx->n3, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  int rc = sclet_read_restart(path, ctx->n, blk.data());
+  if (rc != SCLET_OK) return fail(ctx, rc, std::string("cannot read restart file ") + path);
+  return sclet_set_field(ctx, kind, m, blk.data());
+}
+
+int sclet_get_rhs(sclet_ctx *ctx, int slot, int kind, int m, double *block) {
+  int f = field_index(ctx, kind, m);
+  if (f < 0 || (slot != 1 && slot != 2) || (slot == 2 && !ctx->rhs2)) return fail(ctx, SCLET_ERR_ARG, "bad rhs slot");
+  const double *src = (slot == 1 ? rhs1_of(ctx) : ctx->rhs2) + f * ctx->n3;
+  CK(cudaMemcpyAsync(block, src, sizeof(double) * ctx->n3, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return SCLET_OK;
+}
+
+int sclet_get_felas(sclet_ctx *ctx, int m, double *block) {
+  if (m < 0 || m >= ctx->nac) return fail(ctx, SCLET_ERR_ARG, "no such field");
+  CK(cudaMemcpyAsync(block, ctx->felas + m * ctx->n3, sizeof(double) * ctx->n3, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return SCLET_OK;
+}
+
+int sclet_transfer(sclet_ctx *ctx) {
+  StageEv ev;
+  long long l0 = launch_counter();
+  stage_begin(ctx, 3, ev);
+  CK(launch_ghost_fill<double>(u_of(ctx), ctx->F, ctx->n, ctx->shell, ctx->stream));
+  stage_end(ctx, ev, l0);
+  return SCLET_OK;
+}
+
+int sclet_elastic_calculate(sclet_ctx *ctx) {
+  if (!ctx->elastic) return SCLET_OK;
+  StageEv ev;
+  long long l0 = launch_counter();
+  stage_begin(ctx, 2, ev);
+  CK(elastic_compute<double>(ctx->elastic, u_of(ctx), ctx->felas, ctx->n, ctx->scratch, ctx->stream));
+  stage_end(ctx, ev, l0);
+  return SCLET_OK;
+}
+
+int sclet_calc_rhs(sclet_ctx *ctx, int slot) {
+  if (slot != 1 && slot != 2) return fail(ctx, SCLET_ERR_ARG, "slot must be 1 or 2");
+  if (slot == 2 && !ctx->rhs2) return fail(ctx, SCLET_ERR_ARG, "slot 2 needs ETD2 = 1");
+  StageEv ev;
+  long long l0 = launch_counter();
+  stage_begin(ctx, 1, ev);
+  double *dst = slot == 1 ? rhs1_of(ctx) : ctx->rhs2;
+  CK(launch_rhs<double>(ctx->ph, u_of(ctx), ctx->felas, dst, ctx->scratch, ctx->stream));
+  stage_end(ctx, ev, l0);
+  return SCLET_OK;
+}
+
+int sclet_etd_update(sclet_ctx *ctx) {
+  const int F = ctx->F;
+  const long long n3 = ctx->n3;
+  EtdCoef ec = etd_coef(ctx);
+  set_phi_tables(ctx->phi1[0], ctx->phi1[1], ctx->phi2[0], ctx->phi2[1]);
+  StageEv ev;
+  long long l0 = launch_counter();
+  stage_begin(ctx, 0, ev);
+  cudaStream_t s = ctx->stream;
+  // V^-1 along x, y for u and N1 together; along z for u, then for N1 with
+  // the ETD1 update fused (uhat in A[0..F) is updated in place).
+  CK(launch_modeprod_f64(ctx->Vi[0], ctx->state2, nullptr, ctx->A, nullptr, 2 * F, ctx->n, 0, ec, n3, n3, s));
+  CK(launch_modeprod_f64(ctx->Vi[1], ctx->A, nullptr, ctx->B, nullptr, 2 * F, ctx->n, 0, ec, n3, n3, s));
+  CK(launch_modeprod_f64(ctx->Vi[2], ctx->B, nullptr, ctx->A, nullptr, F, ctx->n, 0, ec, n3, n3, s));
+  CK(launch_modeprod_f64(ctx->Vi[2], ctx->B + F * n3, nullptr, ctx->A, ctx->A, F, ctx->n, 1, ec, n3, n3, s));
+  // V along x, y, z back to physical space
+  CK(launch_modeprod_f64(ctx->V[0], ctx->A, nullptr, ctx->B, nullptr, F, ctx->n, 0, ec, n3, n3, s));
+  CK(launch_modeprod_f64(ctx->V[1], ctx->B, nullptr, ctx->A, nullptr, F, ctx->n, 0, ec, n3, n3, s));
+  CK(launch_modeprod_f64(ctx->V[2], ctx->A, nullptr, u_of(ctx), nullptr, F, ctx->n, 0, ec, n3, n3, s));
+  stage_end(ctx, ev, l0);
+  return SCLET_OK;
+}
+
+int sclet_etd2_correct(sclet_ctx *ctx) {
+  if (!ctx->rhs2) return fail(ctx, SCLET_ERR_ARG, "ETD2 = 0");
+  const int F = ctx->F;
+  const long long n3 = ctx->n3;
+  EtdCoef ec = etd_coef(ctx);
+  set_phi_tables(ctx->phi1[0], ctx->phi1[1], ctx->phi2[0], ctx->phi2[1]);
+  StageEv ev;
+  long long l0 = launch_counter();
+  stage_begin(ctx, 0, ev);
+  cudaStream_t s = ctx->stream;
+  CK(launch_modeprod_f64(ctx->Vi[0], ctx->rhs2, rhs1_of(ctx), ctx->A, nullptr, F, ctx->n, 0, ec, n3, n3, s));
+  CK(launch_modeprod_f64(ctx->Vi[1], ctx->A, nullptr, ctx->B, nullptr, F, ctx->n, 0, ec, n3, n3, s));
+  CK(launch_modeprod_f64(ctx->Vi[2], ctx->B, nullptr, ctx->A, nullptr, F, ctx->n, 2, ec, n3, n3, s));
+  CK(launch_modeprod_f64(ctx->V[0], ctx->A, nullptr, ctx->B, nullptr, F, ctx->n, 0, ec, n3, n3, s));
+  CK(launch_modeprod_f64(ctx->V[1], ctx->B, nullptr, ctx->A, nullptr, F, ctx->n, 0, ec, n3, n3, s));
+  CK(launch_modeprod_f64(ctx->V[2], ctx->A, nullptr, u_of(ctx), nullptr, F, ctx->n, 3, ec, n3, n3, s));
+  stage_end(ctx, ev, l0);
+  return SCLET_OK;
+}
+
+int sclet_step(sclet_ctx *ctx, int nsteps) {
+  int rc;
+  CK(cudaSetDevice(ctx->device));
+  for (int s = 0; s < nsteps; s++) {
+    if ((rc = sclet_transfer(ctx)) != SCLET_OK) return rc;
+    if ((rc = sclet_elastic_calculate(ctx)) != SCLET_OK) return rc;
+    if ((rc = sclet_calc_rhs(ctx, 1)) != SCLET_OK) return rc;
+    if ((rc = sclet_etd_update(ctx)) != SCLET_OK) return rc;
+    if (ctx->p.etd2) {
+      if ((rc = sclet_transfer(ctx)) != SCLET_OK) return rc;
+      if ((rc = sclet_elastic_calculate(ctx)) != SCLET_OK) return rc;
+      if ((rc = sclet_calc_rhs(ctx, 2)) != SCLET_OK) return rc;
+      if ((rc = sclet_etd2_correct(ctx)) != SCLET_OK) return rc;
+    }
+  }
+  return SCLET_OK;
+}
+
+int sclet_check_soln(sclet_ctx *ctx, int energy_form, sclet_diag *out) {
+  StageEv ev;
+  long long l0 = launch_counter();
+  stage_begin(ctx, 4, ev);
+  CK(launch_check_soln<double>(ctx->ph, u_of(ctx), ctx->elam, energy_form, ctx->partials, ctx->npart, ctx->diag,
+                               ctx->stream));
+  stage_end(ctx, ev, l0);
+  std::vector<double> h(4 * ctx->F);
+  CK(cudaMemcpyAsync(h.data(), ctx->diag, sizeof(double) * 4 * ctx->F, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  int nonfinite = 0;
+  for (int f = 0; f < ctx->F; f++) {
+    out[f].max = h[4 * f];
+    out[f].min = h[4 * f + 1];
+    out[f].vol = h[4 * f + 2];
+    out[f].energy = h[4 * f + 3];
+    if (!isfinite(out[f].max) || !isfinite(out[f].min) || !isfinite(out[f].energy)) nonfinite = 1;
+  }
+  if (nonfinite) return fail(ctx, SCLET_ERR_NONFINITE, "non-finite value in the state");
+  return SCLET_OK;
+}
+
+int sclet_mode_product(sclet_ctx *ctx, int inverse, const double *in, double *out) {
+  EtdCoef ec = etd_coef(ctx);
+  const long long n3 = ctx->n3;
+  CK(cudaMemcpyAsync(ctx->A, in, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
+  CK(launch_modeprod_f64(inverse ? ctx->V[0] : ctx->Vi[0], ctx->A, nullptr, ctx->B, nullptr, 1, ctx->n, 0, ec, n3, n3,
+                         ctx->stream));
+  CK(cudaMemcpyAsync(out, ctx->B, sizeof(double) * n3, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return SCLET_OK;
+}
+
+int sclet_sync(sclet_ctx *ctx) {
+  CK(cudaStreamSynchronize(ctx->stream));
+  return SCLET_OK;
+}
+
+int sclet_set_profiling(sclet_ctx *ctx, int on) {
+  ctx->profiling = on != 0;
+  return SCLET_OK;
+}
+
+int sclet_time_steps(sclet_ctx *ctx, int nsteps, float *ms) {
+  cudaEvent_t a, b;
+  CK(cudaSetDevice(ctx->device));
+  for (auto &e : ctx->evs) {
+    cudaEventDestroy(e.a);
+    cudaEventDestroy(e.b);
+  }
+  ctx->evs.clear();
+  memset(ctx->stage_ms, 0, sizeof ctx->stage_ms);
+  memset(ctx->stage_launches, 0, sizeof ctx->stage_launches);
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  CK(cudaEventRecord(a, ctx->stream));
+  int rc = sclet_step(ctx, nsteps);
+  CK(cudaEventRecord(b, ctx->stream));
+  CK(cudaEventSynchronize(b));
+  CK(cudaEventElapsedTime(ms, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  for (auto &e : ctx->evs) {
+    float t = 0;
+    cudaEventElapsedTime(&t, e.a, e.b);
+    ctx->stage_ms[e.cls] += t;
+  }
+  return rc;
+}
+
+int sclet_stage_times(const sclet_ctx *ctx, float *ms, int *launches, int nclasses) {
+  for (int k = 0; k < nclasses && k < 8; k++) {
+    ms[k] = ctx->stage_ms[k];
+    launches[k] = ctx->stage_launches[k];
+  }
+  return SCLET_OK;
+}
+
+}  // extern "C"

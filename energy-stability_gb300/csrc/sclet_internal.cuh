@@ -1,0 +1,124 @@
+// Internal declarations shared by the CUDA translation units of sclet_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sclet_gb300.h"
+
+namespace sclet {
+
+// Physics-plugin constants and per-run scalars passed by value to kernels.
+struct Phys {
+  int n, nac, nch, F;
+  int anisotropic, elastic;
+  double dt, epn2;
+  double h[3];
+  double kk[3];
+  double lam[4][9];      // F2 tensors: diag(kk) - file tensor, row-major
+  double elastic_scale;
+  double a2, a4, a6, g, th, c0, A, LE, KE, LCI, KCI;
+};
+
+// Geometry helpers (owned cells are 2 .. n-3 per axis, period N = n - 4).
+__host__ __device__ inline int img(int n, int v) {
+  int N = n - 4;
+  int r = (v - 2) % N;
+  if (r < 0) r += N;
+  return 2 + r;
+}
+__host__ __device__ inline int wrap1(int n, int v) {
+  int N = n - 4;
+  return v < 2 ? v + N : (v >= n - 2 ? v - N : v);
+}
+
+// Number of ghost cells of an n^3 block: 4 z-planes, 4 y-slabs of the inner
+// z range, 4 x-columns of the inner z,y range.
+__host__ __device__ inline long long shell_count(int n) {
+  long long N = n - 4;
+  return 4LL * n * n + 4LL * N * n + 4LL * N * N;
+}
+// Maps a shell index to its cell.
+__device__ inline void shell_cell(int n, long long s, int &z, int &y, int &x) {
+  long long N = n - 4;
+  long long nz = 4LL * n * n;
+  if (s < nz) {
+    int p = (int)(s / ((long long)n * n));
+    long long r = s - (long long)p * n * n;
+    z = p < 2 ? p : n - 4 + p;
+    y = (int)(r / n);
+    x = (int)(r % n);
+    return;
+  }
+  s -= nz;
+  long long ny = 4LL * N * n;
+  if (s < ny) {
+    int zz = (int)(s / (4LL * n));
+    long long r = s - (long long)zz * 4 * n;
+    int p = (int)(r / n);
+    z = 2 + zz;
+    y = p < 2 ? p : n - 4 + p;
+    x = (int)(r % n);
+    return;
+  }
+  s -= ny;
+  {
+    int zz = (int)(s / (4LL * N));
+    long long r = s - (long long)zz * 4 * N;
+    int yy = (int)(r / 4);
+    int p = (int)(r % 4);
+    z = 2 + zz;
+    y = 2 + yy;
+    x = p < 2 ? p : n - 4 + p;
+  }
+}
+
+// ---- kernel launchers (each returns the launch's cudaError_t) -------------
+// Ghost fill of `count` blocks (stride n^3) in place; shell: scratch of
+// count * shell_count(n) elements.
+template <typename T>
+cudaError_t launch_ghost_fill(T *u, int count, int n, T *shell, cudaStream_t s);
+// Elastic scratch semantics: felas_p (p in order) gets its ghost cells from
+// the fill of the shared scratch block (see k_halo.cu).  `prev` is the block
+// that was last filled (felas_{p-1}, or the last field of the previous call).
+template <typename T>
+cudaError_t launch_elastic_shell(T *felas_p, const T *prev, int n, T *shell, cudaStream_t s);
+
+// Right-hand sides of all fields into out (F blocks).  felas: nac blocks.
+template <typename T>
+cudaError_t launch_rhs(const Phys &ph, const T *u, const T *felas, T *out, T *scratch, cudaStream_t s);
+
+// Mode-n product with rotation, FP64: for `count` tensors,
+// out_t[a'*n*n + r] = sum_a M[a'*n + a] in_t[r*n + a]  (M row-major).
+// Epilogues: 0 store; 1 ETD1 update out = (1 - phi H) uhat + phi * acc with
+// uhat = aux_t (read) ; 2 out = phi2 * acc ; 3 out += acc.  Prologue `sub`:
+// in_t - sub_t.  kinds: per-tensor field kind selector (t % F >= nac -> CH).
+struct EtdCoef {
+  const double *dd[3];   // eigenvalues / h^2 per axis (device)
+  double kk[3];
+  double epn2, dt, LE, KE, LCI, KCI;
+  int nac, F;
+};
+cudaError_t launch_modeprod_f64(const double *M, const double *in, const double *sub, double *out,
+                                const double *aux, int count, int n, int epilogue, const EtdCoef &ec,
+                                long long in_stride, long long out_stride, cudaStream_t s);
+
+// Elastic force (FFT based) -- see k_fft.cu.
+struct ElasticPlan;
+cudaError_t elastic_plan_create(ElasticPlan **plan, int big_n, int nac, const double *voigt,
+                                const double *eps, int fp32, cudaStream_t s);
+void elastic_plan_destroy(ElasticPlan *plan);
+// felas (nac blocks of n^3) from the AC fields u (first nac blocks).
+template <typename T>
+cudaError_t elastic_compute(ElasticPlan *plan, const T *u, T *felas, int n, T *shell, cudaStream_t s);
+
+// Diagnostics: out (F*4 doubles, device) per field max, min, vol, energy.
+template <typename T>
+cudaError_t launch_check_soln(const Phys &ph, const T *u, const double *elam, int form, double *partials,
+                              int npart, double *out, cudaStream_t s);
+int check_soln_partials(int n);
+
+// Counts kernel launches issued by this library (per process).
+long long &launch_counter();
+
+}  // namespace sclet

@@ -1,0 +1,212 @@
+/*
+ * Host-side input handling of the ScLETD step: the reference's positional
+ * file formats, the eigen-data files, restart text and the seeded initial
+ * values.  Plain C; no CUDA.
+ */
+#include "sclet_gb300.h"
+
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+void sclet_params_default(sclet_params *p) {
+  int i;
+  memset(p, 0, sizeof *p);
+  p->nx = p->ny = p->nz = 68;
+  p->px = p->py = p->pz = 1;
+  p->nghost = 2;
+  strcpy(p->work_dir, "./output/");
+  strcpy(p->data_dir, "./data/");
+  p->dt = 0.01;
+  p->t_total = 9.995;
+  p->epn2 = 0.5;
+  p->periodic = 1;
+  p->nac = 4;
+  p->nch = 0;
+  strcpy(p->restart_dir, "./restart/");
+  p->xmax = p->ymax = p->zmax = 32.0;
+  p->elastic = 1;
+  p->kkx = p->kky = p->kkz = 1.0;
+  p->elastic_scale = 50.0;
+  for (i = 0; i < 3; i++) {
+    int j;
+    for (j = 0; j < 3; j++) p->voigt[i * 6 + j] = (i == j) ? 1.0 : 0.6;
+    p->voigt[(3 + i) * 6 + 3 + i] = 0.4;
+  }
+  {
+    static const int dirs[4][3] = {{1, 1, 1}, {1, -1, -1}, {-1, 1, -1}, {-1, -1, 1}};
+    int v, a, b;
+    for (v = 0; v < 4; v++)
+      for (a = 0; a < 3; a++)
+        for (b = 0; b < 3; b++) p->eigenstrain[v][a * 3 + b] = a == b ? 0.01 : 0.005 * dirs[v][a] * dirs[v][b];
+  }
+  {
+    static const double lan[11] = {-1.0, -1.0, 2.0, 1.5, 0.8, 0.5, 1.0, 1.0, 6.0, 1.0, 2.0};
+    memcpy(p->landau, lan, sizeof lan);
+  }
+}
+
+/* Positional parse with the same fscanf formats as main() (ScLETD.c:18-34). */
+int sclet_read_ini(const char *path, sclet_params *p) {
+  FILE *f = fopen(path, "r");
+  int ok = 1;
+  if (!f) return SCLET_ERR_IO;
+  ok &= fscanf(f, "%d,%d,%d", &p->nx, &p->ny, &p->nz) == 3;
+  ok &= fscanf(f, "%d,%d,%d", &p->px, &p->py, &p->pz) == 3;
+  ok &= fscanf(f, "%d", &p->nghost) == 1;
+  ok &= fscanf(f, "%1023s", p->work_dir) == 1;
+  ok &= fscanf(f, "%1023s", p->data_dir) == 1;
+  ok &= fscanf(f, "%lf,%lf", &p->dt, &p->t_total) == 2;
+  ok &= fscanf(f, "%lf", &p->epn2) == 1;
+  ok &= fscanf(f, "%d", &p->periodic) == 1;
+  ok &= fscanf(f, "%d, %d", &p->nac, &p->nch) == 2;
+  ok &= fscanf(f, "%d, %d, %1023s", &p->restart, &p->restart_iter, p->restart_dir) == 3;
+  ok &= fscanf(f, "%lf,%lf,%lf", &p->xmin, &p->ymin, &p->zmin) == 3;
+  ok &= fscanf(f, "%lf,%lf,%lf", &p->xmax, &p->ymax, &p->zmax) == 3;
+  ok &= fscanf(f, "%d", &p->etd2) == 1;
+  ok &= fscanf(f, "%d", &p->elastic) == 1;
+  ok &= fscanf(f, "%d", &p->anisotropic) == 1;
+  ok &= fscanf(f, "%lf,%lf,%lf", &p->kkx, &p->kky, &p->kkz) == 3;
+  ok &= fscanf(f, "%d", &p->variable_mobility) == 1;
+  fclose(f);
+  return ok ? SCLET_OK : SCLET_ERR_IO;
+}
+
+/* elastic_input(), elastic.c:349-439: ElasticScale, 36 stiffness values,
+ * then four 3x3 eigenstrains. */
+int sclet_read_elastic_input(const char *path, sclet_params *p) {
+  FILE *f = fopen(path, "r");
+  int i, ok = 1;
+  if (!f) return SCLET_ERR_IO;
+  ok &= fscanf(f, "%lf", &p->elastic_scale) == 1;
+  for (i = 0; i < 36 && ok; i++) ok &= fscanf(f, "%lf", &p->voigt[i]) == 1;
+  for (i = 0; i < 36 && ok; i++) ok &= fscanf(f, "%lf", &p->eigenstrain[i / 9][i % 9]) == 1;
+  fclose(f);
+  return ok ? SCLET_OK : SCLET_ERR_IO;
+}
+
+/* anisotropic_input(), anisotropic.c:630-674: nac 3x3 tensors. */
+int sclet_read_anisotropic_input(const char *path, sclet_params *p) {
+  FILE *f = fopen(path, "r");
+  int i, ok = 1;
+  if (!f) return SCLET_ERR_IO;
+  if (p->nac > 4) {
+    fclose(f);
+    return SCLET_ERR_ARG;
+  }
+  for (i = 0; i < 9 * p->nac && ok; i++) ok &= fscanf(f, "%lf", &p->lambda_file[i / 9][i % 9]) == 1;
+  fclose(f);
+  return ok ? SCLET_OK : SCLET_ERR_IO;
+}
+
+int sclet_read_landau_input(const char *path, sclet_params *p) {
+  FILE *f = fopen(path, "r");
+  int i, ok = 1;
+  if (!f) return SCLET_ERR_IO;
+  for (i = 0; i < 11 && ok; i++) ok &= fscanf(f, "%lf", &p->landau[i]) == 1;
+  fclose(f);
+  return ok ? SCLET_OK : SCLET_ERR_IO;
+}
+
+int sclet_read_case(const char *dir, const char *suffix, sclet_params *p) {
+  char path[2300];
+  int rc;
+  sclet_params_default(p);
+  snprintf(path, sizeof path, "%s/input%s.ini", dir, suffix);
+  if ((rc = sclet_read_ini(path, p)) != SCLET_OK) return rc;
+  if (p->elastic != 0) {
+    snprintf(path, sizeof path, "%s/elastic_input.txt", dir);
+    if ((rc = sclet_read_elastic_input(path, p)) != SCLET_OK) return rc;
+  }
+  if (p->anisotropic == 1) {
+    snprintf(path, sizeof path, "%s/anisotropic_input.txt", dir);
+    if ((rc = sclet_read_anisotropic_input(path, p)) != SCLET_OK) return rc;
+  }
+  snprintf(path, sizeof path, "%s/landau_input.txt", dir);
+  {
+    FILE *f = fopen(path, "r");
+    if (f) {
+      fclose(f);
+      if ((rc = sclet_read_landau_input(path, p)) != SCLET_OK) return rc;
+    }
+  }
+  return SCLET_OK;
+}
+
+/* read_matrices(), vars.c:375-476: eigenvalues one per token; V and V^-1 row
+ * by row. */
+int sclet_read_eigen(const char *dir, int n, int variant, double *d, double *v, double *vi) {
+  char path[2300];
+  FILE *f;
+  int i, ok = 1;
+  snprintf(path, sizeof path, "%s/d%d%d.dat", dir, variant, n);
+  if (!(f = fopen(path, "r"))) return SCLET_ERR_IO;
+  for (i = 0; i < n && ok; i++) ok &= fscanf(f, "%lf", &d[i]) == 1;
+  fclose(f);
+  snprintf(path, sizeof path, "%s/v%d%d.dat", dir, variant, n);
+  if (!(f = fopen(path, "r"))) return SCLET_ERR_IO;
+  for (i = 0; i < n * n && ok; i++) ok &= fscanf(f, "%lf", &v[i]) == 1;
+  fclose(f);
+  snprintf(path, sizeof path, "%s/vi%d%d.dat", dir, variant, n);
+  if (!(f = fopen(path, "r"))) return SCLET_ERR_IO;
+  for (i = 0; i < n * n && ok; i++) ok &= fscanf(f, "%lf", &vi[i]) == 1;
+  fclose(f);
+  return ok ? SCLET_OK : SCLET_ERR_IO;
+}
+
+/* DST-I: T = V diag(d) V^T for the Dirichlet second difference, eigenvalues
+ * -4 sin^2(k pi / (2(n+1))) in ascending order (k = n .. 1). */
+void sclet_eigen_dirichlet(int n, double *d, double *v, double *vi) {
+  const double pi = 3.14159265358979323846;
+  double s = sqrt(2.0 / (n + 1));
+  int i, j;
+  for (j = 0; j < n; j++) {
+    double k = (double)(n - j);
+    double t = sin(k * pi / (2.0 * (n + 1)));
+    d[j] = -4.0 * t * t;
+  }
+  for (i = 0; i < n; i++)
+    for (j = 0; j < n; j++) {
+      double k = (double)(n - j);
+      double val = s * sin(pi * (double)(i + 1) * k / (n + 1));
+      v[i * n + j] = val;
+      vi[j * n + i] = val;
+    }
+}
+
+static unsigned long long splitmix64(unsigned long long x) {
+  x += 0x9E3779B97F4A7C15ULL;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBULL;
+  return x ^ (x >> 31);
+}
+
+double sclet_seeded_value(unsigned long long seed, int field, long long cell, double lo, double hi) {
+  unsigned long long key = seed * 0xD1B54A32D192ED03ULL + (unsigned long long)(field + 1) * 0xA0761D6478BD642FULL;
+  unsigned long long z = splitmix64(splitmix64((unsigned long long)cell ^ key));
+  double u = (double)(z >> 11) * (1.0 / 9007199254740992.0);
+  return lo + (hi - lo) * u;
+}
+
+int sclet_write_restart(const char *path, int n, const double *block) {
+  FILE *f = fopen(path, "w");
+  int x, y, z;
+  if (!f) return SCLET_ERR_IO;
+  for (z = 2; z < n - 2; z++)
+    for (y = 2; y < n - 2; y++)
+      for (x = 2; x < n - 2; x++) fprintf(f, "%.17g\n", block[((size_t)z * n + y) * n + x]);
+  fclose(f);
+  return SCLET_OK;
+}
+
+int sclet_read_restart(const char *path, int n, double *block) {
+  FILE *f = fopen(path, "r");
+  int x, y, z, ok = 1;
+  if (!f) return SCLET_ERR_IO;
+  for (z = 2; z < n - 2 && ok; z++)
+    for (y = 2; y < n - 2 && ok; y++)
+      for (x = 2; x < n - 2 && ok; x++) ok &= fscanf(f, "%lf", &block[((size_t)z * n + y) * n + x]) == 1;
+  fclose(f);
+  return ok ? SCLET_OK : SCLET_ERR_IO;
+}

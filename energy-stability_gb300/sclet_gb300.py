@@ -1,0 +1,255 @@
+"""Python host side of sclet_gb300: ctypes bindings of the C ABI
+(include/sclet_gb300.h) and a small object wrapper.
+
+The CUDA library must be built (energy-stability_gb300/build_ext.py); if it
+is missing or fails to load, every entry point raises: there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import List, Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsclet_gb300.so")
+
+AC, CH = 0, 1
+FP64, MIXED = 0, 1
+
+_c_dp = ctypes.POINTER(ctypes.c_double)
+
+
+class Params(ctypes.Structure):
+    _fields_ = [
+        ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
+        ("px", ctypes.c_int), ("py", ctypes.c_int), ("pz", ctypes.c_int),
+        ("nghost", ctypes.c_int),
+        ("work_dir", ctypes.c_char * 1024), ("data_dir", ctypes.c_char * 1024),
+        ("dt", ctypes.c_double), ("t_total", ctypes.c_double),
+        ("epn2", ctypes.c_double),
+        ("periodic", ctypes.c_int),
+        ("nac", ctypes.c_int), ("nch", ctypes.c_int),
+        ("restart", ctypes.c_int), ("restart_iter", ctypes.c_int),
+        ("restart_dir", ctypes.c_char * 1024),
+        ("xmin", ctypes.c_double), ("ymin", ctypes.c_double), ("zmin", ctypes.c_double),
+        ("xmax", ctypes.c_double), ("ymax", ctypes.c_double), ("zmax", ctypes.c_double),
+        ("etd2", ctypes.c_int), ("elastic", ctypes.c_int), ("anisotropic", ctypes.c_int),
+        ("kkx", ctypes.c_double), ("kky", ctypes.c_double), ("kkz", ctypes.c_double),
+        ("variable_mobility", ctypes.c_int),
+        ("elastic_scale", ctypes.c_double),
+        ("voigt", ctypes.c_double * 36),
+        ("eigenstrain", ctypes.c_double * 36),
+        ("lambda_file", ctypes.c_double * 36),
+        ("landau", ctypes.c_double * 11),
+    ]
+
+
+class Diag(ctypes.Structure):
+    _fields_ = [("max", ctypes.c_double), ("min", ctypes.c_double), ("vol", ctypes.c_double),
+                ("energy", ctypes.c_double)]
+
+
+# Every entry point of include/sclet_gb300.h with its ctypes signature.
+SIGNATURES = {
+    "sclet_params_default": (None, [ctypes.c_void_p]),
+    "sclet_read_ini": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_void_p]),
+    "sclet_read_elastic_input": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_void_p]),
+    "sclet_read_anisotropic_input": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_void_p]),
+    "sclet_read_landau_input": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_void_p]),
+    "sclet_read_case": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_void_p]),
+    "sclet_read_eigen": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, _c_dp, _c_dp, _c_dp]),
+    "sclet_eigen_dirichlet": (None, [ctypes.c_int, _c_dp, _c_dp, _c_dp]),
+    "sclet_seeded_value": (ctypes.c_double, [ctypes.c_ulonglong, ctypes.c_int, ctypes.c_longlong,
+                                             ctypes.c_double, ctypes.c_double]),
+    "sclet_write_restart": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, _c_dp]),
+    "sclet_read_restart": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, _c_dp]),
+    "sclet_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "sclet_destroy": (None, [ctypes.c_void_p]),
+    "sclet_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+    "sclet_set_eigen": (ctypes.c_int, [ctypes.c_void_p, _c_dp, _c_dp, _c_dp]),
+    "sclet_block_edge": (ctypes.c_int, [ctypes.c_void_p]),
+    "sclet_field_count": (ctypes.c_int, [ctypes.c_void_p]),
+    "sclet_stream": (ctypes.c_void_p, [ctypes.c_void_p]),
+    "sclet_set_field": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _c_dp]),
+    "sclet_get_field": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _c_dp]),
+    "sclet_load_restart": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_char_p]),
+    "sclet_transfer": (ctypes.c_int, [ctypes.c_void_p]),
+    "sclet_elastic_calculate": (ctypes.c_int, [ctypes.c_void_p]),
+    "sclet_calc_rhs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "sclet_etd_update": (ctypes.c_int, [ctypes.c_void_p]),
+    "sclet_etd2_correct": (ctypes.c_int, [ctypes.c_void_p]),
+    "sclet_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "sclet_check_soln": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "sclet_set_energy_tensors": (ctypes.c_int, [ctypes.c_void_p, _c_dp]),
+    "sclet_get_rhs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _c_dp]),
+    "sclet_get_felas": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _c_dp]),
+    "sclet_mode_product": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _c_dp, _c_dp]),
+    "sclet_sync": (ctypes.c_int, [ctypes.c_void_p]),
+    "sclet_time_steps": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
+    "sclet_set_profiling": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "sclet_stage_times": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float),
+                                         ctypes.POINTER(ctypes.c_int), ctypes.c_int]),
+    "sclet_launch_count": (ctypes.c_longlong, [ctypes.c_void_p]),
+}
+
+_LIB = None
+
+
+def lib():
+    """Loads the CUDA library (raises OSError if it is not built)."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise OSError(f"{LIB_PATH} is not built; run energy-stability_gb300/build_ext.py")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+class ScletError(RuntimeError):
+    pass
+
+
+def _dp(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_c_dp)
+
+
+def read_case(case_dir: str, suffix: str) -> Params:
+    p = Params()
+    rc = lib().sclet_read_case(case_dir.encode(), suffix.encode(), ctypes.byref(p))
+    if rc != 0:
+        raise ScletError(f"sclet_read_case({case_dir}, {suffix}) failed with status {rc}")
+    return p
+
+
+def default_params() -> Params:
+    p = Params()
+    lib().sclet_params_default(ctypes.byref(p))
+    return p
+
+
+class Solver:
+    """One device-resident ETD state (a sclet_ctx)."""
+
+    def __init__(self, params: Params, precision: int = FP64, device: int = 0):
+        self.L = lib()
+        h = ctypes.c_void_p()
+        rc = self.L.sclet_create(ctypes.byref(params), precision, device, ctypes.byref(h))
+        if rc != 0:
+            raise ScletError(f"sclet_create failed ({rc}): {self.L.sclet_last_error(None).decode()}")
+        self.h = h
+        self.params = params
+        self.n = self.L.sclet_block_edge(h)
+        self.F = self.L.sclet_field_count(h)
+        self.nac = params.nac
+        self.nch = params.nch
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.sclet_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, rc: int, what: str):
+        if rc != 0:
+            raise ScletError(f"{what} failed ({rc}): {self.L.sclet_last_error(self.h).decode()}")
+
+    def _kind(self, f: int):
+        return (AC, f) if f < self.nac else (CH, f - self.nac)
+
+    def set_fields(self, u: np.ndarray):
+        for f in range(self.F):
+            k, m = self._kind(f)
+            self._ck(self.L.sclet_set_field(self.h, k, m, _dp(np.ascontiguousarray(u[f], dtype=np.float64))),
+                     "set_field")
+
+    def get_fields(self) -> np.ndarray:
+        out = np.zeros((self.F, self.n, self.n, self.n))
+        for f in range(self.F):
+            k, m = self._kind(f)
+            self._ck(self.L.sclet_get_field(self.h, k, m, _dp(out[f])), "get_field")
+        return out
+
+    def load_restart_dir(self, case_dir: str, restart_iter: int = 0):
+        """init_field with restart = 1: ./input/field_iter{it}_{ac|ch}{m}_000.txt"""
+        for f in range(self.F):
+            k, m = self._kind(f)
+            name = f"field_iter{restart_iter}_{'ac' if k == AC else 'ch'}{m}_000.txt"
+            path = os.path.join(case_dir, "input", name)
+            self._ck(self.L.sclet_load_restart(self.h, k, m, path.encode()), "load_restart")
+
+    def set_eigen(self, d: np.ndarray, v: np.ndarray, vi: np.ndarray):
+        self._ck(self.L.sclet_set_eigen(self.h, _dp(np.ascontiguousarray(d)), _dp(np.ascontiguousarray(v)),
+                                        _dp(np.ascontiguousarray(vi))), "set_eigen")
+
+    def transfer(self):
+        self._ck(self.L.sclet_transfer(self.h), "transfer")
+
+    def elastic(self):
+        self._ck(self.L.sclet_elastic_calculate(self.h), "elastic_calculate")
+
+    def calc_rhs(self, slot: int = 1):
+        self._ck(self.L.sclet_calc_rhs(self.h, slot), "calc_rhs")
+
+    def get_rhs(self, slot: int = 1) -> np.ndarray:
+        out = np.zeros((self.F, self.n, self.n, self.n))
+        for f in range(self.F):
+            k, m = self._kind(f)
+            self._ck(self.L.sclet_get_rhs(self.h, slot, k, m, _dp(out[f])), "get_rhs")
+        return out
+
+    def get_felas(self) -> np.ndarray:
+        out = np.zeros((self.nac, self.n, self.n, self.n))
+        for m in range(self.nac):
+            self._ck(self.L.sclet_get_felas(self.h, m, _dp(out[m])), "get_felas")
+        return out
+
+    def step(self, k: int = 1):
+        self._ck(self.L.sclet_step(self.h, k), "step")
+
+    def sync(self):
+        self._ck(self.L.sclet_sync(self.h), "sync")
+
+    def check_soln(self, form: int = 1) -> np.ndarray:
+        d = (Diag * self.F)()
+        self._ck(self.L.sclet_check_soln(self.h, form, d), "check_soln")
+        return np.array([[x.max, x.min, x.vol, x.energy] for x in d])
+
+    def set_energy_tensors(self, lam: np.ndarray):
+        self._ck(self.L.sclet_set_energy_tensors(self.h, _dp(np.ascontiguousarray(lam, dtype=np.float64))),
+                 "set_energy_tensors")
+
+    def mode_product(self, a: np.ndarray, inverse: bool = False) -> np.ndarray:
+        out = np.zeros_like(a)
+        self._ck(self.L.sclet_mode_product(self.h, int(inverse), _dp(np.ascontiguousarray(a)), _dp(out)),
+                 "mode_product")
+        return out
+
+    def time_steps(self, k: int) -> float:
+        ms = ctypes.c_float()
+        self._ck(self.L.sclet_time_steps(self.h, k, ctypes.byref(ms)), "time_steps")
+        return ms.value
+
+    def set_profiling(self, on: bool):
+        self._ck(self.L.sclet_set_profiling(self.h, int(on)), "set_profiling")
+
+    def stage_times(self, nclasses: int = 5):
+        ms = (ctypes.c_float * nclasses)()
+        ln = (ctypes.c_int * nclasses)()
+        self._ck(self.L.sclet_stage_times(self.h, ms, ln, nclasses), "stage_times")
+        return list(ms), list(ln)
+
+    def launch_count(self) -> int:
+        return int(self.L.sclet_launch_count(self.h))

@@ -1,0 +1,192 @@
+/*
+ * sclet_gb300 -- C ABI of the GB300 (sm_103a) implementation of the ScLETD
+ * exponential-time-differencing step (beta->omega / beta->alpha phase field).
+ *
+ * The reference keeps its state in process globals and exits on error; this
+ * boundary keeps the same step sequence and file formats behind an opaque
+ * context that owns the device-resident state, and returns an int status
+ * (SCLET_OK = 0) instead of calling exit().  Plain pointers and sizes only.
+ *
+ * Each entry point names the reference routine it replaces
+ * (paths relative to the reference project).
+ *
+ * Field blocks are n*n*n doubles (n = N + 4: N owned cells plus two ghost
+ * layers per side), index z*n*n + y*n + x, exactly the reference's
+ * ac[m].fieldE / ch[m].fieldCI layout (source_beta_to_omega/src/ScLETD.h:60-96).
+ * Field kinds: SCLET_AC (non-conserved order parameters eta_m, m < nac) and
+ * SCLET_CH (conserved concentrations c_m, m < nch).
+ */
+#ifndef SCLET_GB300_H
+#define SCLET_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define SCLET_OK 0
+#define SCLET_ERR_ARG 1         /* bad argument or unsupported size          */
+#define SCLET_ERR_IO 2          /* input file missing or malformed           */
+#define SCLET_ERR_CUDA 3        /* CUDA runtime error (message: last_error)  */
+#define SCLET_ERR_UNSUPPORTED 4 /* option the reference path does not take   */
+#define SCLET_ERR_NOMEM 5       /* device allocation failed                  */
+#define SCLET_ERR_TIMEOUT 6     /* a bounded device wait gave up             */
+#define SCLET_ERR_NONFINITE 7   /* a diagnostic found NaN/Inf in the state   */
+
+#define SCLET_AC 0
+#define SCLET_CH 1
+
+/* Arithmetic of the step.  SCLET_FP64: every stage in FP64 (the plain form,
+ * checked against the reference).  SCLET_MIXED: eigenbasis products as
+ * split-precision tensor-core products with FP32 accumulation, stencils and
+ * FFT in FP32, diagnostics and mass correction in FP64. */
+#define SCLET_FP64 0
+#define SCLET_MIXED 1
+
+typedef struct sclet_ctx sclet_ctx;
+
+/* Everything the reference reads from its input files. */
+typedef struct sclet_params {
+  /* input<suffix>.ini, positional (source_beta_to_omega/src/ScLETD.c:16-34) */
+  int nx, ny, nz;          /* local block incl. ghosts; must be equal here   */
+  int px, py, pz;          /* process grid; 1,1,1 on one GPU                 */
+  int nghost;              /* 2                                              */
+  char work_dir[1024];
+  char data_dir[1024];
+  double dt, t_total;
+  double epn2;
+  int periodic;            /* 1                                              */
+  int nac, nch;
+  int restart, restart_iter;
+  char restart_dir[1024];
+  double xmin, ymin, zmin, xmax, ymax, zmax;
+  int etd2;                /* 1: second-order corrector                      */
+  int elastic;             /* 0 none, 1 elastic force on the AC fields       */
+  int anisotropic;         /* 1: explicit div(lambda grad eta) term          */
+  double kkx, kky, kkz;
+  int variable_mobility;   /* must be 0 (constant-mobility CH)               */
+  /* elastic_input.txt (source_beta_to_omega/src/elastic.c:349-439) */
+  double elastic_scale;
+  double voigt[36];        /* 6x6, order 11,22,33,23,13,12                   */
+  double eigenstrain[4][9];
+  /* anisotropic_input.txt (source_beta_to_omega/src/anisotropic.c:630-674):
+   * the file tensors; the step uses diag(kk) - lambda_file */
+  double lambda_file[4][9];
+  /* physics plugin constants (replaces the compile-time constants of
+   * source_beta_to_omega/src/formula.c:9-38): a2 a4 a6 g th c0 A LE KE LCI KCI */
+  double landau[11];
+} sclet_params;
+
+/* Diagnostics of one state (check_soln_new, field.c:407-678), per field. */
+typedef struct sclet_diag {
+  double max, min, vol, energy;
+} sclet_diag;
+
+/* ---- input files (host only; no GPU needed) ---------------------------- */
+/* Defaults of the 64^3 beta->omega case; all file readers start from them. */
+void sclet_params_default(sclet_params *p);
+/* main()'s ini parse, ScLETD.c:16-34 */
+int sclet_read_ini(const char *path, sclet_params *p);
+/* elastic_input(), elastic.c:349-439 */
+int sclet_read_elastic_input(const char *path, sclet_params *p);
+/* anisotropic_input(), anisotropic.c:630-674 (file tensors only) */
+int sclet_read_anisotropic_input(const char *path, sclet_params *p);
+/* init_KL() constants of the physics plugin (formula.c:9-19); 11 numbers */
+int sclet_read_landau_input(const char *path, sclet_params *p);
+/* All of the above from a run directory, as main() does (ScLETD.c:15-72). */
+int sclet_read_case(const char *dir, const char *suffix, sclet_params *p);
+/* One eigen variant as read_matrices() reads it (vars.c:370-476):
+ * d<k><n>.dat (n values), v<k><n>.dat and vi<k><n>.dat (n x n, row by row).
+ * d, v, vi receive n, n*n, n*n doubles; v and vi row-major. */
+int sclet_read_eigen(const char *dir, int n, int variant, double *d, double *v, double *vi);
+/* Closed-form Dirichlet-Dirichlet basis (variant 3, the one a periodic single
+ * block selects in read_matrices, vars.c:488-582): the DST-I, eigenvalues
+ * ascending, v = vi^T = vi.  Same output layout as sclet_read_eigen. */
+void sclet_eigen_dirichlet(int n, double *d, double *v, double *vi);
+/* Seeded initial value of cell (x, y, z) of field f, uniform in [lo, hi):
+ * SplitMix64 on (seed, field, owned-cell index z*N*N + y*N + x). */
+double sclet_seeded_value(unsigned long long seed, int field, long long cell, double lo, double hi);
+/* Writes the interior of a field block as restart text (write_field,
+ * field.c:156-174) / reads it (read_field, field.c:137-154). */
+int sclet_write_restart(const char *path, int n, const double *block);
+int sclet_read_restart(const char *path, int n, double *block);
+
+/* ---- context ----------------------------------------------------------- */
+/* alloc_vars (vars.c:166-300), init_para (vars.c:58-157), read_matrices
+ * (vars.c:361-591; closed-form variant 3 unless sclet_set_eigen is called),
+ * ac_init_phi/ch_init_phi (vars.c:302-359) and elastic_init (elastic.c:607)
+ * on device `device`.  Fields start at zero. */
+int sclet_create(const sclet_params *p, int precision, int device, sclet_ctx **out);
+/* dealloc_vars (vars.c:593-732), elastic_finish (elastic.c:276-300) */
+void sclet_destroy(sclet_ctx *ctx);
+/* Last error message of this context (or of the last failed create). */
+const char *sclet_last_error(const sclet_ctx *ctx);
+/* Replaces the per-axis eigen data (all three axes use the same n-point
+ * basis, as read_matrices does for nx = ny = nz): d (n, unscaled; divided by
+ * h^2 here as vars.c:512 does), v and vi row-major n x n. */
+int sclet_set_eigen(sclet_ctx *ctx, const double *d, const double *v, const double *vi);
+/* Block edge n, field count, and the CUDA stream the context runs on. */
+int sclet_block_edge(const sclet_ctx *ctx);
+int sclet_field_count(const sclet_ctx *ctx);
+void *sclet_stream(const sclet_ctx *ctx);
+
+/* ---- state transfer (host <-> device) ---------------------------------- */
+int sclet_set_field(sclet_ctx *ctx, int kind, int m, const double *block);
+int sclet_get_field(sclet_ctx *ctx, int kind, int m, double *block);
+/* init_field with restart = 1 (field.c:743-755): interior from text. */
+int sclet_load_restart(sclet_ctx *ctx, int kind, int m, const char *path);
+
+/* ---- step routines (the reference's time-loop pieces) ------------------ */
+/* transfer(), trans.c:1939-1996: ghost exchange of every field. */
+int sclet_transfer(sclet_ctx *ctx);
+/* elastic_calculate(), elastic.c:689-763 (ELASTIC == 1). */
+int sclet_elastic_calculate(sclet_ctx *ctx);
+/* calc_mu() + ac_calc_FU / ch_calc_FU for every field (trans.c:1998-2013,
+ * calc.c:8-68, 70-487) into slot 1 (fieldE1/fieldCI1) or 2 (fieldE2/...). */
+int sclet_calc_rhs(sclet_ctx *ctx, int slot);
+/* PUX/PUY/PUZ + ac_updateU_new/ch_updateU_new + zxy_xyz + back transform for
+ * every field (ScLETD.c:105-142, calc.c:489-535, 585-684). */
+int sclet_etd_update(sclet_ctx *ctx);
+/* ETD2 corrector: prepare_U1_new .. correct_U_new (ScLETD.c:159-188,
+ * calc.c:537-583), after transfer/elastic/calc_rhs(slot 2). */
+int sclet_etd2_correct(sclet_ctx *ctx);
+/* `nsteps` passes of the time-loop body (ScLETD.c:86-190), asynchronous on
+ * the context's stream. */
+int sclet_step(sclet_ctx *ctx, int nsteps);
+/* check_soln_new(), field.c:407-678: diagnostics of the current state
+ * (compensated FP64 reduction on the device; out has field-count entries,
+ * AC fields first).  energy_form 0: the reference's hard-coded polynomial and
+ * its per-kind energies; 1: the plugin's total free energy. */
+int sclet_check_soln(sclet_ctx *ctx, int energy_form, sclet_diag *out);
+/* Gradient tensors used by the energy (per AC field, 3x3 row-major).  The
+ * default is the gradient operator of the dynamics: lambda_file when
+ * anisotropic, else diag(kk). */
+int sclet_set_energy_tensors(sclet_ctx *ctx, const double *lam /* nac*9 */);
+
+/* ---- inspection (host buffers) ------------------------------------------ */
+/* fieldE1/fieldE2 of one field, and the elastic force felas. */
+int sclet_get_rhs(sclet_ctx *ctx, int slot, int kind, int m, double *block);
+int sclet_get_felas(sclet_ctx *ctx, int m, double *block);
+/* One mode-n product with layout rotation (one PUX/PUY/PUZ contraction,
+ * calc.c:631-684): out[b + n*c + n*n*a'] = sum_a M(a', a) in[a + n*b + n*n*c]
+ * with M = V^-1 (inverse = 0) or V (inverse = 1) of axis 0. */
+int sclet_mode_product(sclet_ctx *ctx, int inverse, const double *in, double *out);
+
+/* ---- synchronisation and timing ---------------------------------------- */
+int sclet_sync(sclet_ctx *ctx);
+/* Runs `nsteps` steps between two CUDA events on the context's stream and
+ * returns the elapsed milliseconds. */
+int sclet_time_steps(sclet_ctx *ctx, int nsteps, float *ms);
+/* Per-kernel-class timing of the last sclet_time_steps call when profiling
+ * was enabled with sclet_set_profiling(ctx, 1): ms[k] for classes
+ * 0 mode-n products, 1 right-hand sides, 2 FFT/elastic, 3 halo, 4 diagnostics;
+ * launches[k] kernel launches. */
+int sclet_set_profiling(sclet_ctx *ctx, int on);
+int sclet_stage_times(const sclet_ctx *ctx, float *ms, int *launches, int nclasses);
+/* Kernel launches issued by this context so far. */
+long long sclet_launch_count(const sclet_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
