@@ -1,0 +1,290 @@
+"""Benchmark of the ScLETD ETD step on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|mixed]
+                    [--impl reference] [--size N3EDGE]
+
+Workload: the beta->alpha coupled case -- one conserved concentration
+c = 0.5 + U(-0.02, 0.02) and four order parameters U(-0.01, 0.01) on a 192^3
+periodic grid (block edge 196), Landau 2-4-6 with cross term 1.5 and c-eta
+coupling 0.8, anisotropic gradient tensors diag(0.5, 0.5, 0.3) with
+stabiliser kk = 0.5, cubic elasticity C11/C12/C44 = 1.0/0.6/0.4 with four
+<111> eigenstrains, dt = 0.005, first-order ETD.  Synthetic seeded data.
+
+A step is one pass of the reference's time loop (ghost exchange, elastic
+force, right-hand sides, eigenbasis transforms and update) plus the
+diagnostics check_soln_new it runs every pass.  `value` is cell-updates/s
+(N^3 owned cells x steps / time) with the state resident in HBM; `e2e` is the
+same through the C ABI with the fields copied in from pinned host memory and
+copied back out (with the diagnostics) every step.
+
+--impl reference times the reference's CPU path (the C restatement of
+oracle/, the reference's own build cannot run on this host) on all host
+cores, on the same workload.
+
+Several GPUs (torchrun): independent replicas with their own seeds (the path
+has no data exchange between replicas); value = all ranks' cell updates /
+slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "energy-stability_gb300"), os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import cases  # noqa: E402
+
+METRIC = "cell-updates/s on 1 GB300: mixed/learned vs plain FP64 at ≤1e-5 rel L2"
+UNIT = "cell-updates/s"
+FP64_PEAK_TFLOPS = 1.20  # measured FP64 FMA throughput of this machine's GB300 (profiles/gb300_throughput_probe.md)
+
+
+def workload(big_n: int, seed: int) -> cases.Case:
+    return cases.Case(
+        big_n=big_n, nac=4, nch=1, etd2=0, elastic=1, anisotropic=1, kk=(0.5, 0.5, 0.5),
+        lambdas=[np.diag([0.5, 0.5, 0.3]) for _ in range(4)], dt=0.005, epn2=1.0, steps=2000,
+        eta_range=(-0.01, 0.01), c_range=(0.48, 0.52), seed=seed, suffix="bench")
+
+
+def workload_name(big_n: int) -> str:
+    return (f"beta-alpha coupled CH + 4 AC, {big_n}^3 periodic (block {big_n + 4}^3), Landau 2-4-6, "
+            f"anisotropic, cubic elasticity, ETD1, dt 0.005")
+
+
+def block_fields(case: cases.Case) -> np.ndarray:
+    n = case.n
+    out = np.zeros((case.nac + case.nch, n, n, n))
+    for f, (_, _, vals) in enumerate(case.initial_fields()):
+        out[f, 2:-2, 2:-2, 2:-2] = vals
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.out = tempfile.NamedTemporaryFile(mode="w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.out, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=10)
+
+    def summary(self):
+        try:
+            with open(self.out.name) as fp:
+                rows = [r.split(",") for r in fp.read().strip().splitlines() if r.strip()]
+        except Exception:
+            rows = []
+        os.unlink(self.out.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if len(r) > 5 + i and "Active" in r[5 + i]
+                          and "Not" not in r[5 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return world, rank, local
+
+
+def dist_max(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def cpu_oracle_rate(case: cases.Case, steps: int, warmup: int):
+    """Times the C oracle (all host threads) on the case; returns
+    (cell-updates/s, cores, seconds)."""
+    import oracle_py
+    if not os.path.exists(oracle_py.LIB_PATH):
+        oracle_py.build()
+    with tempfile.TemporaryDirectory() as td:
+        cases.write_case(case, td, fields=False)
+        p = oracle_py.load_case_params(td, case.suffix, block_fields(case))
+        o = oracle_py.Oracle(p)
+        o.step(warmup)
+        t0 = time.perf_counter()
+        o.step(steps)
+        o.check_soln()
+        dt = time.perf_counter() - t0
+    return case.big_n ** 3 * steps / dt, o.threads(), dt
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    case = workload(args.size, seed=1000)
+    rate, cores, secs = cpu_oracle_rate(case, args.steps, args.warmup)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * secs / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": workload_name(args.size), "cells_per_step": args.size ** 3},
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} full steps of the workload after {args.warmup} warm-up steps "
+                                   f"(C restatement of the reference's step, OpenMP on {cores} threads)"},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, world, rank, local):
+    import sclet_gb300 as sg
+    sg.lib()
+    precision = {"fp64": sg.FP64, "mixed": sg.MIXED}[args.precision]
+    case = workload(args.size, seed=1000 + rank)
+    n, F = case.n, case.nac + case.nch
+    with tempfile.TemporaryDirectory() as td:
+        cases.write_case(case, td, eigen=False, fields=False)
+        params = sg.read_case(td, case.suffix)
+    s = sg.Solver(params, precision, device=local)
+    u0 = block_fields(case)
+    s.set_fields(u0)
+    # warm-up
+    s.step(args.warmup)
+    s.check_soln()
+    # device-resident timed region: K steps, diagnostics every step
+    dist_barrier(world)
+    l0 = s.launch_count()
+    with ClockSampler(local) as clk:
+        s.sync()
+        t0 = time.perf_counter()
+        ms = 0.0
+        for _ in range(args.steps):
+            ms += s.time_steps(1)
+            s.check_soln()
+        wall = time.perf_counter() - t0
+    launches = s.launch_count() - l0
+    ms_max = dist_max(ms, world)
+    cells = case.big_n ** 3 * args.steps * world
+    value = cells / (ms_max / 1000.0)
+    # end to end through the C ABI with host buffers
+    pin_in = sg.PinnedArray((F, n, n, n))
+    pin_out = sg.PinnedArray((F, n, n, n))
+    pin_in.array[...] = u0
+    dist_barrier(world)
+    s.sync()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s.set_fields(pin_in.array)
+        s.step(1)
+        s.check_soln()
+        for f in range(F):
+            k, m = s._kind(f)
+            s._ck(s.L.sclet_get_field(s.h, k, m, sg._dp(pin_out.array[f])), "get_field")
+    e2e_s = dist_max(time.perf_counter() - t0, world)
+    e2e_value = cells / e2e_s
+    bytes_step = F * n ** 3 * 8
+    # per-stage timing for the roofline of the dominant kernel class
+    s.set_profiling(True)
+    s.time_steps(2)
+    stage_ms, stage_launches = s.stage_times(5)
+    s.set_profiling(False)
+    s.close()
+    pin_in.free()
+    pin_out.free()
+    if rank != 0:
+        return
+    flops_products = 2.0 * n ** 4 * 9 * F * 2  # 9 rotating products per field per ETD1 step, 2 steps
+    achieved = flops_products / (stage_ms[0] / 1000.0) / 1e12
+    roofline = {"bound": "fp64", "kernel": "modeprod_f64 (eigenbasis mode-n products)",
+                "achieved": achieved, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s", "frac": achieved / FP64_PEAK_TFLOPS,
+                "traffic": None, "peak_source": "measured FP64 FMA probe on GB300",
+                "avg_launch_ms": stage_ms[0] / max(stage_launches[0], 1),
+                "stage_ms": dict(zip(["products", "rhs", "elastic", "halo", "diagnostics"], stage_ms)),
+                "stage_launches": dict(zip(["products", "rhs", "elastic", "halo", "diagnostics"], stage_launches))}
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        small = workload(args.size, seed=1000)
+        rate, cores, secs = cpu_oracle_rate(small, args.cpu_steps, 0)
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{args.cpu_steps} full steps of the same workload, C restatement of the reference's step "
+                         f"on {cores} host threads ({secs:.1f} s)"}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if precision == sg.FP64 else "bf16x3/f32", "data": "synthetic",
+        "config": {"workload": workload_name(args.size), "cells_per_step": args.size ** 3,
+                   "precision": args.precision, "l2": "inputs larger than L2 (state of a step > 129 MB)",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": bytes_step, "d2h_bytes_per_step": bytes_step},
+        "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--size", type=int, default=192, help="physical grid edge N")
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_gpu(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

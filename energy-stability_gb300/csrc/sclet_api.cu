@@ -552,6 +552,16 @@ int sclet_time_steps(sclet_ctx *ctx, int nsteps, float *ms) {
   return rc;
 }
 
+void *sclet_host_alloc(size_t bytes) {
+  void *p = nullptr;
+  if (cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
+  return p;
+}
+
+void sclet_host_free(void *ptr) {
+  if (ptr) cudaFreeHost(ptr);
+}
+
 int sclet_stage_times(const sclet_ctx *ctx, float *ms, int *launches, int nclasses) {
   for (int k = 0; k < nclasses && k < 8; k++) {
     ms[k] = ctx->stage_ms[k];

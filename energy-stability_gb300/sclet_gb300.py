@@ -92,6 +92,8 @@ SIGNATURES = {
     "sclet_stage_times": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float),
                                          ctypes.POINTER(ctypes.c_int), ctypes.c_int]),
     "sclet_launch_count": (ctypes.c_longlong, [ctypes.c_void_p]),
+    "sclet_host_alloc": (ctypes.c_void_p, [ctypes.c_size_t]),
+    "sclet_host_free": (None, [ctypes.c_void_p]),
 }
 
 _LIB = None
@@ -114,6 +116,24 @@ def lib():
 
 class ScletError(RuntimeError):
     pass
+
+
+class PinnedArray:
+    """numpy view of page-locked host memory (sclet_host_alloc)."""
+
+    def __init__(self, shape, dtype=np.float64):
+        self.nbytes = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        self.ptr = lib().sclet_host_alloc(self.nbytes)
+        if not self.ptr:
+            raise MemoryError("sclet_host_alloc failed")
+        buf = (ctypes.c_char * self.nbytes).from_address(self.ptr)
+        self.array = np.frombuffer(buf, dtype=dtype).reshape(shape)
+
+    def free(self):
+        if self.ptr:
+            self.array = None
+            lib().sclet_host_free(self.ptr)
+            self.ptr = None
 
 
 def _dp(a: np.ndarray):

@@ -19,6 +19,8 @@
 #ifndef SCLET_GB300_H
 #define SCLET_GB300_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -185,6 +187,11 @@ int sclet_set_profiling(sclet_ctx *ctx, int on);
 int sclet_stage_times(const sclet_ctx *ctx, float *ms, int *launches, int nclasses);
 /* Kernel launches issued by this context so far. */
 long long sclet_launch_count(const sclet_ctx *ctx);
+/* Page-locked host buffers for the field blocks (no reference counterpart:
+ * the reference's arrays are plain host memory, vars.c:166-300).  Copies
+ * from/to these overlap nothing else but run at full link speed. */
+void *sclet_host_alloc(size_t bytes);
+void sclet_host_free(void *ptr);
 
 #ifdef __cplusplus
 }

@@ -179,7 +179,7 @@ class Case:
         return out
 
 
-def write_case(case: Case, dirpath: str, eigen: bool = True) -> None:
+def write_case(case: Case, dirpath: str, eigen: bool = True, fields: bool = True) -> None:
     os.makedirs(os.path.join(dirpath, "input"), exist_ok=True)
     os.makedirs(os.path.join(dirpath, "output"), exist_ok=True)
     os.makedirs(os.path.join(dirpath, "restart"), exist_ok=True)
@@ -211,7 +211,7 @@ def write_case(case: Case, dirpath: str, eigen: bool = True) -> None:
             fp.write("\n")
     with open(os.path.join(dirpath, "landau_input.txt"), "w") as fp:
         fp.write(" ".join(repr(float(x)) for x in case.landau) + "\n")
-    for kind, m, vals in case.initial_fields():
+    for kind, m, vals in (case.initial_fields() if fields else []):
         with open(os.path.join(dirpath, "input", f"field_iter0_{kind}{m}_000.txt"), "w") as fp:
             np.savetxt(fp, vals.reshape(-1), fmt="%.17g")
     if eigen:

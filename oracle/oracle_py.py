@@ -69,8 +69,9 @@ def _read_numbers(path: str):
         return [float(t) for t in fp.read().replace(",", " ").split()]
 
 
-def load_case(case_dir: str, suffix: str) -> Dict:
-    """Parses a run directory (ini: source_beta_to_omega/src/ScLETD.c:16-34)."""
+def load_case(case_dir: str, suffix: str, fields=None) -> Dict:
+    """Parses a run directory (ini: source_beta_to_omega/src/ScLETD.c:16-34).
+    `fields` (F, n, n, n) replaces the restart files as initial state."""
     with open(os.path.join(case_dir, f"input{suffix}.ini")) as fp:
         lines = [ln.strip() for ln in fp if ln.strip()]
     nums = lambda s: [float(t) for t in s.replace(",", " ").split()]
@@ -97,11 +98,19 @@ def load_case(case_dir: str, suffix: str) -> Dict:
         lam_file[: p["nac"]] = np.array(an[: 9 * p["nac"]]).reshape(p["nac"], 3, 3)
     p["lam_file"] = lam_file
     p["landau"] = _read_numbers(os.path.join(case_dir, "landau_input.txt"))
-    # eigen data of the Dirichlet-Dirichlet variant (id 3, src/vars.c:488-582)
-    d = np.loadtxt(os.path.join(case_dir, f"d3{n}.dat"))
-    v = np.loadtxt(os.path.join(case_dir, f"v3{n}.dat"))
-    vi = np.loadtxt(os.path.join(case_dir, f"vi3{n}.dat"))
+    # eigen data of the Dirichlet-Dirichlet variant (id 3, src/vars.c:488-582):
+    # the case's files when written, else the closed form
+    if os.path.exists(os.path.join(case_dir, f"d3{n}.dat")):
+        d = np.loadtxt(os.path.join(case_dir, f"d3{n}.dat"))
+        v = np.loadtxt(os.path.join(case_dir, f"v3{n}.dat"))
+        vi = np.loadtxt(os.path.join(case_dir, f"vi3{n}.dat"))
+    else:
+        import cases
+        d, v, vi = cases.eigen_variant(n, 3)
     p["d"], p["v"], p["vi"] = d, v, vi
+    if fields is not None:
+        p["fields"] = np.ascontiguousarray(fields, dtype=np.float64)
+        return p
     fields = []
     for kind, cnt in (("ac", p["nac"]), ("ch", p["nch"])):
         for m in range(cnt):
@@ -111,6 +120,10 @@ def load_case(case_dir: str, suffix: str) -> Dict:
             fields.append(blk)
     p["fields"] = np.stack(fields)
     return p
+
+
+def load_case_params(case_dir: str, suffix: str, fields) -> Dict:
+    return load_case(case_dir, suffix, fields=fields)
 
 
 class Oracle:
@@ -151,7 +164,12 @@ class Oracle:
             self.lib.orc_compute_bn(ctypes.c_int(big_n), _ptr(np.ascontiguousarray(p["voigt"].reshape(-1))),
                                     _ptr(np.ascontiguousarray(p["eps"].reshape(-1))), _ptr(self.bn))
             c.bn = _ptr(self.bn)
-        elam = lam.copy() if p["anisotropic"] else np.zeros((4, 3, 3))
+        # energy tensors: the gradient operator of the dynamics (the file
+        # tensors when ANISOTROPIC, else diag(kk)); the reference's own
+        # check_soln_new uses diag(kk) - file tensor (set_energy_tensors)
+        elam = np.zeros((4, 3, 3))
+        for m in range(p["nac"]):
+            elam[m] = p["lam_file"][m] if p["anisotropic"] else np.diag(p["kk"])
         for i, v in enumerate(elam.reshape(-1)):
             c.elam[i] = v
         c.energy_form = energy_form
