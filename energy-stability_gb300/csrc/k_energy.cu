@@ -162,30 +162,54 @@ __global__ void __launch_bounds__(EB) energy_partial_kernel(Phys ph, const T *__
   }
 }
 
-__global__ void energy_final_kernel(Phys ph, int form, const double *__restrict__ part, int npart, double *__restrict__ out) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  const int F = ph.F;
+// Final reduction over the block records: one block; each thread folds a
+// fixed strided subset of the records, then a fixed-shape tree (deterministic).
+__global__ void __launch_bounds__(EB) energy_final_kernel(Phys ph, int form, const double *__restrict__ part, int npart,
+                                                          double *__restrict__ out) {
+  const int F = ph.F, L = rec_len(F);
   const double h3 = ph.h[0] * ph.h[1] * ph.h[2];
-  KS eac = {0, 0}, ech = {0, 0};
-  for (int b = 0; b < npart; b++) {
-    const double *r = part + (long long)b * rec_len(F);
-    eac = ks_merge(eac, KS{r[4 * F], r[4 * F + 1]});
-    ech = ks_merge(ech, KS{r[4 * F + 2], r[4 * F + 3]});
-  }
-  for (int f = 0; f < F; f++) {
-    double mx = -1.0e30, mn = 1.0e30;
-    KS vol = {0, 0};
-    for (int b = 0; b < npart; b++) {
-      const double *r = part + (long long)b * rec_len(F);
-      mx = fmax(mx, r[4 * f]);
-      mn = fmin(mn, r[4 * f + 1]);
-      vol = ks_merge(vol, KS{r[4 * f + 2], r[4 * f + 3]});
+  __shared__ double sa[EB], sb[EB];
+  __shared__ double res[4 * MAXF + 4];
+  // quantities: per field max (0), min (1), vol (2); then eng_ac, eng_ch
+  const int nq = 3 * F + 2;
+  for (int q = 0; q < nq; q++) {
+    const int f = q < 3 * F ? q / 3 : -1, kind = q < 3 * F ? q % 3 : 3 + (q - 3 * F);
+    double m = kind == 0 ? -1.0e30 : (kind == 1 ? 1.0e30 : 0.0);
+    KS k = {0, 0};
+    for (int b = threadIdx.x; b < npart; b += EB) {
+      const double *r = part + (long long)b * L;
+      if (kind == 0) m = fmax(m, r[4 * f]);
+      else if (kind == 1) m = fmin(m, r[4 * f + 1]);
+      else if (kind == 2) k = ks_merge(k, KS{r[4 * f + 2], r[4 * f + 3]});
+      else if (kind == 3) k = ks_merge(k, KS{r[4 * F], r[4 * F + 1]});
+      else k = ks_merge(k, KS{r[4 * F + 2], r[4 * F + 3]});
     }
-    out[4 * f] = mx;
-    out[4 * f + 1] = mn;
-    out[4 * f + 2] = (vol.s + vol.c) * h3;
-    double e = (form == 0 && f >= ph.nac) ? (ech.s + ech.c) : (eac.s + eac.c);
-    out[4 * f + 3] = e * h3;
+    sa[threadIdx.x] = kind < 2 ? m : k.s;
+    sb[threadIdx.x] = k.c;
+    __syncthreads();
+    for (int w = EB / 2; w > 0; w >>= 1) {
+      if (threadIdx.x < w) {
+        if (kind == 0) sa[threadIdx.x] = fmax(sa[threadIdx.x], sa[threadIdx.x + w]);
+        else if (kind == 1) sa[threadIdx.x] = fmin(sa[threadIdx.x], sa[threadIdx.x + w]);
+        else {
+          KS x = ks_merge(KS{sa[threadIdx.x], sb[threadIdx.x]}, KS{sa[threadIdx.x + w], sb[threadIdx.x + w]});
+          sa[threadIdx.x] = x.s;
+          sb[threadIdx.x] = x.c;
+        }
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) res[q] = kind < 2 ? sa[0] : sa[0] + sb[0];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    for (int f = 0; f < F; f++) {
+      out[4 * f] = res[3 * f];
+      out[4 * f + 1] = res[3 * f + 1];
+      out[4 * f + 2] = res[3 * f + 2] * h3;
+      double e = (form == 0 && f >= ph.nac) ? res[3 * F + 1] : res[3 * F];
+      out[4 * f + 3] = e * h3;
+    }
   }
 }
 
@@ -200,7 +224,7 @@ cudaError_t launch_check_soln(const Phys &ph, const T *u, const double *elam, in
                               double *out, cudaStream_t s) {
   if (ph.F > MAXF) return cudaErrorInvalidValue;
   energy_partial_kernel<T><<<npart, EB, 0, s>>>(ph, u, elam, form, partials);
-  energy_final_kernel<<<1, 32, 0, s>>>(ph, form, partials, npart, out);
+  energy_final_kernel<<<1, EB, 0, s>>>(ph, form, partials, npart, out);
   launch_counter() += 2;
   return cudaGetLastError();
 }

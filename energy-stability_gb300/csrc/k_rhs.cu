@@ -24,6 +24,8 @@ template <typename T>
 struct P {
   int n, nac, nch, F, aniso, elastic;
   T epn2, hx, hy, hz, LE, KE, LCI, KCI, es;
+  T ih2x, ih2y, ih2z;   // 1 / h^2 per axis
+  T i2hx, i2hy, i2hz;   // 1 / (2 h) per axis
   T a2, a4, a6, g, th, c0, A;
   T lam[4][9];
 };
@@ -33,6 +35,9 @@ static P<T> to_p(const Phys &ph) {
   P<T> p;
   p.n = ph.n; p.nac = ph.nac; p.nch = ph.nch; p.F = ph.F; p.aniso = ph.anisotropic; p.elastic = ph.elastic;
   p.epn2 = (T)ph.epn2; p.hx = (T)ph.h[0]; p.hy = (T)ph.h[1]; p.hz = (T)ph.h[2];
+  p.ih2x = (T)(1.0 / (ph.h[0] * ph.h[0])); p.ih2y = (T)(1.0 / (ph.h[1] * ph.h[1]));
+  p.ih2z = (T)(1.0 / (ph.h[2] * ph.h[2]));
+  p.i2hx = (T)(0.5 / ph.h[0]); p.i2hy = (T)(0.5 / ph.h[1]); p.i2hz = (T)(0.5 / ph.h[2]);
   p.LE = (T)ph.LE; p.KE = (T)ph.KE; p.LCI = (T)ph.LCI; p.KCI = (T)ph.KCI; p.es = (T)ph.elastic_scale;
   p.a2 = (T)ph.a2; p.a4 = (T)ph.a4; p.a6 = (T)ph.a6; p.g = (T)ph.g; p.th = (T)ph.th; p.c0 = (T)ph.c0; p.A = (T)ph.A;
   for (int m = 0; m < 4; m++)
@@ -69,7 +74,7 @@ __device__ inline T grad_comp(const P<T> &p, const T *__restrict__ u, const T *l
   T al = x > 0 ? u[L3(n, z, y, x - 1)] : (T)0, ar = x < n - 1 ? u[L3(n, z, y, x + 1)] : (T)0;
   T at = y > 0 ? u[L3(n, z, y - 1, x)] : (T)0, ab = y < n - 1 ? u[L3(n, z, y + 1, x)] : (T)0;
   T af = z > 0 ? u[L3(n, z - 1, y, x)] : (T)0, ak = z < n - 1 ? u[L3(n, z + 1, y, x)] : (T)0;
-  T gx = (ar - al) / ((T)2 * p.hx), gy = (at - ab) / ((T)2 * p.hy), gz = (af - ak) / ((T)2 * p.hz);
+  T gx = (ar - al) * p.i2hx, gy = (at - ab) * p.i2hy, gz = (af - ak) * p.i2hz;
   return lam[comp * 3 + 0] * gx + lam[comp * 3 + 1] * gy + lam[comp * 3 + 2] * gz;
 }
 
@@ -84,9 +89,9 @@ __device__ inline T aniso_f2(const P<T> &p, const T *__restrict__ u, const T *la
   T af = z > 0 ? grad_comp(p, u, lam, z - 1, y, x, 2) : (T)0;
   T ak = z < n - 1 ? grad_comp(p, u, lam, z + 1, y, x, 2) : (T)0;
   T t = (T)0;
-  t += (ar - al) / (T)2 / p.hx;
-  t += (at - ab) / (T)2 / p.hy;
-  t += (af - ak) / (T)2 / p.hz;
+  t += (ar - al) * p.i2hx;
+  t += (at - ab) * p.i2hy;
+  t += (af - ak) * p.i2hz;
   return t;
 }
 
@@ -108,12 +113,12 @@ __global__ void __launch_bounds__(256) rhs_ac_kernel(P<T> p, const T *__restrict
       v -= p.LE * ac_f(p, e, c, m);
       if (face) {
         T w = p.LE * p.epn2;
-        if (x == 0) v += w * um[L3(n, iz, iy, lo)] / p.hx / p.hx;
-        if (x == n - 1) v += w * um[L3(n, iz, iy, hi)] / p.hx / p.hx;
-        if (y == 0) v += w * um[L3(n, iz, lo, ix)] / p.hy / p.hy;
-        if (y == n - 1) v += w * um[L3(n, iz, hi, ix)] / p.hy / p.hy;
-        if (z == 0) v += w * um[L3(n, lo, iy, ix)] / p.hz / p.hz;
-        if (z == n - 1) v += w * um[L3(n, hi, iy, ix)] / p.hz / p.hz;
+        if (x == 0) v += w * um[L3(n, iz, iy, lo)] * p.ih2x;
+        if (x == n - 1) v += w * um[L3(n, iz, iy, hi)] * p.ih2x;
+        if (y == 0) v += w * um[L3(n, iz, lo, ix)] * p.ih2y;
+        if (y == n - 1) v += w * um[L3(n, iz, hi, ix)] * p.ih2y;
+        if (z == 0) v += w * um[L3(n, lo, iy, ix)] * p.ih2z;
+        if (z == n - 1) v += w * um[L3(n, hi, iy, ix)] * p.ih2z;
       }
       if (p.aniso) v -= p.epn2 * p.LE * aniso_f2(p, um, p.lam[m], z, y, x);
       if (p.elastic == 1) v -= p.LE * p.es * felas[m * n3 + l];
@@ -139,12 +144,12 @@ __global__ void __launch_bounds__(256) rhs_ch_t_kernel(P<T> p, const T *__restri
     if (x == 0 || x == n - 1 || y == 0 || y == n - 1 || z == 0 || z == n - 1) {
       int iz = img(n, z), iy = img(n, y), ix = img(n, x), lo = img(n, -1), hi = img(n, n);
       T w = p.LCI * p.epn2;
-      if (x == 0) v -= w * cf[L3(n, iz, iy, lo)] / p.hx / p.hx;
-      if (x == n - 1) v -= w * cf[L3(n, iz, iy, hi)] / p.hx / p.hx;
-      if (y == 0) v -= w * cf[L3(n, iz, lo, ix)] / p.hy / p.hy;
-      if (y == n - 1) v -= w * cf[L3(n, iz, hi, ix)] / p.hy / p.hy;
-      if (z == 0) v -= w * cf[L3(n, lo, iy, ix)] / p.hz / p.hz;
-      if (z == n - 1) v -= w * cf[L3(n, hi, iy, ix)] / p.hz / p.hz;
+      if (x == 0) v -= w * cf[L3(n, iz, iy, lo)] * p.ih2x;
+      if (x == n - 1) v -= w * cf[L3(n, iz, iy, hi)] * p.ih2x;
+      if (y == 0) v -= w * cf[L3(n, iz, lo, ix)] * p.ih2y;
+      if (y == n - 1) v -= w * cf[L3(n, iz, hi, ix)] * p.ih2y;
+      if (z == 0) v -= w * cf[L3(n, lo, iy, ix)] * p.ih2z;
+      if (z == n - 1) v -= w * cf[L3(n, hi, iy, ix)] * p.ih2z;
     }
     t[l] = v;
   }
@@ -157,9 +162,9 @@ __device__ inline T ch_mu_at(const P<T> &p, const T *__restrict__ u, int z, int 
   long long n3 = (long long)n * n * n;
   const T *cf = u + p.nac * n3;
   T cv = cf[L3(n, z, y, x)];
-  T lap = (cf[L3(n, z, y, img(n, x - 1))] + (T)(-2.0) * cv + cf[L3(n, z, y, img(n, x + 1))]) / p.hx / p.hx;
-  lap += (cf[L3(n, z, img(n, y - 1), x)] + (T)(-2.0) * cv + cf[L3(n, z, img(n, y + 1), x)]) / p.hy / p.hy;
-  lap += (cf[L3(n, img(n, z - 1), y, x)] + (T)(-2.0) * cv + cf[L3(n, img(n, z + 1), y, x)]) / p.hz / p.hz;
+  T lap = (cf[L3(n, z, y, img(n, x - 1))] + (T)(-2.0) * cv + cf[L3(n, z, y, img(n, x + 1))]) * p.ih2x;
+  lap += (cf[L3(n, z, img(n, y - 1), x)] + (T)(-2.0) * cv + cf[L3(n, z, img(n, y + 1), x)]) * p.ih2y;
+  lap += (cf[L3(n, img(n, z - 1), y, x)] + (T)(-2.0) * cv + cf[L3(n, img(n, z + 1), y, x)]) * p.ih2z;
   T e[4];
   for (int m = 0; m < p.nac; m++) e[m] = u[m * n3 + L3(n, z, y, x)];
   T mu = p.LCI * p.epn2 * lap;
@@ -179,17 +184,17 @@ __global__ void __launch_bounds__(256) rhs_ch_lap_kernel(P<T> p, const T *__rest
     T fl = x > 0 ? t[l - 1] : (T)0, fr = x < n - 1 ? t[l + 1] : (T)0;
     T ft = y > 0 ? t[l - n] : (T)0, fb = y < n - 1 ? t[l + n] : (T)0;
     T ff = z > 0 ? t[l - nn] : (T)0, fk = z < n - 1 ? t[l + nn] : (T)0;
-    T v = (fl + fr - (T)2 * tc) / p.hx / p.hx;
-    v += (ft + fb - (T)2 * tc) / p.hy / p.hy;
-    v += (ff + fk - (T)2 * tc) / p.hz / p.hz;
+    T v = (fl + fr - (T)2 * tc) * p.ih2x;
+    v += (ft + fb - (T)2 * tc) * p.ih2y;
+    v += (ff + fk - (T)2 * tc) * p.ih2z;
     if (x == 0 || x == n - 1 || y == 0 || y == n - 1 || z == 0 || z == n - 1) {
       int iz = img(n, z), iy = img(n, y), ix = img(n, x), lo = img(n, -1), hi = img(n, n);
-      if (x == 0) v -= ch_mu_at(p, u, iz, iy, lo) / p.hx / p.hx;
-      if (x == n - 1) v -= ch_mu_at(p, u, iz, iy, hi) / p.hx / p.hx;
-      if (y == 0) v -= ch_mu_at(p, u, iz, lo, ix) / p.hy / p.hy;
-      if (y == n - 1) v -= ch_mu_at(p, u, iz, hi, ix) / p.hy / p.hy;
-      if (z == 0) v -= ch_mu_at(p, u, lo, iy, ix) / p.hz / p.hz;
-      if (z == n - 1) v -= ch_mu_at(p, u, hi, iy, ix) / p.hz / p.hz;
+      if (x == 0) v -= ch_mu_at(p, u, iz, iy, lo) * p.ih2x;
+      if (x == n - 1) v -= ch_mu_at(p, u, iz, iy, hi) * p.ih2x;
+      if (y == 0) v -= ch_mu_at(p, u, iz, lo, ix) * p.ih2y;
+      if (y == n - 1) v -= ch_mu_at(p, u, iz, hi, ix) * p.ih2y;
+      if (z == 0) v -= ch_mu_at(p, u, lo, iy, ix) * p.ih2z;
+      if (z == n - 1) v -= ch_mu_at(p, u, hi, iy, ix) * p.ih2z;
     }
     out[l] = v;
   }

@@ -1,5 +1,12 @@
 // C ABI of sclet_gb300: context, device state and the step sequence of the
 // reference's time loop (source_beta_to_omega/src/ScLETD.c:84-191) on one GPU.
+//
+// Two arithmetic forms share the sequence:
+//   SCLET_FP64  -- FP64 state, FP64 SIMT mode-n products (k_modeprod_f64.cu);
+//   SCLET_MIXED -- FP32 state and stencils/FFT, eigenbasis products as
+//                  split-BF16 tcgen05 products with FP32 accumulation
+//                  (k_modeprod_tc.cu), FP64-compensated diagnostics.
+#include <cuda_bf16.h>
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -10,6 +17,7 @@
 
 #include "sclet_gb300.h"
 #include "sclet_internal.cuh"
+#include "sclet_tc.cuh"
 
 namespace sclet {
 void set_phi_tables(const double *phi1_ac, const double *phi1_ch, const double *phi2_ac, const double *phi2_ch);
@@ -30,14 +38,23 @@ struct sclet_ctx {
   Phys ph;
   cudaStream_t stream = nullptr;
   std::string err;
-  // FP64 state: state2 = [u (F blocks) | rhs1 (F blocks)]
-  double *state2 = nullptr, *rhs2 = nullptr, *A = nullptr, *B = nullptr;
-  double *felas = nullptr, *scratch = nullptr, *shell = nullptr;
-  double *V[3] = {nullptr, nullptr, nullptr}, *Vi[3] = {nullptr, nullptr, nullptr}, *dd[3] = {nullptr, nullptr, nullptr};
-  double *phi1[2] = {nullptr, nullptr}, *phi2[2] = {nullptr, nullptr};
+  // shared
+  double *dd[3] = {nullptr, nullptr, nullptr};  // eigenvalues / h^2 (FP64)
   double *elam = nullptr, *partials = nullptr, *diag = nullptr;
   int npart = 0;
   ElasticPlan *elastic = nullptr;
+  int *dev_err = nullptr;  // bounded-wait failures of device kernels
+  // FP64 form: state2 = [u (F) | rhs1 (F)]
+  double *state2 = nullptr, *rhs2 = nullptr, *A = nullptr, *B = nullptr;
+  double *felas = nullptr, *scratch = nullptr, *shell = nullptr;
+  double *V[3] = {nullptr, nullptr, nullptr}, *Vi[3] = {nullptr, nullptr, nullptr};
+  double *phi1[2] = {nullptr, nullptr}, *phi2[2] = {nullptr, nullptr};
+  // MIXED form: fstate2 = [u (F) | rhs1 (F)] in FP32, split planes Sa / Sb
+  float *fstate2 = nullptr, *frhs2 = nullptr, *ffelas = nullptr, *fscratch = nullptr, *fshell = nullptr;
+  float *ddf[3] = {nullptr, nullptr, nullptr};
+  __nv_bfloat16 *Sa = nullptr, *Sb = nullptr, *matV = nullptr, *matVi = nullptr;
+  double *stage64 = nullptr;  // n^3 FP64 staging block for host transfers
+  // profiling
   bool profiling = false;
   std::vector<StageEv> evs;
   float stage_ms[8] = {0};
@@ -58,8 +75,11 @@ static std::string g_create_error;
 
 namespace {
 
+bool mixed(const sclet_ctx *ctx) { return ctx->precision == SCLET_MIXED; }
 double *u_of(sclet_ctx *ctx) { return ctx->state2; }
 double *rhs1_of(sclet_ctx *ctx) { return ctx->state2 + (long long)ctx->F * ctx->n3; }
+float *fu_of(sclet_ctx *ctx) { return ctx->fstate2; }
+float *frhs1_of(sclet_ctx *ctx) { return ctx->fstate2 + (long long)ctx->F * ctx->n3; }
 
 // phi1, phi2 of each field kind at eigen-mode (i, j, k), layout [k][j][i]
 // (ac_init_phi / ch_init_phi, vars.c:302-359).
@@ -91,6 +111,15 @@ __global__ void phi_kernel(double *phi1, double *phi2, int n, int kind, const do
   }
 }
 
+__global__ void f64_to_f32(const double *__restrict__ a, float *__restrict__ b, long long count) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+__global__ void f32_to_f64(const float *__restrict__ a, double *__restrict__ b, long long count) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x)
+    b[i] = (double)a[i];
+}
+
 int grid_of(long long total) {
   long long b = (total + 255) / 256;
   return (int)(b > 152LL * 16 ? 152LL * 16 : (b < 1 ? 1 : b));
@@ -104,14 +133,31 @@ int fail(sclet_ctx *ctx, int code, const std::string &msg) {
 int upload_eigen(sclet_ctx *ctx, const double *d, const double *v, const double *vi) {
   const int n = ctx->n;
   std::vector<double> ds(n);
+  std::vector<float> dsf(n);
   for (int ax = 0; ax < 3; ax++) {
     double h = ctx->ph.h[ax];
     // DDX[l] = DDX_b[l] / hx / hx (vars.c:510-513)
-    for (int l = 0; l < n; l++) ds[l] = d[l] / h / h;
+    for (int l = 0; l < n; l++) {
+      ds[l] = d[l] / h / h;
+      dsf[l] = (float)ds[l];
+    }
     CK(cudaMemcpyAsync(ctx->dd[ax], ds.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    if (mixed(ctx)) CK(cudaMemcpyAsync(ctx->ddf[ax], dsf.data(), sizeof(float) * n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  if (mixed(ctx)) {
+    // the stage block holds the FP64 matrices while they are split
+    CK(cudaMemcpyAsync(ctx->stage64, vi, sizeof(double) * n * n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(tc_split_matrix(ctx->stage64, ctx->matVi, n, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpyAsync(ctx->stage64, v, sizeof(double) * n * n, cudaMemcpyHostToDevice, ctx->stream));
+    CK(tc_split_matrix(ctx->stage64, ctx->matV, n, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SCLET_OK;
+  }
+  for (int ax = 0; ax < 3; ax++) {
     CK(cudaMemcpyAsync(ctx->V[ax], v, sizeof(double) * n * n, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(ctx->Vi[ax], vi, sizeof(double) * n * n, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));
   }
   const sclet_params &p = ctx->p;
   const double *lan = p.landau;
@@ -142,6 +188,32 @@ EtdCoef etd_coef(sclet_ctx *ctx) {
   return ec;
 }
 
+TcArgs tc_args(sclet_ctx *ctx, int count, int epi, int outmode) {
+  TcArgs g;
+  memset(&g, 0, sizeof g);
+  g.n = ctx->n;
+  g.count = count;
+  g.epi = epi;
+  g.outmode = outmode;
+  for (int a = 0; a < 3; a++) g.dd[a] = ctx->ddf[a];
+  g.kk[0] = (float)ctx->p.kkx;
+  g.kk[1] = (float)ctx->p.kky;
+  g.kk[2] = (float)ctx->p.kkz;
+  g.epn2 = (float)ctx->p.epn2;
+  g.dt = (float)ctx->p.dt;
+  g.LE = (float)ctx->ph.LE;
+  g.KE = (float)ctx->ph.KE;
+  g.LCI = (float)ctx->ph.LCI;
+  g.KCI = (float)ctx->ph.KCI;
+  g.nac = ctx->nac;
+  g.F = ctx->F;
+  g.err = ctx->dev_err;
+  return g;
+}
+
+// Elements of one split tensor (three planes of n*n rows of kp)
+long long split_stride(const sclet_ctx *ctx) { return 3LL * ctx->n * ctx->n * tc_kp(ctx->n); }
+
 void stage_begin(sclet_ctx *ctx, int cls, StageEv &ev) {
   if (!ctx->profiling) return;
   ev.cls = cls;
@@ -154,6 +226,39 @@ void stage_end(sclet_ctx *ctx, StageEv &ev, long long l0) {
   cudaEventRecord(ev.b, ctx->stream);
   ctx->evs.push_back(ev);
   ctx->stage_launches[ev.cls] += (int)(launch_counter() - l0);
+}
+
+int field_index(sclet_ctx *ctx, int kind, int m) {
+  if (kind == SCLET_AC && m >= 0 && m < ctx->nac) return m;
+  if (kind == SCLET_CH && m >= 0 && m < ctx->nch) return ctx->nac + m;
+  return -1;
+}
+
+// host FP64 block -> device block of the working precision
+int put_block(sclet_ctx *ctx, const double *host, double *dst64, float *dst32) {
+  if (!mixed(ctx)) {
+    CK(cudaMemcpyAsync(dst64, host, sizeof(double) * ctx->n3, cudaMemcpyHostToDevice, ctx->stream));
+  } else {
+    CK(cudaMemcpyAsync(ctx->stage64, host, sizeof(double) * ctx->n3, cudaMemcpyHostToDevice, ctx->stream));
+    f64_to_f32<<<grid_of(ctx->n3), 256, 0, ctx->stream>>>(ctx->stage64, dst32, ctx->n3);
+    launch_counter()++;
+    CK(cudaGetLastError());
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  return SCLET_OK;
+}
+
+int get_block(sclet_ctx *ctx, const double *src64, const float *src32, double *host) {
+  if (!mixed(ctx)) {
+    CK(cudaMemcpyAsync(host, src64, sizeof(double) * ctx->n3, cudaMemcpyDeviceToHost, ctx->stream));
+  } else {
+    f32_to_f64<<<grid_of(ctx->n3), 256, 0, ctx->stream>>>(src32, ctx->stage64, ctx->n3);
+    launch_counter()++;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(host, ctx->stage64, sizeof(double) * ctx->n3, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  return SCLET_OK;
 }
 
 }  // namespace
@@ -171,13 +276,16 @@ void sclet_destroy(sclet_ctx *ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-  double *bufs[] = {ctx->state2, ctx->rhs2, ctx->A, ctx->B, ctx->felas, ctx->scratch, ctx->shell, ctx->elam,
-                    ctx->partials, ctx->diag, ctx->phi1[0], ctx->phi1[1], ctx->phi2[0], ctx->phi2[1]};
-  for (double *b : bufs) cudaFree(b);
+  void *bufs[] = {ctx->state2, ctx->rhs2, ctx->A, ctx->B, ctx->felas, ctx->scratch, ctx->shell, ctx->elam,
+                  ctx->partials, ctx->diag, ctx->phi1[0], ctx->phi1[1], ctx->phi2[0], ctx->phi2[1], ctx->dev_err,
+                  ctx->fstate2, ctx->frhs2, ctx->ffelas, ctx->fscratch, ctx->fshell, ctx->Sa, ctx->Sb, ctx->matV,
+                  ctx->matVi, ctx->stage64};
+  for (void *b : bufs) cudaFree(b);
   for (int a = 0; a < 3; a++) {
     cudaFree(ctx->V[a]);
     cudaFree(ctx->Vi[a]);
     cudaFree(ctx->dd[a]);
+    cudaFree(ctx->ddf[a]);
   }
   for (auto &e : ctx->evs) {
     cudaEventDestroy(e.a);
@@ -212,10 +320,6 @@ int sclet_create(const sclet_params *p, int precision, int device, sclet_ctx **o
   }
   if (p->elastic == 1 && p->nac < 1) return bad("ELASTIC = 1 needs Allen-Cahn fields");
   if (precision != SCLET_FP64 && precision != SCLET_MIXED) return bad("precision must be SCLET_FP64 or SCLET_MIXED");
-  if (precision == SCLET_MIXED) {
-    g_create_error = "SCLET_MIXED is not available in this build";
-    return SCLET_ERR_UNSUPPORTED;
-  }
   sclet_ctx *ctx = new sclet_ctx();
   ctx->p = *p;
   ctx->precision = precision;
@@ -262,43 +366,65 @@ int sclet_create(const sclet_params *p, int precision, int device, sclet_ctx **o
   ph.KCI = p->landau[10];
 
   int rc = SCLET_OK;
-  auto cfail = [&](cudaError_t e, const char *what) {
-    ctx->err = std::string(what) + ": " + cudaGetErrorString(e);
-    return e == cudaErrorMemoryAllocation ? SCLET_ERR_NOMEM : SCLET_ERR_CUDA;
-  };
   cudaError_t e;
-#define CC(call)                       \
-  if ((e = (call)) != cudaSuccess) {   \
-    rc = cfail(e, #call);              \
-    g_create_error = ctx->err;         \
-    sclet_destroy(ctx);                \
-    return rc;                         \
+#define CC(call)                                                                   \
+  if ((e = (call)) != cudaSuccess) {                                               \
+    ctx->err = std::string(#call) + ": " + cudaGetErrorString(e);                  \
+    rc = e == cudaErrorMemoryAllocation ? SCLET_ERR_NOMEM : SCLET_ERR_CUDA;         \
+    g_create_error = ctx->err;                                                     \
+    sclet_destroy(ctx);                                                            \
+    return rc;                                                                     \
   }
   CC(cudaSetDevice(device));
   CC(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
-  const size_t blk = sizeof(double) * ctx->n3;
-  CC(cudaMalloc(&ctx->state2, 2 * F * blk));
-  CC(cudaMemsetAsync(ctx->state2, 0, 2 * F * blk, ctx->stream));
-  if (p->etd2) CC(cudaMalloc(&ctx->rhs2, F * blk));
-  CC(cudaMalloc(&ctx->A, 2 * F * blk));
-  CC(cudaMalloc(&ctx->B, 2 * F * blk));
-  CC(cudaMalloc(&ctx->felas, (ctx->nac > 0 ? ctx->nac : 1) * blk));
-  CC(cudaMemsetAsync(ctx->felas, 0, (ctx->nac > 0 ? ctx->nac : 1) * blk, ctx->stream));
-  CC(cudaMalloc(&ctx->scratch, 2 * blk));
-  CC(cudaMalloc(&ctx->shell, sizeof(double) * F * shell_count(n)));
-  for (int a = 0; a < 3; a++) {
-    CC(cudaMalloc(&ctx->V[a], sizeof(double) * n * n));
-    CC(cudaMalloc(&ctx->Vi[a], sizeof(double) * n * n));
-    CC(cudaMalloc(&ctx->dd[a], sizeof(double) * n));
-  }
-  for (int k = 0; k < 2; k++) {
-    CC(cudaMalloc(&ctx->phi1[k], blk));
-    CC(cudaMalloc(&ctx->phi2[k], blk));
-  }
+  cudaStream_t s = ctx->stream;
+  for (int a = 0; a < 3; a++) CC(cudaMalloc(&ctx->dd[a], sizeof(double) * n));
   CC(cudaMalloc(&ctx->elam, sizeof(double) * 36));
   ctx->npart = check_soln_partials(n);
   CC(cudaMalloc(&ctx->partials, sizeof(double) * ctx->npart * (4 * F + 4)));
   CC(cudaMalloc(&ctx->diag, sizeof(double) * 4 * F));
+  CC(cudaMalloc(&ctx->dev_err, sizeof(int)));
+  CC(cudaMemsetAsync(ctx->dev_err, 0, sizeof(int), s));
+  const int nfel = ctx->nac > 0 ? ctx->nac : 1;
+  if (!mixed(ctx)) {
+    const size_t blk = sizeof(double) * ctx->n3;
+    CC(cudaMalloc(&ctx->state2, 2 * F * blk));
+    CC(cudaMemsetAsync(ctx->state2, 0, 2 * F * blk, s));
+    if (p->etd2) CC(cudaMalloc(&ctx->rhs2, F * blk));
+    CC(cudaMalloc(&ctx->A, 2 * F * blk));
+    CC(cudaMalloc(&ctx->B, 2 * F * blk));
+    CC(cudaMalloc(&ctx->felas, nfel * blk));
+    CC(cudaMemsetAsync(ctx->felas, 0, nfel * blk, s));
+    CC(cudaMalloc(&ctx->scratch, 2 * blk));
+    CC(cudaMalloc(&ctx->shell, sizeof(double) * F * shell_count(n)));
+    for (int a = 0; a < 3; a++) {
+      CC(cudaMalloc(&ctx->V[a], sizeof(double) * n * n));
+      CC(cudaMalloc(&ctx->Vi[a], sizeof(double) * n * n));
+    }
+    for (int k = 0; k < 2; k++) {
+      CC(cudaMalloc(&ctx->phi1[k], blk));
+      CC(cudaMalloc(&ctx->phi2[k], blk));
+    }
+  } else {
+    const size_t blk = sizeof(float) * ctx->n3;
+    CC(cudaMalloc(&ctx->fstate2, 2 * F * blk));
+    CC(cudaMemsetAsync(ctx->fstate2, 0, 2 * F * blk, s));
+    if (p->etd2) CC(cudaMalloc(&ctx->frhs2, F * blk));
+    CC(cudaMalloc(&ctx->ffelas, nfel * blk));
+    CC(cudaMemsetAsync(ctx->ffelas, 0, nfel * blk, s));
+    CC(cudaMalloc(&ctx->fscratch, 2 * blk));
+    CC(cudaMalloc(&ctx->fshell, sizeof(float) * F * shell_count(n)));
+    const size_t sbytes = sizeof(__nv_bfloat16) * split_stride(ctx) * 2 * F;
+    // pad columns of the split tensors are never written and must stay zero
+    CC(cudaMalloc(&ctx->Sa, sbytes));
+    CC(cudaMalloc(&ctx->Sb, sbytes));
+    CC(cudaMemsetAsync(ctx->Sa, 0, sbytes, s));
+    CC(cudaMemsetAsync(ctx->Sb, 0, sbytes, s));
+    CC(cudaMalloc(&ctx->matV, sizeof(__nv_bfloat16) * 3 * n * tc_kp(n)));
+    CC(cudaMalloc(&ctx->matVi, sizeof(__nv_bfloat16) * 3 * n * tc_kp(n)));
+    for (int a = 0; a < 3; a++) CC(cudaMalloc(&ctx->ddf[a], sizeof(float) * n));
+    CC(cudaMalloc(&ctx->stage64, sizeof(double) * ctx->n3));
+  }
   {
     // energy tensors: the gradient operator of the dynamics
     double el[36] = {0};
@@ -306,8 +432,8 @@ int sclet_create(const sclet_params *p, int precision, int device, sclet_ctx **o
       for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++)
           el[m * 9 + i * 3 + j] = p->anisotropic ? p->lambda_file[m][i * 3 + j] : (i == j ? ph.kk[i] : 0.0);
-    CC(cudaMemcpyAsync(ctx->elam, el, sizeof el, cudaMemcpyHostToDevice, ctx->stream));
-    CC(cudaStreamSynchronize(ctx->stream));
+    CC(cudaMemcpyAsync(ctx->elam, el, sizeof el, cudaMemcpyHostToDevice, s));
+    CC(cudaStreamSynchronize(s));
   }
   {
     std::vector<double> d(n), v((size_t)n * n), vi((size_t)n * n);
@@ -320,9 +446,9 @@ int sclet_create(const sclet_params *p, int precision, int device, sclet_ctx **o
     }
   }
   if (p->elastic == 1) {
-    CC(elastic_plan_create(&ctx->elastic, N, ctx->nac, p->voigt, &p->eigenstrain[0][0], 0, ctx->stream));
+    CC(elastic_plan_create(&ctx->elastic, N, ctx->nac, p->voigt, &p->eigenstrain[0][0], mixed(ctx) ? 1 : 0, s));
   }
-  CC(cudaStreamSynchronize(ctx->stream));
+  CC(cudaStreamSynchronize(s));
 #undef CC
   *out = ctx;
   return SCLET_OK;
@@ -341,60 +467,51 @@ int sclet_set_energy_tensors(sclet_ctx *ctx, const double *lam) {
   return SCLET_OK;
 }
 
-static int field_index(sclet_ctx *ctx, int kind, int m) {
-  if (kind == SCLET_AC && m >= 0 && m < ctx->nac) return m;
-  if (kind == SCLET_CH && m >= 0 && m < ctx->nch) return ctx->nac + m;
-  return -1;
-}
-
 int sclet_set_field(sclet_ctx *ctx, int kind, int m, const double *block) {
   int f = field_index(ctx, kind, m);
   if (f < 0) return fail(ctx, SCLET_ERR_ARG, "no such field");
-  CK(cudaMemcpyAsync(u_of(ctx) + f * ctx->n3, block, sizeof(double) * ctx->n3, cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
-  return SCLET_OK;
+  return mixed(ctx) ? put_block(ctx, block, nullptr, fu_of(ctx) + f * ctx->n3)
+                    : put_block(ctx, block, u_of(ctx) + f * ctx->n3, nullptr);
 }
 
 int sclet_get_field(sclet_ctx *ctx, int kind, int m, double *block) {
   int f = field_index(ctx, kind, m);
   if (f < 0) return fail(ctx, SCLET_ERR_ARG, "no such field");
-  CK(cudaMemcpyAsync(block, u_of(ctx) + f * ctx->n3, sizeof(double) * ctx->n3, cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
-  return SCLET_OK;
+  return mixed(ctx) ? get_block(ctx, nullptr, fu_of(ctx) + f * ctx->n3, block)
+                    : get_block(ctx, u_of(ctx) + f * ctx->n3, nullptr, block);
 }
 
 int sclet_load_restart(sclet_ctx *ctx, int kind, int m, const char *path) {
   std::vector<double> blk(ctx->n3, 0.0);
   int f = field_index(ctx, kind, m);
   if (f < 0) return fail(ctx, SCLET_ERR_ARG, "no such field");
-  CK(cudaMemcpyAsync(blk.data(), u_of(ctx) + f * ctx->n3, sizeof(double) * ctx->n3, cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
-  int rc = sclet_read_restart(path, ctx->n, blk.data());
+  int rc = sclet_get_field(ctx, kind, m, blk.data());
+  if (rc != SCLET_OK) return rc;
+  rc = sclet_read_restart(path, ctx->n, blk.data());
   if (rc != SCLET_OK) return fail(ctx, rc, std::string("cannot read restart file ") + path);
   return sclet_set_field(ctx, kind, m, blk.data());
 }
 
 int sclet_get_rhs(sclet_ctx *ctx, int slot, int kind, int m, double *block) {
   int f = field_index(ctx, kind, m);
-  if (f < 0 || (slot != 1 && slot != 2) || (slot == 2 && !ctx->rhs2)) return fail(ctx, SCLET_ERR_ARG, "bad rhs slot");
-  const double *src = (slot == 1 ? rhs1_of(ctx) : ctx->rhs2) + f * ctx->n3;
-  CK(cudaMemcpyAsync(block, src, sizeof(double) * ctx->n3, cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
-  return SCLET_OK;
+  bool have2 = mixed(ctx) ? ctx->frhs2 != nullptr : ctx->rhs2 != nullptr;
+  if (f < 0 || (slot != 1 && slot != 2) || (slot == 2 && !have2)) return fail(ctx, SCLET_ERR_ARG, "bad rhs slot");
+  if (mixed(ctx)) return get_block(ctx, nullptr, (slot == 1 ? frhs1_of(ctx) : ctx->frhs2) + f * ctx->n3, block);
+  return get_block(ctx, (slot == 1 ? rhs1_of(ctx) : ctx->rhs2) + f * ctx->n3, nullptr, block);
 }
 
 int sclet_get_felas(sclet_ctx *ctx, int m, double *block) {
   if (m < 0 || m >= ctx->nac) return fail(ctx, SCLET_ERR_ARG, "no such field");
-  CK(cudaMemcpyAsync(block, ctx->felas + m * ctx->n3, sizeof(double) * ctx->n3, cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
-  return SCLET_OK;
+  if (mixed(ctx)) return get_block(ctx, nullptr, ctx->ffelas + m * ctx->n3, block);
+  return get_block(ctx, ctx->felas + m * ctx->n3, nullptr, block);
 }
 
 int sclet_transfer(sclet_ctx *ctx) {
   StageEv ev;
   long long l0 = launch_counter();
   stage_begin(ctx, 3, ev);
-  CK(launch_ghost_fill<double>(u_of(ctx), ctx->F, ctx->n, ctx->shell, ctx->stream));
+  if (mixed(ctx)) CK(launch_ghost_fill<float>(fu_of(ctx), ctx->F, ctx->n, ctx->fshell, ctx->stream));
+  else CK(launch_ghost_fill<double>(u_of(ctx), ctx->F, ctx->n, ctx->shell, ctx->stream));
   stage_end(ctx, ev, l0);
   return SCLET_OK;
 }
@@ -404,31 +521,90 @@ int sclet_elastic_calculate(sclet_ctx *ctx) {
   StageEv ev;
   long long l0 = launch_counter();
   stage_begin(ctx, 2, ev);
-  CK(elastic_compute<double>(ctx->elastic, u_of(ctx), ctx->felas, ctx->n, ctx->scratch, ctx->stream));
+  if (mixed(ctx))
+    CK(elastic_compute<float>(ctx->elastic, fu_of(ctx), ctx->ffelas, ctx->n, ctx->fscratch, ctx->stream));
+  else
+    CK(elastic_compute<double>(ctx->elastic, u_of(ctx), ctx->felas, ctx->n, ctx->scratch, ctx->stream));
   stage_end(ctx, ev, l0);
   return SCLET_OK;
 }
 
 int sclet_calc_rhs(sclet_ctx *ctx, int slot) {
   if (slot != 1 && slot != 2) return fail(ctx, SCLET_ERR_ARG, "slot must be 1 or 2");
-  if (slot == 2 && !ctx->rhs2) return fail(ctx, SCLET_ERR_ARG, "slot 2 needs ETD2 = 1");
+  if (slot == 2 && !ctx->p.etd2) return fail(ctx, SCLET_ERR_ARG, "slot 2 needs ETD2 = 1");
   StageEv ev;
   long long l0 = launch_counter();
   stage_begin(ctx, 1, ev);
-  double *dst = slot == 1 ? rhs1_of(ctx) : ctx->rhs2;
-  CK(launch_rhs<double>(ctx->ph, u_of(ctx), ctx->felas, dst, ctx->scratch, ctx->stream));
+  if (mixed(ctx)) {
+    float *dst = slot == 1 ? frhs1_of(ctx) : ctx->frhs2;
+    CK(launch_rhs<float>(ctx->ph, fu_of(ctx), ctx->ffelas, dst, ctx->fscratch, ctx->stream));
+  } else {
+    double *dst = slot == 1 ? rhs1_of(ctx) : ctx->rhs2;
+    CK(launch_rhs<double>(ctx->ph, u_of(ctx), ctx->felas, dst, ctx->scratch, ctx->stream));
+  }
   stage_end(ctx, ev, l0);
   return SCLET_OK;
 }
 
+// Mixed form of the transforms: split, three forward products (the third of
+// the right-hand-side tensors fuses the ETD update), three inverse products.
+static int etd_update_mixed(sclet_ctx *ctx) {
+  const int F = ctx->F;
+  const long long ss = split_stride(ctx);
+  cudaStream_t s = ctx->stream;
+  CK(tc_split_fields(ctx->fstate2, nullptr, ctx->Sb, ctx->n, 2 * F, s));
+  TcArgs g = tc_args(ctx, 2 * F, 0, 0);
+  g.out_split = ctx->Sa;
+  CK(launch_modeprod_tc(ctx->matVi, ctx->Sb, 2 * F, g, s));
+  g.out_split = ctx->Sb;
+  CK(launch_modeprod_tc(ctx->matVi, ctx->Sa, 2 * F, g, s));
+  g = tc_args(ctx, F, 0, 0);
+  g.out_split = ctx->Sa;
+  CK(launch_modeprod_tc(ctx->matVi, ctx->Sb, F, g, s));
+  g = tc_args(ctx, F, 1, 0);
+  g.aux = ctx->Sa;
+  g.out_split = ctx->Sa;
+  CK(launch_modeprod_tc(ctx->matVi, ctx->Sb + F * ss, F, g, s));
+  g = tc_args(ctx, F, 0, 0);
+  g.out_split = ctx->Sb;
+  CK(launch_modeprod_tc(ctx->matV, ctx->Sa, F, g, s));
+  g.out_split = ctx->Sa;
+  CK(launch_modeprod_tc(ctx->matV, ctx->Sb, F, g, s));
+  g = tc_args(ctx, F, 0, 1);
+  g.out_f32 = fu_of(ctx);
+  CK(launch_modeprod_tc(ctx->matV, ctx->Sa, F, g, s));
+  return SCLET_OK;
+}
+
+static int etd2_correct_mixed(sclet_ctx *ctx) {
+  const int F = ctx->F;
+  cudaStream_t s = ctx->stream;
+  CK(tc_split_fields(ctx->frhs2, frhs1_of(ctx), ctx->Sb, ctx->n, F, s));
+  const __nv_bfloat16 *mats[6] = {ctx->matVi, ctx->matVi, ctx->matVi, ctx->matV, ctx->matV, ctx->matV};
+  __nv_bfloat16 *bufs[2] = {ctx->Sb, ctx->Sa};
+  for (int k = 0; k < 6; k++) {
+    TcArgs g = tc_args(ctx, F, k == 2 ? 2 : 0, k == 5 ? 2 : 0);
+    g.out_split = bufs[(k + 1) % 2];
+    g.out_f32 = fu_of(ctx);
+    CK(launch_modeprod_tc(mats[k], bufs[k % 2], F, g, s));
+  }
+  return SCLET_OK;
+}
+
 int sclet_etd_update(sclet_ctx *ctx) {
+  StageEv ev;
+  long long l0 = launch_counter();
+  stage_begin(ctx, 0, ev);
+  if (mixed(ctx)) {
+    int rc = etd_update_mixed(ctx);
+    if (rc != SCLET_OK) return rc;
+    stage_end(ctx, ev, l0);
+    return SCLET_OK;
+  }
   const int F = ctx->F;
   const long long n3 = ctx->n3;
   EtdCoef ec = etd_coef(ctx);
   set_phi_tables(ctx->phi1[0], ctx->phi1[1], ctx->phi2[0], ctx->phi2[1]);
-  StageEv ev;
-  long long l0 = launch_counter();
-  stage_begin(ctx, 0, ev);
   cudaStream_t s = ctx->stream;
   // V^-1 along x, y for u and N1 together; along z for u, then for N1 with
   // the ETD1 update fused (uhat in A[0..F) is updated in place).
@@ -445,14 +621,20 @@ int sclet_etd_update(sclet_ctx *ctx) {
 }
 
 int sclet_etd2_correct(sclet_ctx *ctx) {
-  if (!ctx->rhs2) return fail(ctx, SCLET_ERR_ARG, "ETD2 = 0");
+  if (!ctx->p.etd2) return fail(ctx, SCLET_ERR_ARG, "ETD2 = 0");
+  StageEv ev;
+  long long l0 = launch_counter();
+  stage_begin(ctx, 0, ev);
+  if (mixed(ctx)) {
+    int rc = etd2_correct_mixed(ctx);
+    if (rc != SCLET_OK) return rc;
+    stage_end(ctx, ev, l0);
+    return SCLET_OK;
+  }
   const int F = ctx->F;
   const long long n3 = ctx->n3;
   EtdCoef ec = etd_coef(ctx);
   set_phi_tables(ctx->phi1[0], ctx->phi1[1], ctx->phi2[0], ctx->phi2[1]);
-  StageEv ev;
-  long long l0 = launch_counter();
-  stage_begin(ctx, 0, ev);
   cudaStream_t s = ctx->stream;
   CK(launch_modeprod_f64(ctx->Vi[0], ctx->rhs2, rhs1_of(ctx), ctx->A, nullptr, F, ctx->n, 0, ec, n3, n3, s));
   CK(launch_modeprod_f64(ctx->Vi[1], ctx->A, nullptr, ctx->B, nullptr, F, ctx->n, 0, ec, n3, n3, s));
@@ -486,8 +668,12 @@ int sclet_check_soln(sclet_ctx *ctx, int energy_form, sclet_diag *out) {
   StageEv ev;
   long long l0 = launch_counter();
   stage_begin(ctx, 4, ev);
-  CK(launch_check_soln<double>(ctx->ph, u_of(ctx), ctx->elam, energy_form, ctx->partials, ctx->npart, ctx->diag,
-                               ctx->stream));
+  if (mixed(ctx))
+    CK(launch_check_soln<float>(ctx->ph, fu_of(ctx), ctx->elam, energy_form, ctx->partials, ctx->npart, ctx->diag,
+                                ctx->stream));
+  else
+    CK(launch_check_soln<double>(ctx->ph, u_of(ctx), ctx->elam, energy_form, ctx->partials, ctx->npart, ctx->diag,
+                                 ctx->stream));
   stage_end(ctx, ev, l0);
   std::vector<double> h(4 * ctx->F);
   CK(cudaMemcpyAsync(h.data(), ctx->diag, sizeof(double) * 4 * ctx->F, cudaMemcpyDeviceToHost, ctx->stream));
@@ -505,8 +691,25 @@ int sclet_check_soln(sclet_ctx *ctx, int energy_form, sclet_diag *out) {
 }
 
 int sclet_mode_product(sclet_ctx *ctx, int inverse, const double *in, double *out) {
-  EtdCoef ec = etd_coef(ctx);
   const long long n3 = ctx->n3;
+  if (mixed(ctx)) {
+    // in -> FP32 scratch, split, product, FP32 -> host FP64
+    float *tmp = ctx->fscratch;
+    CK(cudaMemcpyAsync(ctx->stage64, in, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
+    f64_to_f32<<<grid_of(n3), 256, 0, ctx->stream>>>(ctx->stage64, tmp, n3);
+    launch_counter()++;
+    CK(cudaGetLastError());
+    CK(tc_split_fields(tmp, nullptr, ctx->Sb, ctx->n, 1, ctx->stream));
+    TcArgs g = tc_args(ctx, 1, 0, 1);
+    g.out_f32 = tmp + n3;
+    CK(launch_modeprod_tc(inverse ? ctx->matV : ctx->matVi, ctx->Sb, 1, g, ctx->stream));
+    f32_to_f64<<<grid_of(n3), 256, 0, ctx->stream>>>(tmp + n3, ctx->stage64, n3);
+    launch_counter()++;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, ctx->stage64, sizeof(double) * n3, cudaMemcpyDeviceToHost, ctx->stream));
+    return sclet_sync(ctx);
+  }
+  EtdCoef ec = etd_coef(ctx);
   CK(cudaMemcpyAsync(ctx->A, in, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
   CK(launch_modeprod_f64(inverse ? ctx->V[0] : ctx->Vi[0], ctx->A, nullptr, ctx->B, nullptr, 1, ctx->n, 0, ec, n3, n3,
                          ctx->stream));
@@ -517,6 +720,10 @@ int sclet_mode_product(sclet_ctx *ctx, int inverse, const double *in, double *ou
 
 int sclet_sync(sclet_ctx *ctx) {
   CK(cudaStreamSynchronize(ctx->stream));
+  int e = 0;
+  CK(cudaMemcpyAsync(&e, ctx->dev_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (e) return fail(ctx, SCLET_ERR_TIMEOUT, "a bounded device wait gave up (tensor-core pipeline)");
   return SCLET_OK;
 }
 
@@ -549,6 +756,7 @@ int sclet_time_steps(sclet_ctx *ctx, int nsteps, float *ms) {
     cudaEventElapsedTime(&t, e.a, e.b);
     ctx->stage_ms[e.cls] += t;
   }
+  if (rc == SCLET_OK) rc = sclet_sync(ctx);
   return rc;
 }
 
