@@ -2,28 +2,35 @@
 // the mixed-precision form of PUX / PUY / PUZ (source_beta_to_omega/src/
 // calc.c:631-684).
 //
-// Operands travel as three BF16 planes x = x0 + x1 + x2 (x0 = bf16(x),
-// x1 = bf16(x - x0), x2 = bf16(x - x0 - x1): 24 significant bits, the FP32
-// state exactly).  The product keeps every cross term of order <= 2,
-//   M x ~ M0 x0 + M0 x1 + M1 x0 + M0 x2 + M1 x1 + M2 x0,
-// six BF16 MMAs with one FP32 accumulator in tensor memory (the 3-term split
-// of Markidis et al. 2018 / Ootomo & Yokota 2022 carried to third order).
+// Number format: each operand is a power-of-two scale times four fixed-point
+// slices of 6 bits, x = S * sum_p d_p 64^-(p+1), d_0 in [-64, 64], d_p in
+// [-32, 32] (round to nearest at every level; 24 bits below S).  The slices
+// are small integers held exactly in BF16.  The product keeps every cross term
+// of weight w = p + q <= 3 (ten BF16 MMAs per k-step, the split-precision
+// scheme of Markidis et al. 2018 / Ootomo & Yokota 2022 carried to fixed
+// point, as in the Ozaki scheme), one FP32 accumulator in tensor memory per
+// weight class.  Every partial sum is an integer below 2^24 (|sum| <= 6144 per
+// k times K <= 1040), so the tensor-core accumulation is exact and unbiased;
+// the epilogue combines the four classes with round-to-nearest FP32 adds.
 //
-// Layout ("split tensor"): for each tensor t and plane p, rows r = 0 .. n*n-1
-// of kp = roundup(n, 8) BF16 values, one 1-D line along the contracted axis per
-// row: S[t][p][r][k].  A product contracts k and writes row (a' * n + c),
-// column b for input row r = c * n + b -- the cyclic rotation that makes three
-// products return to x-fastest order.
+// Scales: per matrix row (static) and per input tensor (2^ceil(log2 max|x|),
+// from the max that the producing kernel records).
 //
-// Tile: D[128 a' x 128 r] in TMEM (128 lanes x 128 FP32 columns).  A = matrix
-// planes (128 a' rows x 64 k, 128-byte swizzle), B = input planes (128 r rows
-// x 64 k), both K-major, loaded by TMA into a two-stage mbarrier pipeline.
-// Warp 0 issues TMA, warp 1 issues MMAs (one elected thread each), warp 2 owns
-// the TMEM allocation, all four warps run the epilogue: TMEM -> registers ->
-// shared tile -> coalesced global stores, with the ETD update (ac_updateU_new
-// / ch_updateU_new, calc.c:489-535) or the phi2 scaling (prepare_U2_new,
-// calc.c:553-567) fused.  Every mbarrier wait is bounded: on timeout the CTA
-// records an error code, drains its copies (bounded), frees TMEM and returns.
+// Layout: input planes P[t][p][r][k], rows r = 0 .. n*n-1 of kp = roundup(n, 8)
+// BF16 values (one 1-D line along the contracted axis per row).  Output FP32
+// out[t][a' * n*n + r] for input row r = c * n + b, i.e. contracted index
+// slowest: three products return to x-fastest order.
+//
+// Tile: D[128 a' x 128 r], 4 accumulators x 128 TMEM columns.  A = matrix
+// slices (128 a' rows x 32 k, 64-byte swizzle), B = input slices (128 r rows x
+// 32 k), both K-major, TMA-loaded into a three-stage mbarrier pipeline.  Warp 0
+// issues TMA, warp 1 issues MMAs (one elected thread each), warp 2 owns the
+// TMEM allocation, all four warps run the epilogue: TMEM -> registers ->
+// shared tile -> coalesced FP32 stores, with the ETD update (ac_updateU_new /
+// ch_updateU_new, calc.c:489-535) or the phi2 scaling (prepare_U2_new,
+// calc.c:553-567) fused, and the tile's max |out| folded into out_max.  Every
+// mbarrier wait is bounded: on timeout the CTA records an error, drains its
+// copies (bounded), frees TMEM and returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
@@ -37,13 +44,16 @@ namespace sclet {
 
 namespace tc {
 
-constexpr int BM = 128, BN = 128, BK = 64, STAGES = 2;
-constexpr int PLANE_A = BM * BK * 2;   // 16 KB
-constexpr int PLANE_B = BN * BK * 2;   // 16 KB
-constexpr int STAGE_BYTES = 3 * PLANE_A + 3 * PLANE_B;
+constexpr int BM = 128, BN = 128, BK = 32, STAGES = 3, NP = TC_PLANES;
+constexpr int PLANE_A = BM * BK * 2;  // 8 KB
+constexpr int PLANE_B = BN * BK * 2;  // 8 KB
+constexpr int STAGE_BYTES = NP * PLANE_A + NP * PLANE_B;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;
-constexpr int TMEM_COLS = 128;
-constexpr long long WAIT_LIMIT = 1LL << 22;   // polls (with backoff) before giving up
+constexpr int NACC = 4;  // weight classes w = 0..3
+constexpr int TMEM_COLS = NACC * BN;
+constexpr long long WAIT_LIMIT = 1LL << 22;  // polls (with backoff) before giving up
+static_assert(TMEM_COLS <= 512, "tensor memory holds 512 columns");
+static_assert(BM * (BN + 1) * 4 <= STAGES * STAGE_BYTES, "epilogue tile reuses the stage buffers");
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -79,15 +89,15 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, i
       : "memory");
 }
 
-// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
-// 1024 bytes apart.
+// Shared-memory matrix descriptor: K-major, 64-byte swizzle, 8-row groups
+// 512 bytes apart.
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
   uint64_t d = 0;
   d |= (uint64_t)((addr & 0x3FFFFu) >> 4);
-  d |= (uint64_t)1 << 16;               // leading byte offset (unused for swizzled K-major)
-  d |= (uint64_t)(1024 >> 4) << 32;     // stride byte offset
-  d |= (uint64_t)1 << 46;               // descriptor version
-  d |= (uint64_t)2 << 61;               // 128-byte swizzle
+  d |= (uint64_t)1 << 16;             // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(512 >> 4) << 32;    // stride byte offset
+  d |= (uint64_t)1 << 46;             // descriptor version
+  d |= (uint64_t)4 << 61;             // 64-byte swizzle
   return d;
 }
 
@@ -125,43 +135,6 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
   for (int j = 0; j < 32; j++) v[j] = __uint_as_float(r[j]);
 }
 
-// Splits a float into three bf16 terms (round to nearest at each level).
-__device__ __forceinline__ void split3(float x, __nv_bfloat16 &a, __nv_bfloat16 &b, __nv_bfloat16 &c) {
-  a = __float2bfloat16_rn(x);
-  float r = x - __bfloat162float(a);
-  b = __float2bfloat16_rn(r);
-  r -= __bfloat162float(b);
-  c = __float2bfloat16_rn(r);
-}
-
-__device__ __forceinline__ float etd_H(const TcArgs &g, int kind, int i, int j, int k) {
-  float tmp, H;
-  if (kind == 0) {
-    tmp = g.kk[2] * g.dd[2][k] + g.kk[1] * g.dd[1][j] + g.kk[0] * g.dd[0][i];
-    H = -g.LE * (tmp * g.epn2 - g.KE);
-  } else {
-    tmp = g.dd[2][k] + g.dd[1][j] + g.dd[0][i];
-    H = g.LCI * (tmp * tmp * g.epn2 - g.KCI * tmp);
-  }
-  return H;
-}
-
-// phi1 = (1 - e^{-dt H}) / H, phi2 = (1 - phi1/dt) / H (ac_init_phi, vars.c:
-// 302-330), with series forms where dt H is small.
-__device__ __forceinline__ void etd_phi(float H, float dt, float &phi1, float &phi2) {
-  float x = dt * H;
-  if (fabsf(x) < 1.0e-3f) {
-    phi1 = dt * (1.0f - x * (0.5f - x * (1.0f / 6.0f)));
-    phi2 = dt * (0.5f - x * (1.0f / 6.0f - x * (1.0f / 24.0f)));
-  } else if (fabsf(x) < 0.1f) {
-    phi1 = -expm1f(-x) / H;
-    phi2 = dt * (0.5f - x * (1.0f / 6.0f - x * (1.0f / 24.0f - x * (1.0f / 120.0f - x * (1.0f / 720.0f)))));
-  } else {
-    phi1 = -expm1f(-x) / H;
-    phi2 = (1.0f - phi1 / dt) / H;
-  }
-}
-
 __global__ void __launch_bounds__(128, 1)
     modeprod_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcArgs g) {
   extern __shared__ uint8_t smem_raw[];
@@ -170,6 +143,7 @@ __global__ void __launch_bounds__(128, 1)
   __shared__ __align__(8) uint64_t acc_bar;
   __shared__ uint32_t tmem_slot;
   __shared__ int failed;
+  __shared__ float warp_max[4];
 
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -199,7 +173,7 @@ __global__ void __launch_bounds__(128, 1)
   const int nkb = g.kblocks;
 
   if (warp == 0 && lane == 0) {
-    // producer: three A planes and three B planes per stage
+    // producer: four A slices and four B slices per stage
     int issued = 0;
     for (int kb = 0; kb < nkb; kb++) {
       const int s = kb % STAGES;
@@ -210,20 +184,23 @@ __global__ void __launch_bounds__(128, 1)
       if (*(volatile int *)&failed) break;
       uint8_t *st = base + s * STAGE_BYTES;
       mbar_expect_tx(&full_bar[s], STAGE_BYTES);
-      for (int p = 0; p < 3; p++) tma_load_3d(st + p * PLANE_A, &tmA, kb * BK, a_tile * BM, p, &full_bar[s]);
-      for (int p = 0; p < 3; p++)
-        tma_load_3d(st + 3 * PLANE_A + p * PLANE_B, &tmB, kb * BK, r_tile * BN, t * 3 + p, &full_bar[s]);
+      for (int p = 0; p < NP; p++) tma_load_3d(st + p * PLANE_A, &tmA, kb * BK, a_tile * BM, p, &full_bar[s]);
+      for (int p = 0; p < NP; p++)
+        tma_load_3d(st + NP * PLANE_A + p * PLANE_B, &tmB, kb * BK, r_tile * BN, t * NP + p, &full_bar[s]);
       issued = kb + 1;
     }
     if (*(volatile int *)&failed) {
-      // drain: wait (bounded) for the copies still in flight into this CTA's
-      // shared memory before it is reused or released
+      // drain: wait (bounded) for copies still in flight into this CTA
       for (int kb = issued - STAGES < 0 ? 0 : issued - STAGES; kb < issued; kb++)
         mbar_wait(&full_bar[kb % STAGES], (kb / STAGES) & 1);
     }
   } else if (warp == 1 && lane == 0) {
-    // MMA issuer: 4 k-steps of 16 per stage, six split terms each
+    // MMA issuer: 2 k-steps of 16 per stage, ten terms each; (matrix slice,
+    // input slice) grouped by weight class, small classes first; the first
+    // term of each class at the first k-step starts its accumulator
     const uint32_t idesc = idesc_bf16(BM, BN);
+    const int pairA[10] = {0, 1, 2, 3, 0, 1, 2, 0, 1, 0};
+    const int pairB[10] = {3, 2, 1, 0, 2, 1, 0, 1, 0, 0};
     for (int kb = 0; kb < nkb; kb++) {
       const int s = kb % STAGES;
       if (!mbar_wait(&full_bar[s], (kb / STAGES) & 1)) {
@@ -232,18 +209,18 @@ __global__ void __launch_bounds__(128, 1)
       }
       fence_after();
       const uint32_t sa = smem_u32(base + s * STAGE_BYTES);
-      const uint32_t sb = sa + 3 * PLANE_A;
+      const uint32_t sb = sa + NP * PLANE_A;
 #pragma unroll
       for (int ks = 0; ks < BK / 16; ks++) {
         const uint32_t koff = ks * 32;
-        // (a plane, b plane) pairs of order <= 2; small terms first
-        const int pa[6] = {2, 1, 0, 1, 0, 0};
-        const int pb[6] = {0, 1, 2, 0, 1, 0};
+        const bool first = (kb == 0 && ks == 0);
 #pragma unroll
-        for (int q = 0; q < 6; q++) {
-          uint64_t da = smem_desc(sa + pa[q] * PLANE_A + koff);
-          uint64_t db = smem_desc(sb + pb[q] * PLANE_B + koff);
-          mma_bf16(tmem, da, db, idesc, (kb | ks | q) != 0);
+        for (int q = 0; q < 10; q++) {
+          const int pa = pairA[q], pb = pairB[q], w = pa + pb;
+          const bool start = first && (q == 0 || q == 4 || q == 7 || q == 9);
+          uint64_t da = smem_desc(sa + pa * PLANE_A + koff);
+          uint64_t db = smem_desc(sb + pb * PLANE_B + koff);
+          mma_bf16(tmem + (uint32_t)(w * BN), da, db, idesc, start ? 0u : 1u);
         }
       }
       mma_commit(&empty_bar[s]);
@@ -261,69 +238,104 @@ __global__ void __launch_bounds__(128, 1)
   __syncthreads();
   if (!failed) {
     const int row = warp * 32 + lane;
+    // class weights 64^-(w+2); exact integers combined small to large
+    const float wt[NACC] = {1.0f / 4096.0f, 1.0f / 262144.0f, 1.0f / 16777216.0f, 1.0f / 1073741824.0f};
 #pragma unroll 1
     for (int c = 0; c < BN / 32; c++) {
-      float v[32];
-      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), v);
+      float v[32], w[32];
+      const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32);
+      tmem_ld32(ta + 3 * BN, v);
+#pragma unroll
+      for (int j = 0; j < 32; j++) v[j] *= wt[3];
+#pragma unroll
+      for (int k = 2; k >= 0; k--) {
+        tmem_ld32(ta + k * BN, w);
+#pragma unroll
+        for (int j = 0; j < 32; j++) v[j] = fmaf(w[j], wt[k], v[j]);
+      }
 #pragma unroll
       for (int j = 0; j < 32; j++) tile[row * TS + c * 32 + j] = v[j];
     }
   }
   fence_before();
   __syncthreads();
+  float tmax = 0.0f;
   if (!failed) {
     const int col = threadIdx.x;
     const long long r = (long long)r_tile * BN + col;
     const int kind = (t % g.F) >= g.nac ? 1 : 0;
+    const float sin_t = g.in_scale[t];
     if (r < rows) {
-      const int cc = (int)(r / g.n), b = (int)(r % g.n);
+      const long long tb = (long long)t * g.n * rows;
 #pragma unroll 1
       for (int rr = 0; rr < BM; rr++) {
         const int a = a_tile * BM + rr;
         if (a >= g.n) break;
-        float v = tile[rr * TS + col];
-        if (g.epi != 0) {
-          // eigen-mode (i, j, k) = (b, c, a) of the z-contraction output
-          float H = etd_H(g, kind, b, cc, a);
-          float phi1, phi2;
-          etd_phi(H, g.dt, phi1, phi2);
-          if (fabsf(H) < 1.0e-8f) H = 0.0f;
-          if (g.epi == 1) {
-            const long long ao = (((long long)t * 3) * rows + (long long)a * g.n + cc) * g.kp + b;
-            const long long ps = rows * g.kp;
-            float uh = __bfloat162float(g.aux[ao]) + __bfloat162float(g.aux[ao + ps]) +
-                       __bfloat162float(g.aux[ao + 2 * ps]);
-            v = (1.0f - phi1 * H) * uh + phi1 * v;
-          } else {
-            v = phi2 * v;
-          }
+        float v = tile[rr * TS + col] * (sin_t * g.row_scale[a]);
+        const long long o = (long long)a * rows + r;  // = eigen-mode [k][j][i] of a z-contraction
+        if (g.epi == 1) {
+          const float uh = g.aux[tb + o];
+          const float4 c = g.coef[kind][o];  // (e_hi, e_lo, phi1_hi, phi1_lo)
+          v = fmaf(c.x, uh, fmaf(c.y, uh, fmaf(c.z, v, c.w * v)));
+        } else if (g.epi == 2) {
+          const float2 c = g.coef2[kind][o];  // (phi2_hi, phi2_lo)
+          v = fmaf(c.x, v, c.y * v);
         }
-        if (g.outmode == 0) {
-          const long long ps = rows * g.kp;
-          const long long o = (((long long)t * 3) * rows + (long long)a * g.n + cc) * g.kp + b;
-          __nv_bfloat16 h0, h1, h2;
-          split3(v, h0, h1, h2);
-          g.out_split[o] = h0;
-          g.out_split[o + ps] = h1;
-          g.out_split[o + 2 * ps] = h2;
-        } else {
-          const long long o = (long long)t * g.n * rows + (long long)a * rows + r;
-          if (g.outmode == 1) g.out_f32[o] = v;
-          else g.out_f32[o] += v;
-        }
+        if (g.outmode == 1) g.out[tb + o] = v;
+        else g.out[tb + o] += v;
+        tmax = fmaxf(tmax, fabsf(v));
       }
     }
   }
+  if (g.out_max) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) tmax = fmaxf(tmax, __shfl_xor_sync(0xffffffffu, tmax, off));
+    if (lane == 0) warp_max[warp] = tmax;
+  }
   __syncthreads();
-  if (failed && threadIdx.x == 0) atomicExch(g.err, 1);
+  if (threadIdx.x == 0) {
+    if (g.out_max && !failed) {
+      float m = fmaxf(fmaxf(warp_max[0], warp_max[1]), fmaxf(warp_max[2], warp_max[3]));
+      atomicMax(g.out_max + t, __float_as_uint(m));
+    }
+    if (failed) atomicExch(g.err, 1);
+  }
   if (warp == 2) {
     fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
   }
 }
 
-// FP32 field blocks (x fastest) -> split planes, rows (z, y), columns x.
-__global__ void split_fields_kernel(const float *__restrict__ u, const float *__restrict__ sub,
+// power-of-two scale S >= m (S = 1 for m = 0)
+__device__ __forceinline__ float pow2_scale(float m) {
+  if (!(m > 0.0f)) return 1.0f;
+  int e;
+  frexpf(m, &e);  // m = f 2^e, f in [0.5, 1)
+  return ldexpf(1.0f, e);
+}
+
+__global__ void tensor_max_kernel(const float *__restrict__ x, const float *__restrict__ sub,
+                                  unsigned int *__restrict__ max_bits, long long n3, int count) {
+  const long long total = n3 * count;
+  float m = 0.0f;
+  int t_cur = -1;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
+    int t = (int)(i / n3);
+    if (t != t_cur) {
+      if (t_cur >= 0 && m > 0.0f) atomicMax(max_bits + t_cur, __float_as_uint(m));
+      t_cur = t;
+      m = 0.0f;
+    }
+    float v = sub ? x[i] - sub[i] : x[i];
+    m = fmaxf(m, fabsf(v));
+  }
+  if (t_cur >= 0 && m > 0.0f) atomicMax(max_bits + t_cur, __float_as_uint(m));
+}
+
+// FP32 rows of n -> slices.  Each slice is exact: x/S and the residuals are
+// scaled by powers of two and reduced by their nearest integer.
+__global__ void slice_fields_kernel(const float *__restrict__ x, const float *__restrict__ sub,
+                                    const unsigned int *__restrict__ max_bits, float *__restrict__ scale,
                                     __nv_bfloat16 *__restrict__ out, int n, int kp, int count) {
   const long long n3 = (long long)n * n * n, rows = (long long)n * n;
   const long long total = n3 * count;
@@ -331,30 +343,92 @@ __global__ void split_fields_kernel(const float *__restrict__ u, const float *__
     int t = (int)(i / n3);
     long long l = i - (long long)t * n3;
     long long row = l / n;
-    int x = (int)(l % n);
-    __nv_bfloat16 a, b, c;
-    split3(sub ? u[i] - sub[i] : u[i], a, b, c);
-    long long o = (((long long)t * 3) * rows + row) * kp + x;
-    out[o] = a;
-    out[o + rows * kp] = b;
-    out[o + 2 * rows * kp] = c;
+    int k = (int)(l % n);
+    const float S = pow2_scale(__uint_as_float(max_bits[t]));
+    if (l == 0) scale[t] = S;
+    float r = (sub ? x[i] - sub[i] : x[i]) * (1.0f / S);
+    const long long o = ((long long)t * TC_PLANES * rows + row) * kp + k;
+#pragma unroll
+    for (int p = 0; p < TC_PLANES; p++) {
+      float y = r * 64.0f;
+      float d = rintf(y);
+      r = y - d;
+      out[o + (long long)p * rows * kp] = __float2bfloat16_rn(d);
+    }
   }
 }
 
-// FP64 row-major n x n matrix -> zero-padded split planes [3][n][kp].
-__global__ void split_matrix_kernel(const double *__restrict__ m, __nv_bfloat16 *__restrict__ out, int n, int kp) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n * kp; i += gridDim.x * blockDim.x) {
-    int r = i / kp, c = i % kp;
-    // split the double itself: hi from the double, the rest from residuals
-    double x = c < n ? m[(long long)r * n + c] : 0.0;
-    __nv_bfloat16 a = __double2bfloat16(x);
-    double rem = x - (double)__bfloat162float(a);
-    __nv_bfloat16 b = __double2bfloat16(rem);
-    rem -= (double)__bfloat162float(b);
-    __nv_bfloat16 cc = __double2bfloat16(rem);
-    out[i] = a;
-    out[i + (long long)n * kp] = b;
-    out[i + 2LL * n * kp] = cc;
+// FP64 matrix rows -> slices with a power-of-two scale per row.
+__global__ void slice_matrix_kernel(const double *__restrict__ m, __nv_bfloat16 *__restrict__ out,
+                                    float *__restrict__ row_scale, int n, int kp) {
+  __shared__ double smax[128];
+  for (int r = blockIdx.x; r < n; r += gridDim.x) {
+    double mx = 0.0;
+    for (int c = threadIdx.x; c < n; c += blockDim.x) mx = fmax(mx, fabs(m[(long long)r * n + c]));
+    smax[threadIdx.x] = mx;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+      if (threadIdx.x < w) smax[threadIdx.x] = fmax(smax[threadIdx.x], smax[threadIdx.x + w]);
+      __syncthreads();
+    }
+    double S = 1.0;
+    if (smax[0] > 0.0) {
+      int e;
+      frexp(smax[0], &e);
+      S = ldexp(1.0, e);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) row_scale[r] = (float)S;
+    for (int c = threadIdx.x; c < kp; c += blockDim.x) {
+      double v = c < n ? m[(long long)r * n + c] / S : 0.0;
+      for (int p = 0; p < TC_PLANES; p++) {
+        double y = v * 64.0;
+        double d = rint(y);
+        v = y - d;
+        out[((long long)p * n + r) * kp + c] = __float2bfloat16_rn((float)d);
+      }
+    }
+  }
+}
+
+// ETD coefficients in FP64 (the plain form's ac_init_phi / ch_init_phi and
+// ac_updateU_new / ch_updateU_new arithmetic), stored as FP32 hi + lo.
+__global__ void coef_kernel(float4 *coef, float2 *coef2, int n, int kind, const double *dx, const double *dy,
+                            const double *dz, double kkx, double kky, double kkz, double epn2, double dt, double L,
+                            double K) {
+  const long long n3 = (long long)n * n * n;
+  for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < n3; o += (long long)gridDim.x * blockDim.x) {
+    int i = (int)(o % n), j = (int)((o / n) % n), k = (int)(o / ((long long)n * n));
+    double tmp, H;
+    if (kind == 0) {
+      tmp = kkz * dz[k] + kky * dy[j] + kkx * dx[i];
+      H = -L * (tmp * epn2 - K);
+    } else {
+      tmp = dz[k] + dy[j] + dx[i];
+      H = L * (tmp * tmp * epn2 - K * tmp);
+    }
+    double p1, p2;
+    if (fabs(H) > 1.0e-8) {
+      p1 = -expm1(-dt * H) / H;
+      p2 = (1.0 - p1 / dt) / H;
+    } else {
+      p1 = dt;
+      p2 = dt / 2;
+    }
+    double Hu = fabs(H) < 1.0e-8 ? 0.0 : H;
+    double e = 1.0 - p1 * Hu;
+    float4 c;
+    c.x = (float)e;
+    c.y = (float)(e - (double)c.x);
+    c.z = (float)p1;
+    c.w = (float)(p1 - (double)c.z);
+    coef[o] = c;
+    if (coef2) {
+      float2 c2;
+      c2.x = (float)p2;
+      c2.y = (float)(p2 - (double)c2.x);
+      coef2[o] = c2;
+    }
   }
 }
 
@@ -381,28 +455,51 @@ static cudaError_t make_map(CUtensorMap *map, const void *ptr, int kp, long long
   cuuint32_t box[3] = {(cuuint32_t)tc::BK, (cuuint32_t)box_rows, 1};
   cuuint32_t estr[3] = {1, 1, 1};
   CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void *>(ptr), dims, strides, box, estr,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
 int tc_kp(int n) { return (n + 7) / 8 * 8; }
 
-cudaError_t tc_split_matrix(const double *m, __nv_bfloat16 *out, int n, cudaStream_t s) {
-  tc::split_matrix_kernel<<<(n * tc_kp(n) + 255) / 256, 256, 0, s>>>(m, out, n, tc_kp(n));
-  launch_counter()++;
-  return cudaGetLastError();
-}
-
-cudaError_t tc_split_fields(const float *u, const float *sub, __nv_bfloat16 *out, int n, int count, cudaStream_t s) {
-  long long total = (long long)n * n * n * count;
+static int grid_cap(long long total) {
   long long b = (total + 255) / 256;
-  tc::split_fields_kernel<<<(int)(b > 152 * 32 ? 152 * 32 : b), 256, 0, s>>>(u, sub, out, n, tc_kp(n), count);
+  return (int)(b > 152 * 32 ? 152 * 32 : (b < 1 ? 1 : b));
+}
+
+cudaError_t tc_slice_matrix(const double *m, __nv_bfloat16 *planes, float *row_scale, int n, cudaStream_t s) {
+  tc::slice_matrix_kernel<<<n < 1024 ? n : 1024, 128, 0, s>>>(m, planes, row_scale, n, tc_kp(n));
   launch_counter()++;
   return cudaGetLastError();
 }
 
-cudaError_t launch_modeprod_tc(const __nv_bfloat16 *mat, const __nv_bfloat16 *in, int count, const TcArgs &args,
+cudaError_t tc_tensor_max(const float *x, const float *sub, unsigned int *max_bits, int n, int count, cudaStream_t s) {
+  long long n3 = (long long)n * n * n;
+  tc::tensor_max_kernel<<<grid_cap(n3 * count), 256, 0, s>>>(x, sub, max_bits, n3, count);
+  launch_counter()++;
+  return cudaGetLastError();
+}
+
+cudaError_t tc_slice_fields(const float *x, const float *sub, const unsigned int *max_bits, float *scale,
+                            __nv_bfloat16 *planes, int n, int count, cudaStream_t s) {
+  long long total = (long long)n * n * n * count;
+  tc::slice_fields_kernel<<<grid_cap(total), 256, 0, s>>>(x, sub, max_bits, scale, planes, n, tc_kp(n), count);
+  launch_counter()++;
+  return cudaGetLastError();
+}
+
+cudaError_t tc_make_coefs(float4 *coef, float2 *coef2, int n, int kind, const double *dx, const double *dy,
+                          const double *dz, const double *kk, double epn2, double dt, double L, double K,
+                          cudaStream_t s) {
+  long long n3 = (long long)n * n * n;
+  long long b = (n3 + 255) / 256;
+  tc::coef_kernel<<<(int)(b > 152 * 16 ? 152 * 16 : b), 256, 0, s>>>(coef, coef2, n, kind, dx, dy, dz, kk[0], kk[1],
+                                                                     kk[2], epn2, dt, L, K);
+  launch_counter()++;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_modeprod_tc(const __nv_bfloat16 *mat, const __nv_bfloat16 *planes, int count, const TcArgs &args,
                                cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
@@ -412,10 +509,11 @@ cudaError_t launch_modeprod_tc(const __nv_bfloat16 *mat, const __nv_bfloat16 *in
     attr = true;
   }
   const int n = args.n, kp = tc_kp(n);
+  if ((long long)tc::BK * ((n + tc::BK - 1) / tc::BK) > 1040) return cudaErrorInvalidValue;  // exactness bound
   CUtensorMap ma, mb;
   cudaError_t e;
-  if ((e = make_map(&ma, mat, kp, n, 3, tc::BM)) != cudaSuccess) return e;
-  if ((e = make_map(&mb, in, kp, (long long)n * n, 3 * count, tc::BN)) != cudaSuccess) return e;
+  if ((e = make_map(&ma, mat, kp, n, TC_PLANES, tc::BM)) != cudaSuccess) return e;
+  if ((e = make_map(&mb, planes, kp, (long long)n * n, TC_PLANES * count, tc::BN)) != cudaSuccess) return e;
   TcArgs g = args;
   g.kp = kp;
   g.kblocks = (n + tc::BK - 1) / tc::BK;

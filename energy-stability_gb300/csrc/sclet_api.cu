@@ -49,10 +49,15 @@ struct sclet_ctx {
   double *felas = nullptr, *scratch = nullptr, *shell = nullptr;
   double *V[3] = {nullptr, nullptr, nullptr}, *Vi[3] = {nullptr, nullptr, nullptr};
   double *phi1[2] = {nullptr, nullptr}, *phi2[2] = {nullptr, nullptr};
-  // MIXED form: fstate2 = [u (F) | rhs1 (F)] in FP32, split planes Sa / Sb
+  // MIXED form: fstate2 = [u (F) | rhs1 (F)] in FP32; FP32 work tensors W1, W2
+  // (2F blocks each); slice planes P of up to 2F tensors; per-tensor max
+  // (float bits) and scale buffers; sliced matrices with row scales
   float *fstate2 = nullptr, *frhs2 = nullptr, *ffelas = nullptr, *fscratch = nullptr, *fshell = nullptr;
-  float *ddf[3] = {nullptr, nullptr, nullptr};
-  __nv_bfloat16 *Sa = nullptr, *Sb = nullptr, *matV = nullptr, *matVi = nullptr;
+  float *W1 = nullptr, *W2 = nullptr, *scaleP = nullptr, *rsV = nullptr, *rsVi = nullptr;
+  unsigned int *maxA = nullptr, *maxB = nullptr;
+  __nv_bfloat16 *P = nullptr, *matV = nullptr, *matVi = nullptr;
+  float4 *coef[2] = {nullptr, nullptr};   // ETD1 coefficient pairs per field kind
+  float2 *coef2[2] = {nullptr, nullptr};  // ETD2 phi2 pairs per field kind
   double *stage64 = nullptr;  // n^3 FP64 staging block for host transfers
   // profiling
   bool profiling = false;
@@ -133,25 +138,27 @@ int fail(sclet_ctx *ctx, int code, const std::string &msg) {
 int upload_eigen(sclet_ctx *ctx, const double *d, const double *v, const double *vi) {
   const int n = ctx->n;
   std::vector<double> ds(n);
-  std::vector<float> dsf(n);
   for (int ax = 0; ax < 3; ax++) {
     double h = ctx->ph.h[ax];
     // DDX[l] = DDX_b[l] / hx / hx (vars.c:510-513)
     for (int l = 0; l < n; l++) {
       ds[l] = d[l] / h / h;
-      dsf[l] = (float)ds[l];
     }
     CK(cudaMemcpyAsync(ctx->dd[ax], ds.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
-    if (mixed(ctx)) CK(cudaMemcpyAsync(ctx->ddf[ax], dsf.data(), sizeof(float) * n, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
   }
   if (mixed(ctx)) {
     // the stage block holds the FP64 matrices while they are split
     CK(cudaMemcpyAsync(ctx->stage64, vi, sizeof(double) * n * n, cudaMemcpyHostToDevice, ctx->stream));
-    CK(tc_split_matrix(ctx->stage64, ctx->matVi, n, ctx->stream));
+    CK(tc_slice_matrix(ctx->stage64, ctx->matVi, ctx->rsVi, n, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     CK(cudaMemcpyAsync(ctx->stage64, v, sizeof(double) * n * n, cudaMemcpyHostToDevice, ctx->stream));
-    CK(tc_split_matrix(ctx->stage64, ctx->matV, n, ctx->stream));
+    CK(tc_slice_matrix(ctx->stage64, ctx->matV, ctx->rsV, n, ctx->stream));
+    const sclet_params &p = ctx->p;
+    const double kk[3] = {p.kkx, p.kky, p.kkz};
+    for (int kind = 0; kind < 2; kind++)
+      CK(tc_make_coefs(ctx->coef[kind], ctx->coef2[kind], n, kind, ctx->dd[0], ctx->dd[1], ctx->dd[2], kk, p.epn2,
+                       p.dt, p.landau[7 + 2 * kind], p.landau[8 + 2 * kind], ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     return SCLET_OK;
   }
@@ -188,31 +195,8 @@ EtdCoef etd_coef(sclet_ctx *ctx) {
   return ec;
 }
 
-TcArgs tc_args(sclet_ctx *ctx, int count, int epi, int outmode) {
-  TcArgs g;
-  memset(&g, 0, sizeof g);
-  g.n = ctx->n;
-  g.count = count;
-  g.epi = epi;
-  g.outmode = outmode;
-  for (int a = 0; a < 3; a++) g.dd[a] = ctx->ddf[a];
-  g.kk[0] = (float)ctx->p.kkx;
-  g.kk[1] = (float)ctx->p.kky;
-  g.kk[2] = (float)ctx->p.kkz;
-  g.epn2 = (float)ctx->p.epn2;
-  g.dt = (float)ctx->p.dt;
-  g.LE = (float)ctx->ph.LE;
-  g.KE = (float)ctx->ph.KE;
-  g.LCI = (float)ctx->ph.LCI;
-  g.KCI = (float)ctx->ph.KCI;
-  g.nac = ctx->nac;
-  g.F = ctx->F;
-  g.err = ctx->dev_err;
-  return g;
-}
-
-// Elements of one split tensor (three planes of n*n rows of kp)
-long long split_stride(const sclet_ctx *ctx) { return 3LL * ctx->n * ctx->n * tc_kp(ctx->n); }
+// Elements of one sliced tensor (TC_PLANES planes of n*n rows of kp)
+long long plane_stride(const sclet_ctx *ctx) { return (long long)TC_PLANES * ctx->n * ctx->n * tc_kp(ctx->n); }
 
 void stage_begin(sclet_ctx *ctx, int cls, StageEv &ev) {
   if (!ctx->profiling) return;
@@ -278,14 +262,14 @@ void sclet_destroy(sclet_ctx *ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   void *bufs[] = {ctx->state2, ctx->rhs2, ctx->A, ctx->B, ctx->felas, ctx->scratch, ctx->shell, ctx->elam,
                   ctx->partials, ctx->diag, ctx->phi1[0], ctx->phi1[1], ctx->phi2[0], ctx->phi2[1], ctx->dev_err,
-                  ctx->fstate2, ctx->frhs2, ctx->ffelas, ctx->fscratch, ctx->fshell, ctx->Sa, ctx->Sb, ctx->matV,
-                  ctx->matVi, ctx->stage64};
+                  ctx->fstate2, ctx->frhs2, ctx->ffelas, ctx->fscratch, ctx->fshell, ctx->W1, ctx->W2, ctx->P,
+                  ctx->scaleP, ctx->rsV, ctx->rsVi, ctx->maxA, ctx->maxB, ctx->matV, ctx->matVi, ctx->stage64,
+                  ctx->coef[0], ctx->coef[1], ctx->coef2[0], ctx->coef2[1]};
   for (void *b : bufs) cudaFree(b);
   for (int a = 0; a < 3; a++) {
     cudaFree(ctx->V[a]);
     cudaFree(ctx->Vi[a]);
     cudaFree(ctx->dd[a]);
-    cudaFree(ctx->ddf[a]);
   }
   for (auto &e : ctx->evs) {
     cudaEventDestroy(e.a);
@@ -414,16 +398,24 @@ int sclet_create(const sclet_params *p, int precision, int device, sclet_ctx **o
     CC(cudaMemsetAsync(ctx->ffelas, 0, nfel * blk, s));
     CC(cudaMalloc(&ctx->fscratch, 2 * blk));
     CC(cudaMalloc(&ctx->fshell, sizeof(float) * F * shell_count(n)));
-    const size_t sbytes = sizeof(__nv_bfloat16) * split_stride(ctx) * 2 * F;
-    // pad columns of the split tensors are never written and must stay zero
-    CC(cudaMalloc(&ctx->Sa, sbytes));
-    CC(cudaMalloc(&ctx->Sb, sbytes));
-    CC(cudaMemsetAsync(ctx->Sa, 0, sbytes, s));
-    CC(cudaMemsetAsync(ctx->Sb, 0, sbytes, s));
-    CC(cudaMalloc(&ctx->matV, sizeof(__nv_bfloat16) * 3 * n * tc_kp(n)));
-    CC(cudaMalloc(&ctx->matVi, sizeof(__nv_bfloat16) * 3 * n * tc_kp(n)));
-    for (int a = 0; a < 3; a++) CC(cudaMalloc(&ctx->ddf[a], sizeof(float) * n));
+    CC(cudaMalloc(&ctx->W1, 2 * F * blk));
+    CC(cudaMalloc(&ctx->W2, 2 * F * blk));
+    const size_t pbytes = sizeof(__nv_bfloat16) * plane_stride(ctx) * 2 * F;
+    // pad columns of the slice planes are never written and must stay zero
+    CC(cudaMalloc(&ctx->P, pbytes));
+    CC(cudaMemsetAsync(ctx->P, 0, pbytes, s));
+    CC(cudaMalloc(&ctx->scaleP, sizeof(float) * 2 * F));
+    CC(cudaMalloc(&ctx->maxA, sizeof(unsigned int) * 2 * F));
+    CC(cudaMalloc(&ctx->maxB, sizeof(unsigned int) * 2 * F));
+    CC(cudaMalloc(&ctx->matV, sizeof(__nv_bfloat16) * TC_PLANES * n * tc_kp(n)));
+    CC(cudaMalloc(&ctx->matVi, sizeof(__nv_bfloat16) * TC_PLANES * n * tc_kp(n)));
+    CC(cudaMalloc(&ctx->rsV, sizeof(float) * n));
+    CC(cudaMalloc(&ctx->rsVi, sizeof(float) * n));
     CC(cudaMalloc(&ctx->stage64, sizeof(double) * ctx->n3));
+    for (int k = 0; k < 2; k++) {
+      CC(cudaMalloc(&ctx->coef[k], sizeof(float4) * ctx->n3));
+      if (p->etd2) CC(cudaMalloc(&ctx->coef2[k], sizeof(float2) * ctx->n3));
+    }
   }
   {
     // energy tensors: the gradient operator of the dynamics
@@ -546,48 +538,86 @@ int sclet_calc_rhs(sclet_ctx *ctx, int slot) {
   return SCLET_OK;
 }
 
-// Mixed form of the transforms: split, three forward products (the third of
-// the right-hand-side tensors fuses the ETD update), three inverse products.
+// One fixed-point tensor-core product of `count` sliced tensors (planes at
+// `planes`, scales at `scale`) into FP32 `out`, recording max |out| when
+// out_max is given.
+static cudaError_t tc_prod(sclet_ctx *ctx, bool inverse, const __nv_bfloat16 *planes, const float *scale, int count,
+                           float *out, unsigned int *out_max, int epi, const float *aux, int outmode) {
+  TcArgs g;
+  memset(&g, 0, sizeof g);
+  g.n = ctx->n;
+  g.count = count;
+  g.epi = epi;
+  g.outmode = outmode;
+  g.aux = aux;
+  g.out = out;
+  g.out_max = out_max;
+  g.in_scale = scale;
+  g.row_scale = inverse ? ctx->rsV : ctx->rsVi;
+  for (int k = 0; k < 2; k++) {
+    g.coef[k] = ctx->coef[k];
+    g.coef2[k] = ctx->coef2[k];
+  }
+  g.nac = ctx->nac;
+  g.F = ctx->F;
+  g.err = ctx->dev_err;
+  if (out_max) {
+    cudaError_t e = cudaMemsetAsync(out_max, 0, sizeof(unsigned int) * count, ctx->stream);
+    if (e != cudaSuccess) return e;
+  }
+  return launch_modeprod_tc(inverse ? ctx->matV : ctx->matVi, planes, count, g, ctx->stream);
+}
+
+// x (count FP32 blocks, minus sub) -> slice planes P with scales from max_bits
+static cudaError_t tc_slice(sclet_ctx *ctx, const float *x, const float *sub, const unsigned int *max_bits, int count,
+                            __nv_bfloat16 *planes, float *scale) {
+  return tc_slice_fields(x, sub, max_bits, scale, planes, ctx->n, count, ctx->stream);
+}
+
+// Mixed form of the transforms (ScLETD.c:105-142): V^-1 along x and y for u
+// and N1 together, along z for u, then for N1 with the ETD update fused; V
+// along x, y, z back to the FP32 state.  Each product records the max of its
+// output, from which the next slicing takes its scale.
 static int etd_update_mixed(sclet_ctx *ctx) {
   const int F = ctx->F;
-  const long long ss = split_stride(ctx);
+  const long long ps = plane_stride(ctx);
   cudaStream_t s = ctx->stream;
-  CK(tc_split_fields(ctx->fstate2, nullptr, ctx->Sb, ctx->n, 2 * F, s));
-  TcArgs g = tc_args(ctx, 2 * F, 0, 0);
-  g.out_split = ctx->Sa;
-  CK(launch_modeprod_tc(ctx->matVi, ctx->Sb, 2 * F, g, s));
-  g.out_split = ctx->Sb;
-  CK(launch_modeprod_tc(ctx->matVi, ctx->Sa, 2 * F, g, s));
-  g = tc_args(ctx, F, 0, 0);
-  g.out_split = ctx->Sa;
-  CK(launch_modeprod_tc(ctx->matVi, ctx->Sb, F, g, s));
-  g = tc_args(ctx, F, 1, 0);
-  g.aux = ctx->Sa;
-  g.out_split = ctx->Sa;
-  CK(launch_modeprod_tc(ctx->matVi, ctx->Sb + F * ss, F, g, s));
-  g = tc_args(ctx, F, 0, 0);
-  g.out_split = ctx->Sb;
-  CK(launch_modeprod_tc(ctx->matV, ctx->Sa, F, g, s));
-  g.out_split = ctx->Sa;
-  CK(launch_modeprod_tc(ctx->matV, ctx->Sb, F, g, s));
-  g = tc_args(ctx, F, 0, 1);
-  g.out_f32 = fu_of(ctx);
-  CK(launch_modeprod_tc(ctx->matV, ctx->Sa, F, g, s));
+  CK(cudaMemsetAsync(ctx->maxA, 0, sizeof(unsigned int) * 2 * F, s));
+  CK(tc_tensor_max(ctx->fstate2, nullptr, ctx->maxA, ctx->n, 2 * F, s));
+  CK(tc_slice(ctx, ctx->fstate2, nullptr, ctx->maxA, 2 * F, ctx->P, ctx->scaleP));
+  CK(tc_prod(ctx, false, ctx->P, ctx->scaleP, 2 * F, ctx->W1, ctx->maxB, 0, nullptr, 1));
+  CK(tc_slice(ctx, ctx->W1, nullptr, ctx->maxB, 2 * F, ctx->P, ctx->scaleP));
+  CK(tc_prod(ctx, false, ctx->P, ctx->scaleP, 2 * F, ctx->W2, ctx->maxA, 0, nullptr, 1));
+  CK(tc_slice(ctx, ctx->W2, nullptr, ctx->maxA, 2 * F, ctx->P, ctx->scaleP));
+  CK(tc_prod(ctx, false, ctx->P, ctx->scaleP, F, ctx->W1, nullptr, 0, nullptr, 1));
+  CK(tc_prod(ctx, false, ctx->P + F * ps, ctx->scaleP + F, F, ctx->W1, ctx->maxB, 1, ctx->W1, 1));
+  CK(tc_slice(ctx, ctx->W1, nullptr, ctx->maxB, F, ctx->P, ctx->scaleP));
+  CK(tc_prod(ctx, true, ctx->P, ctx->scaleP, F, ctx->W2, ctx->maxA, 0, nullptr, 1));
+  CK(tc_slice(ctx, ctx->W2, nullptr, ctx->maxA, F, ctx->P, ctx->scaleP));
+  CK(tc_prod(ctx, true, ctx->P, ctx->scaleP, F, ctx->W1, ctx->maxB, 0, nullptr, 1));
+  CK(tc_slice(ctx, ctx->W1, nullptr, ctx->maxB, F, ctx->P, ctx->scaleP));
+  CK(tc_prod(ctx, true, ctx->P, ctx->scaleP, F, fu_of(ctx), nullptr, 0, nullptr, 1));
   return SCLET_OK;
 }
 
+// ETD2 corrector (ScLETD.c:159-188): u += V phi2 V^-1 (N2 - N1).
 static int etd2_correct_mixed(sclet_ctx *ctx) {
   const int F = ctx->F;
   cudaStream_t s = ctx->stream;
-  CK(tc_split_fields(ctx->frhs2, frhs1_of(ctx), ctx->Sb, ctx->n, F, s));
-  const __nv_bfloat16 *mats[6] = {ctx->matVi, ctx->matVi, ctx->matVi, ctx->matV, ctx->matV, ctx->matV};
-  __nv_bfloat16 *bufs[2] = {ctx->Sb, ctx->Sa};
-  for (int k = 0; k < 6; k++) {
-    TcArgs g = tc_args(ctx, F, k == 2 ? 2 : 0, k == 5 ? 2 : 0);
-    g.out_split = bufs[(k + 1) % 2];
-    g.out_f32 = fu_of(ctx);
-    CK(launch_modeprod_tc(mats[k], bufs[k % 2], F, g, s));
-  }
+  CK(cudaMemsetAsync(ctx->maxA, 0, sizeof(unsigned int) * F, s));
+  CK(tc_tensor_max(ctx->frhs2, frhs1_of(ctx), ctx->maxA, ctx->n, F, s));
+  CK(tc_slice(ctx, ctx->frhs2, frhs1_of(ctx), ctx->maxA, F, ctx->P, ctx->scaleP));
+  CK(tc_prod(ctx, false, ctx->P, ctx->scaleP, F, ctx->W1, ctx->maxB, 0, nullptr, 1));
+  CK(tc_slice(ctx, ctx->W1, nullptr, ctx->maxB, F, ctx->P, ctx->scaleP));
+  CK(tc_prod(ctx, false, ctx->P, ctx->scaleP, F, ctx->W2, ctx->maxA, 0, nullptr, 1));
+  CK(tc_slice(ctx, ctx->W2, nullptr, ctx->maxA, F, ctx->P, ctx->scaleP));
+  CK(tc_prod(ctx, false, ctx->P, ctx->scaleP, F, ctx->W1, ctx->maxB, 2, nullptr, 1));
+  CK(tc_slice(ctx, ctx->W1, nullptr, ctx->maxB, F, ctx->P, ctx->scaleP));
+  CK(tc_prod(ctx, true, ctx->P, ctx->scaleP, F, ctx->W2, ctx->maxA, 0, nullptr, 1));
+  CK(tc_slice(ctx, ctx->W2, nullptr, ctx->maxA, F, ctx->P, ctx->scaleP));
+  CK(tc_prod(ctx, true, ctx->P, ctx->scaleP, F, ctx->W1, ctx->maxB, 0, nullptr, 1));
+  CK(tc_slice(ctx, ctx->W1, nullptr, ctx->maxB, F, ctx->P, ctx->scaleP));
+  CK(tc_prod(ctx, true, ctx->P, ctx->scaleP, F, fu_of(ctx), nullptr, 0, nullptr, 2));
   return SCLET_OK;
 }
 
@@ -693,16 +723,16 @@ int sclet_check_soln(sclet_ctx *ctx, int energy_form, sclet_diag *out) {
 int sclet_mode_product(sclet_ctx *ctx, int inverse, const double *in, double *out) {
   const long long n3 = ctx->n3;
   if (mixed(ctx)) {
-    // in -> FP32 scratch, split, product, FP32 -> host FP64
+    // in -> FP32 scratch, slices, product, FP32 -> host FP64
     float *tmp = ctx->fscratch;
     CK(cudaMemcpyAsync(ctx->stage64, in, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
     f64_to_f32<<<grid_of(n3), 256, 0, ctx->stream>>>(ctx->stage64, tmp, n3);
     launch_counter()++;
     CK(cudaGetLastError());
-    CK(tc_split_fields(tmp, nullptr, ctx->Sb, ctx->n, 1, ctx->stream));
-    TcArgs g = tc_args(ctx, 1, 0, 1);
-    g.out_f32 = tmp + n3;
-    CK(launch_modeprod_tc(inverse ? ctx->matV : ctx->matVi, ctx->Sb, 1, g, ctx->stream));
+    CK(cudaMemsetAsync(ctx->maxA, 0, sizeof(unsigned int), ctx->stream));
+    CK(tc_tensor_max(tmp, nullptr, ctx->maxA, ctx->n, 1, ctx->stream));
+    CK(tc_slice(ctx, tmp, nullptr, ctx->maxA, 1, ctx->P, ctx->scaleP));
+    CK(tc_prod(ctx, inverse != 0, ctx->P, ctx->scaleP, 1, tmp + n3, nullptr, 0, nullptr, 1));
     f32_to_f64<<<grid_of(n3), 256, 0, ctx->stream>>>(tmp + n3, ctx->stage64, n3);
     launch_counter()++;
     CK(cudaGetLastError());

@@ -6,26 +6,43 @@
 
 namespace sclet {
 
+constexpr int TC_PLANES = 4;  // fixed-point slices per operand (6 bits each)
+
 struct TcArgs {
   int n, kp, kblocks, count;
-  int epi;                    // 0 none, 1 ETD1 update with aux = uhat planes, 2 phi2 scaling
-  int outmode;                // 0 split planes, 1 FP32 store, 2 FP32 accumulate
-  const __nv_bfloat16 *aux;   // split planes of uhat (same layout as out_split)
-  __nv_bfloat16 *out_split;   // [count][3][n*n][kp]
-  float *out_f32;             // [count][n^3]
-  const float *dd[3];         // eigenvalues / h^2 per axis
-  float kk[3], epn2, dt, LE, KE, LCI, KCI;
+  int epi;                  // 0 none, 1 ETD1 update (aux = uhat), 2 phi2 scaling
+  int outmode;              // 1 FP32 store, 2 FP32 accumulate
+  const float *aux;         // [count][n^3] FP32 uhat, same layout as out
+  float *out;               // [count][n^3] FP32, rotated layout
+  unsigned int *out_max;    // [count] max |out| as float bits (atomicMax), or null
+  const float *in_scale;    // [count] power-of-two scale of each input tensor's slices
+  const float *row_scale;   // [n] power-of-two scale of each matrix row's slices
+  // per field kind (0 AC, 1 CH), per eigen-mode [k][j][i]: ETD1
+  // (e = 1 - phi1 H, phi1) and ETD2 (phi2) coefficients computed in FP64
+  // (ac_init_phi / ch_init_phi, vars.c:302-359) as hi + lo FP32 pairs
+  const float4 *coef[2];
+  const float2 *coef2[2];
   int nac, F;
-  int *err;                   // set to 1 when a bounded wait gives up
+  int *err;                 // set to 1 when a bounded wait gives up
 };
 
 int tc_kp(int n);
-// [3][n][kp] split planes of a row-major FP64 matrix (zero padded columns)
-cudaError_t tc_split_matrix(const double *m, __nv_bfloat16 *out, int n, cudaStream_t s);
-// FP32 field blocks (minus `sub` when given) -> split planes [count][3][n*n][kp]
-cudaError_t tc_split_fields(const float *u, const float *sub, __nv_bfloat16 *out, int n, int count, cudaStream_t s);
+// Row-major FP64 n x n matrix -> TC_PLANES slice planes [p][n][kp] (zero padded
+// columns) and the power-of-two scale of each row.
+cudaError_t tc_slice_matrix(const double *m, __nv_bfloat16 *planes, float *row_scale, int n, cudaStream_t s);
+// max |x - sub| of each FP32 block [count][n^3] into max_bits[count] (atomicMax on
+// the float bits; zero it first).  `sub` may be null.
+cudaError_t tc_tensor_max(const float *x, const float *sub, unsigned int *max_bits, int n, int count, cudaStream_t s);
+// FP32 blocks (x - sub), rows of n -> slice planes [count][p][n*n][kp], with
+// scale[t] = 2^ceil(log2 max_t) (from max_bits) recorded for the product.
+cudaError_t tc_slice_fields(const float *x, const float *sub, const unsigned int *max_bits, float *scale,
+                            __nv_bfloat16 *planes, int n, int count, cudaStream_t s);
+// ETD coefficient tables of one field kind (see TcArgs::coef)
+cudaError_t tc_make_coefs(float4 *coef, float2 *coef2, int n, int kind, const double *dx, const double *dy,
+                          const double *dz, const double *kk, double epn2, double dt, double L, double K,
+                          cudaStream_t s);
 // out[t] = mat x in[t] (contracting the row axis, rotating), count tensors
-cudaError_t launch_modeprod_tc(const __nv_bfloat16 *mat, const __nv_bfloat16 *in, int count, const TcArgs &args,
+cudaError_t launch_modeprod_tc(const __nv_bfloat16 *mat, const __nv_bfloat16 *planes, int count, const TcArgs &args,
                                cudaStream_t s);
 
 }  // namespace sclet

@@ -1,0 +1,77 @@
+"""Mixed-precision form (SCLET_MIXED): split-BF16 tcgen05 eigenbasis products
+with FP32 accumulation, FP32 stencils and FFT, FP64 diagnostics.  Checked
+against the plain FP64 form of the same library (itself checked against the
+reference and the oracle): rel L2 <= 1e-5 per field, energy within 1e-6
+relative."""
+import tempfile
+
+import numpy as np
+import pytest
+
+import bench
+import cases
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def params_for(sg, case):
+    with tempfile.TemporaryDirectory() as td:
+        cases.write_case(case, td, eigen=False, fields=False)
+        return sg.read_case(td, case.suffix)
+
+
+@pytest.mark.parametrize("big_n", [32, 64, 192])
+def test_tc_mode_product_accuracy(big_n, sclet_lib):
+    sg = sclet_lib
+    case = cases.Case(big_n=big_n, nac=1, nch=0, elastic=0, steps=1, suffix="mp")
+    s = sg.Solver(params_for(sg, case), sg.MIXED)
+    n = s.n
+    a = np.random.default_rng(1).standard_normal((n, n, n))
+    d, v, vi = cases.eigen_variant(n, 3)
+    a32 = a.astype(np.float32).astype(np.float64)
+    for inverse, m in ((False, vi), (True, v)):
+        got = s.mode_product(a, inverse)
+        want = np.einsum("pa,cba->pcb", m, a32)
+        assert rel(got, want) <= 1e-7, (n, inverse, rel(got, want))
+    s.sync()
+    s.close()
+
+
+def _mixed_vs_fp64(sg, case, steps):
+    p = params_for(sg, case)
+    u0 = bench.block_fields(case)
+    out = {}
+    for prec in (sg.FP64, sg.MIXED):
+        s = sg.Solver(p, prec)
+        s.set_fields(u0)
+        energies = []
+        for k in range(steps):
+            s.step(1)
+            energies.append(s.check_soln()[0, 3])
+        out[prec] = (s.get_fields(), np.array(energies))
+        s.sync()
+        s.close()
+    (u64, e64), (u32, e32) = out[sg.FP64], out[sg.MIXED]
+    errs = [rel(u32[f][2:-2, 2:-2, 2:-2], u64[f][2:-2, 2:-2, 2:-2]) for f in range(u64.shape[0])]
+    eerr = np.max(np.abs(e32 - e64) / np.abs(e64))
+    return errs, eerr
+
+
+def test_mixed_matches_fp64_beta_omega_64(sclet_lib):
+    """64^3 beta->omega physics (4 order parameters, elasticity), 200 steps."""
+    case = cases.Case(big_n=64, steps=200, seed=77, suffix="m64")
+    errs, eerr = _mixed_vs_fp64(sclet_lib, case, 200)
+    assert max(errs) <= 1e-5, errs
+    assert eerr <= 1e-6, eerr
+
+
+def test_mixed_matches_fp64_beta_alpha_192(sclet_lib):
+    """The 192^3 coupled CH + AC workload of the benchmark, 50 steps."""
+    case = bench.workload(192, seed=9)
+    errs, eerr = _mixed_vs_fp64(sclet_lib, case, 50)
+    assert max(errs) <= 1e-5, errs
+    assert eerr <= 1e-6, eerr
