@@ -13,8 +13,11 @@
 // k times K <= 1040), so the tensor-core accumulation is exact and unbiased;
 // the epilogue combines the four classes with round-to-nearest FP32 adds.
 //
-// Scales: per matrix row (static) and per input tensor (2^ceil(log2 max|x|),
-// from the max that the producing kernel records).
+// Scales: powers of two per matrix row (static) and per input row (one 1-D
+// line along the contracted axis, 2^ceil(log2 max|x|) over the line, found by
+// the slicing kernel), so a line holding a spectral peak or a boundary-lifting
+// outlier costs precision only within itself.  The scale of an output entry
+// is rank one (matrix row a' times input row r), so accumulation stays exact.
 //
 // Layout: input planes P[t][p][r][k], rows r = 0 .. n*n-1 of kp = roundup(n, 8)
 // BF16 values (one 1-D line along the contracted axis per row).  Output FP32
@@ -28,7 +31,7 @@
 // TMEM allocation, all four warps run the epilogue: TMEM -> registers ->
 // shared tile -> coalesced FP32 stores, with the ETD update (ac_updateU_new /
 // ch_updateU_new, calc.c:489-535) or the phi2 scaling (prepare_U2_new,
-// calc.c:553-567) fused, and the tile's max |out| folded into out_max.  Every
+// calc.c:553-567) fused.  Every
 // mbarrier wait is bounded: on timeout the CTA records an error, drains its
 // copies (bounded), frees TMEM and returns.
 #include <cuda.h>
@@ -143,7 +146,6 @@ __global__ void __launch_bounds__(128, 1)
   __shared__ __align__(8) uint64_t acc_bar;
   __shared__ uint32_t tmem_slot;
   __shared__ int failed;
-  __shared__ float warp_max[4];
 
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -259,19 +261,18 @@ __global__ void __launch_bounds__(128, 1)
   }
   fence_before();
   __syncthreads();
-  float tmax = 0.0f;
   if (!failed) {
     const int col = threadIdx.x;
     const long long r = (long long)r_tile * BN + col;
     const int kind = (t % g.F) >= g.nac ? 1 : 0;
-    const float sin_t = g.in_scale[t];
     if (r < rows) {
+      const float sin_r = g.in_scale[(long long)t * rows + r];
       const long long tb = (long long)t * g.n * rows;
 #pragma unroll 1
       for (int rr = 0; rr < BM; rr++) {
         const int a = a_tile * BM + rr;
         if (a >= g.n) break;
-        float v = tile[rr * TS + col] * (sin_t * g.row_scale[a]);
+        float v = tile[rr * TS + col] * (sin_r * g.row_scale[a]);
         const long long o = (long long)a * rows + r;  // = eigen-mode [k][j][i] of a z-contraction
         if (g.epi == 1) {
           const float uh = g.aux[tb + o];
@@ -283,23 +284,11 @@ __global__ void __launch_bounds__(128, 1)
         }
         if (g.outmode == 1) g.out[tb + o] = v;
         else g.out[tb + o] += v;
-        tmax = fmaxf(tmax, fabsf(v));
       }
     }
   }
-  if (g.out_max) {
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) tmax = fmaxf(tmax, __shfl_xor_sync(0xffffffffu, tmax, off));
-    if (lane == 0) warp_max[warp] = tmax;
-  }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    if (g.out_max && !failed) {
-      float m = fmaxf(fmaxf(warp_max[0], warp_max[1]), fmaxf(warp_max[2], warp_max[3]));
-      atomicMax(g.out_max + t, __float_as_uint(m));
-    }
-    if (failed) atomicExch(g.err, 1);
-  }
+  if (threadIdx.x == 0 && failed) atomicExch(g.err, 1);
   if (warp == 2) {
     fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
@@ -314,46 +303,35 @@ __device__ __forceinline__ float pow2_scale(float m) {
   return ldexpf(1.0f, e);
 }
 
-__global__ void tensor_max_kernel(const float *__restrict__ x, const float *__restrict__ sub,
-                                  unsigned int *__restrict__ max_bits, long long n3, int count) {
-  const long long total = n3 * count;
-  float m = 0.0f;
-  int t_cur = -1;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-    int t = (int)(i / n3);
-    if (t != t_cur) {
-      if (t_cur >= 0 && m > 0.0f) atomicMax(max_bits + t_cur, __float_as_uint(m));
-      t_cur = t;
-      m = 0.0f;
-    }
-    float v = sub ? x[i] - sub[i] : x[i];
-    m = fmaxf(m, fabsf(v));
-  }
-  if (t_cur >= 0 && m > 0.0f) atomicMax(max_bits + t_cur, __float_as_uint(m));
-}
-
-// FP32 rows of n -> slices.  Each slice is exact: x/S and the residuals are
-// scaled by powers of two and reduced by their nearest integer.
-__global__ void slice_fields_kernel(const float *__restrict__ x, const float *__restrict__ sub,
-                                    const unsigned int *__restrict__ max_bits, float *__restrict__ scale,
+// FP32 rows of n (x - sub) -> slices, one warp per row: the row's max gives its
+// power-of-two scale S; each slice is exact (the residual is scaled by 64 and
+// reduced by its nearest integer).
+__global__ void slice_fields_kernel(const float *__restrict__ x, const float *__restrict__ sub, float *__restrict__ scale,
                                     __nv_bfloat16 *__restrict__ out, int n, int kp, int count) {
-  const long long n3 = (long long)n * n * n, rows = (long long)n * n;
-  const long long total = n3 * count;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total; i += (long long)gridDim.x * blockDim.x) {
-    int t = (int)(i / n3);
-    long long l = i - (long long)t * n3;
-    long long row = l / n;
-    int k = (int)(l % n);
-    const float S = pow2_scale(__uint_as_float(max_bits[t]));
-    if (l == 0) scale[t] = S;
-    float r = (sub ? x[i] - sub[i] : x[i]) * (1.0f / S);
-    const long long o = ((long long)t * TC_PLANES * rows + row) * kp + k;
+  const long long rows = (long long)n * n, total_rows = rows * count;
+  const int lane = threadIdx.x & 31;
+  const long long warp0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long wr = warp0; wr < total_rows; wr += nwarps) {
+    const int t = (int)(wr / rows);
+    const long long row = wr - (long long)t * rows;
+    const long long in0 = wr * n;  // rows are contiguous lines of n
+    float m = 0.0f;
+    for (int k = lane; k < n; k += 32) m = fmaxf(m, fabsf(sub ? x[in0 + k] - sub[in0 + k] : x[in0 + k]));
 #pragma unroll
-    for (int p = 0; p < TC_PLANES; p++) {
-      float y = r * 64.0f;
-      float d = rintf(y);
-      r = y - d;
-      out[o + (long long)p * rows * kp] = __float2bfloat16_rn(d);
+    for (int off = 16; off > 0; off >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
+    const float S = pow2_scale(m), inv = 1.0f / S;
+    if (lane == 0) scale[wr] = S;
+    const long long o0 = ((long long)t * TC_PLANES * rows + row) * kp;
+    for (int k = lane; k < n; k += 32) {
+      float r = (sub ? x[in0 + k] - sub[in0 + k] : x[in0 + k]) * inv;
+#pragma unroll
+      for (int p = 0; p < TC_PLANES; p++) {
+        float y = r * 64.0f;
+        float d = rintf(y);
+        r = y - d;
+        out[o0 + (long long)p * rows * kp + k] = __float2bfloat16_rn(d);
+      }
     }
   }
 }
@@ -462,28 +440,18 @@ static cudaError_t make_map(CUtensorMap *map, const void *ptr, int kp, long long
 
 int tc_kp(int n) { return (n + 7) / 8 * 8; }
 
-static int grid_cap(long long total) {
-  long long b = (total + 255) / 256;
-  return (int)(b > 152 * 32 ? 152 * 32 : (b < 1 ? 1 : b));
-}
-
 cudaError_t tc_slice_matrix(const double *m, __nv_bfloat16 *planes, float *row_scale, int n, cudaStream_t s) {
   tc::slice_matrix_kernel<<<n < 1024 ? n : 1024, 128, 0, s>>>(m, planes, row_scale, n, tc_kp(n));
   launch_counter()++;
   return cudaGetLastError();
 }
 
-cudaError_t tc_tensor_max(const float *x, const float *sub, unsigned int *max_bits, int n, int count, cudaStream_t s) {
-  long long n3 = (long long)n * n * n;
-  tc::tensor_max_kernel<<<grid_cap(n3 * count), 256, 0, s>>>(x, sub, max_bits, n3, count);
-  launch_counter()++;
-  return cudaGetLastError();
-}
-
-cudaError_t tc_slice_fields(const float *x, const float *sub, const unsigned int *max_bits, float *scale,
-                            __nv_bfloat16 *planes, int n, int count, cudaStream_t s) {
-  long long total = (long long)n * n * n * count;
-  tc::slice_fields_kernel<<<grid_cap(total), 256, 0, s>>>(x, sub, max_bits, scale, planes, n, tc_kp(n), count);
+cudaError_t tc_slice_fields(const float *x, const float *sub, float *scale, __nv_bfloat16 *planes, int n, int count,
+                            cudaStream_t s) {
+  long long warps = (long long)n * n * count;
+  long long blocks = (warps * 32 + 255) / 256;
+  int g = (int)(blocks > 152 * 32 ? 152 * 32 : blocks);
+  tc::slice_fields_kernel<<<g, 256, 0, s>>>(x, sub, scale, planes, n, tc_kp(n), count);
   launch_counter()++;
   return cudaGetLastError();
 }

@@ -50,11 +50,10 @@ struct sclet_ctx {
   double *V[3] = {nullptr, nullptr, nullptr}, *Vi[3] = {nullptr, nullptr, nullptr};
   double *phi1[2] = {nullptr, nullptr}, *phi2[2] = {nullptr, nullptr};
   // MIXED form: fstate2 = [u (F) | rhs1 (F)] in FP32; FP32 work tensors W1, W2
-  // (2F blocks each); slice planes P of up to 2F tensors; per-tensor max
-  // (float bits) and scale buffers; sliced matrices with row scales
+  // (2F blocks each); slice planes P of up to 2F tensors with their row scales
+  // scaleP; sliced matrices with row scales
   float *fstate2 = nullptr, *frhs2 = nullptr, *ffelas = nullptr, *fscratch = nullptr, *fshell = nullptr;
   float *W1 = nullptr, *W2 = nullptr, *scaleP = nullptr, *rsV = nullptr, *rsVi = nullptr;
-  unsigned int *maxA = nullptr, *maxB = nullptr;
   __nv_bfloat16 *P = nullptr, *matV = nullptr, *matVi = nullptr;
   float4 *coef[2] = {nullptr, nullptr};   // ETD1 coefficient pairs per field kind
   float2 *coef2[2] = {nullptr, nullptr};  // ETD2 phi2 pairs per field kind
@@ -263,7 +262,7 @@ void sclet_destroy(sclet_ctx *ctx) {
   void *bufs[] = {ctx->state2, ctx->rhs2, ctx->A, ctx->B, ctx->felas, ctx->scratch, ctx->shell, ctx->elam,
                   ctx->partials, ctx->diag, ctx->phi1[0], ctx->phi1[1], ctx->phi2[0], ctx->phi2[1], ctx->dev_err,
                   ctx->fstate2, ctx->frhs2, ctx->ffelas, ctx->fscratch, ctx->fshell, ctx->W1, ctx->W2, ctx->P,
-                  ctx->scaleP, ctx->rsV, ctx->rsVi, ctx->maxA, ctx->maxB, ctx->matV, ctx->matVi, ctx->stage64,
+                  ctx->scaleP, ctx->rsV, ctx->rsVi, ctx->matV, ctx->matVi, ctx->stage64,
                   ctx->coef[0], ctx->coef[1], ctx->coef2[0], ctx->coef2[1]};
   for (void *b : bufs) cudaFree(b);
   for (int a = 0; a < 3; a++) {
@@ -404,9 +403,7 @@ int sclet_create(const sclet_params *p, int precision, int device, sclet_ctx **o
     // pad columns of the slice planes are never written and must stay zero
     CC(cudaMalloc(&ctx->P, pbytes));
     CC(cudaMemsetAsync(ctx->P, 0, pbytes, s));
-    CC(cudaMalloc(&ctx->scaleP, sizeof(float) * 2 * F));
-    CC(cudaMalloc(&ctx->maxA, sizeof(unsigned int) * 2 * F));
-    CC(cudaMalloc(&ctx->maxB, sizeof(unsigned int) * 2 * F));
+    CC(cudaMalloc(&ctx->scaleP, sizeof(float) * 2 * F * n * n));
     CC(cudaMalloc(&ctx->matV, sizeof(__nv_bfloat16) * TC_PLANES * n * tc_kp(n)));
     CC(cudaMalloc(&ctx->matVi, sizeof(__nv_bfloat16) * TC_PLANES * n * tc_kp(n)));
     CC(cudaMalloc(&ctx->rsV, sizeof(float) * n));
@@ -539,10 +536,9 @@ int sclet_calc_rhs(sclet_ctx *ctx, int slot) {
 }
 
 // One fixed-point tensor-core product of `count` sliced tensors (planes at
-// `planes`, scales at `scale`) into FP32 `out`, recording max |out| when
-// out_max is given.
+// `planes`, row scales at `scale`) into FP32 `out`.
 static cudaError_t tc_prod(sclet_ctx *ctx, bool inverse, const __nv_bfloat16 *planes, const float *scale, int count,
-                           float *out, unsigned int *out_max, int epi, const float *aux, int outmode) {
+                           float *out, int epi, const float *aux, int outmode) {
   TcArgs g;
   memset(&g, 0, sizeof g);
   g.n = ctx->n;
@@ -551,7 +547,6 @@ static cudaError_t tc_prod(sclet_ctx *ctx, bool inverse, const __nv_bfloat16 *pl
   g.outmode = outmode;
   g.aux = aux;
   g.out = out;
-  g.out_max = out_max;
   g.in_scale = scale;
   g.row_scale = inverse ? ctx->rsV : ctx->rsVi;
   for (int k = 0; k < 2; k++) {
@@ -561,63 +556,51 @@ static cudaError_t tc_prod(sclet_ctx *ctx, bool inverse, const __nv_bfloat16 *pl
   g.nac = ctx->nac;
   g.F = ctx->F;
   g.err = ctx->dev_err;
-  if (out_max) {
-    cudaError_t e = cudaMemsetAsync(out_max, 0, sizeof(unsigned int) * count, ctx->stream);
-    if (e != cudaSuccess) return e;
-  }
   return launch_modeprod_tc(inverse ? ctx->matV : ctx->matVi, planes, count, g, ctx->stream);
 }
 
-// x (count FP32 blocks, minus sub) -> slice planes P with scales from max_bits
-static cudaError_t tc_slice(sclet_ctx *ctx, const float *x, const float *sub, const unsigned int *max_bits, int count,
-                            __nv_bfloat16 *planes, float *scale) {
-  return tc_slice_fields(x, sub, max_bits, scale, planes, ctx->n, count, ctx->stream);
+// x (count FP32 blocks, minus sub) -> slice planes P and row scales
+static cudaError_t tc_slice(sclet_ctx *ctx, const float *x, const float *sub, int count) {
+  return tc_slice_fields(x, sub, ctx->scaleP, ctx->P, ctx->n, count, ctx->stream);
 }
 
 // Mixed form of the transforms (ScLETD.c:105-142): V^-1 along x and y for u
 // and N1 together, along z for u, then for N1 with the ETD update fused; V
-// along x, y, z back to the FP32 state.  Each product records the max of its
-// output, from which the next slicing takes its scale.
+// along x, y, z back to the FP32 state.
 static int etd_update_mixed(sclet_ctx *ctx) {
   const int F = ctx->F;
-  const long long ps = plane_stride(ctx);
-  cudaStream_t s = ctx->stream;
-  CK(cudaMemsetAsync(ctx->maxA, 0, sizeof(unsigned int) * 2 * F, s));
-  CK(tc_tensor_max(ctx->fstate2, nullptr, ctx->maxA, ctx->n, 2 * F, s));
-  CK(tc_slice(ctx, ctx->fstate2, nullptr, ctx->maxA, 2 * F, ctx->P, ctx->scaleP));
-  CK(tc_prod(ctx, false, ctx->P, ctx->scaleP, 2 * F, ctx->W1, ctx->maxB, 0, nullptr, 1));
-  CK(tc_slice(ctx, ctx->W1, nullptr, ctx->maxB, 2 * F, ctx->P, ctx->scaleP));
-  CK(tc_prod(ctx, false, ctx->P, ctx->scaleP, 2 * F, ctx->W2, ctx->maxA, 0, nullptr, 1));
-  CK(tc_slice(ctx, ctx->W2, nullptr, ctx->maxA, 2 * F, ctx->P, ctx->scaleP));
-  CK(tc_prod(ctx, false, ctx->P, ctx->scaleP, F, ctx->W1, nullptr, 0, nullptr, 1));
-  CK(tc_prod(ctx, false, ctx->P + F * ps, ctx->scaleP + F, F, ctx->W1, ctx->maxB, 1, ctx->W1, 1));
-  CK(tc_slice(ctx, ctx->W1, nullptr, ctx->maxB, F, ctx->P, ctx->scaleP));
-  CK(tc_prod(ctx, true, ctx->P, ctx->scaleP, F, ctx->W2, ctx->maxA, 0, nullptr, 1));
-  CK(tc_slice(ctx, ctx->W2, nullptr, ctx->maxA, F, ctx->P, ctx->scaleP));
-  CK(tc_prod(ctx, true, ctx->P, ctx->scaleP, F, ctx->W1, ctx->maxB, 0, nullptr, 1));
-  CK(tc_slice(ctx, ctx->W1, nullptr, ctx->maxB, F, ctx->P, ctx->scaleP));
-  CK(tc_prod(ctx, true, ctx->P, ctx->scaleP, F, fu_of(ctx), nullptr, 0, nullptr, 1));
+  const long long ps = plane_stride(ctx), rows = (long long)ctx->n * ctx->n;
+  CK(tc_slice(ctx, ctx->fstate2, nullptr, 2 * F));
+  CK(tc_prod(ctx, false, ctx->P, ctx->scaleP, 2 * F, ctx->W1, 0, nullptr, 1));
+  CK(tc_slice(ctx, ctx->W1, nullptr, 2 * F));
+  CK(tc_prod(ctx, false, ctx->P, ctx->scaleP, 2 * F, ctx->W2, 0, nullptr, 1));
+  CK(tc_slice(ctx, ctx->W2, nullptr, 2 * F));
+  CK(tc_prod(ctx, false, ctx->P, ctx->scaleP, F, ctx->W1, 0, nullptr, 1));
+  CK(tc_prod(ctx, false, ctx->P + F * ps, ctx->scaleP + F * rows, F, ctx->W1, 1, ctx->W1, 1));
+  CK(tc_slice(ctx, ctx->W1, nullptr, F));
+  CK(tc_prod(ctx, true, ctx->P, ctx->scaleP, F, ctx->W2, 0, nullptr, 1));
+  CK(tc_slice(ctx, ctx->W2, nullptr, F));
+  CK(tc_prod(ctx, true, ctx->P, ctx->scaleP, F, ctx->W1, 0, nullptr, 1));
+  CK(tc_slice(ctx, ctx->W1, nullptr, F));
+  CK(tc_prod(ctx, true, ctx->P, ctx->scaleP, F, fu_of(ctx), 0, nullptr, 1));
   return SCLET_OK;
 }
 
 // ETD2 corrector (ScLETD.c:159-188): u += V phi2 V^-1 (N2 - N1).
 static int etd2_correct_mixed(sclet_ctx *ctx) {
   const int F = ctx->F;
-  cudaStream_t s = ctx->stream;
-  CK(cudaMemsetAsync(ctx->maxA, 0, sizeof(unsigned int) * F, s));
-  CK(tc_tensor_max(ctx->frhs2, frhs1_of(ctx), ctx->maxA, ctx->n, F, s));
-  CK(tc_slice(ctx, ctx->frhs2, frhs1_of(ctx), ctx->maxA, F, ctx->P, ctx->scaleP));
-  CK(tc_prod(ctx, false, ctx->P, ctx->scaleP, F, ctx->W1, ctx->maxB, 0, nullptr, 1));
-  CK(tc_slice(ctx, ctx->W1, nullptr, ctx->maxB, F, ctx->P, ctx->scaleP));
-  CK(tc_prod(ctx, false, ctx->P, ctx->scaleP, F, ctx->W2, ctx->maxA, 0, nullptr, 1));
-  CK(tc_slice(ctx, ctx->W2, nullptr, ctx->maxA, F, ctx->P, ctx->scaleP));
-  CK(tc_prod(ctx, false, ctx->P, ctx->scaleP, F, ctx->W1, ctx->maxB, 2, nullptr, 1));
-  CK(tc_slice(ctx, ctx->W1, nullptr, ctx->maxB, F, ctx->P, ctx->scaleP));
-  CK(tc_prod(ctx, true, ctx->P, ctx->scaleP, F, ctx->W2, ctx->maxA, 0, nullptr, 1));
-  CK(tc_slice(ctx, ctx->W2, nullptr, ctx->maxA, F, ctx->P, ctx->scaleP));
-  CK(tc_prod(ctx, true, ctx->P, ctx->scaleP, F, ctx->W1, ctx->maxB, 0, nullptr, 1));
-  CK(tc_slice(ctx, ctx->W1, nullptr, ctx->maxB, F, ctx->P, ctx->scaleP));
-  CK(tc_prod(ctx, true, ctx->P, ctx->scaleP, F, fu_of(ctx), nullptr, 0, nullptr, 2));
+  CK(tc_slice(ctx, ctx->frhs2, frhs1_of(ctx), F));
+  CK(tc_prod(ctx, false, ctx->P, ctx->scaleP, F, ctx->W1, 0, nullptr, 1));
+  CK(tc_slice(ctx, ctx->W1, nullptr, F));
+  CK(tc_prod(ctx, false, ctx->P, ctx->scaleP, F, ctx->W2, 0, nullptr, 1));
+  CK(tc_slice(ctx, ctx->W2, nullptr, F));
+  CK(tc_prod(ctx, false, ctx->P, ctx->scaleP, F, ctx->W1, 2, nullptr, 1));
+  CK(tc_slice(ctx, ctx->W1, nullptr, F));
+  CK(tc_prod(ctx, true, ctx->P, ctx->scaleP, F, ctx->W2, 0, nullptr, 1));
+  CK(tc_slice(ctx, ctx->W2, nullptr, F));
+  CK(tc_prod(ctx, true, ctx->P, ctx->scaleP, F, ctx->W1, 0, nullptr, 1));
+  CK(tc_slice(ctx, ctx->W1, nullptr, F));
+  CK(tc_prod(ctx, true, ctx->P, ctx->scaleP, F, fu_of(ctx), 0, nullptr, 2));
   return SCLET_OK;
 }
 
@@ -729,10 +712,8 @@ int sclet_mode_product(sclet_ctx *ctx, int inverse, const double *in, double *ou
     f64_to_f32<<<grid_of(n3), 256, 0, ctx->stream>>>(ctx->stage64, tmp, n3);
     launch_counter()++;
     CK(cudaGetLastError());
-    CK(cudaMemsetAsync(ctx->maxA, 0, sizeof(unsigned int), ctx->stream));
-    CK(tc_tensor_max(tmp, nullptr, ctx->maxA, ctx->n, 1, ctx->stream));
-    CK(tc_slice(ctx, tmp, nullptr, ctx->maxA, 1, ctx->P, ctx->scaleP));
-    CK(tc_prod(ctx, inverse != 0, ctx->P, ctx->scaleP, 1, tmp + n3, nullptr, 0, nullptr, 1));
+    CK(tc_slice(ctx, tmp, nullptr, 1));
+    CK(tc_prod(ctx, inverse != 0, ctx->P, ctx->scaleP, 1, tmp + n3, 0, nullptr, 1));
     f32_to_f64<<<grid_of(n3), 256, 0, ctx->stream>>>(tmp + n3, ctx->stage64, n3);
     launch_counter()++;
     CK(cudaGetLastError());

@@ -14,8 +14,7 @@ struct TcArgs {
   int outmode;              // 1 FP32 store, 2 FP32 accumulate
   const float *aux;         // [count][n^3] FP32 uhat, same layout as out
   float *out;               // [count][n^3] FP32, rotated layout
-  unsigned int *out_max;    // [count] max |out| as float bits (atomicMax), or null
-  const float *in_scale;    // [count] power-of-two scale of each input tensor's slices
+  const float *in_scale;    // [count][n*n] power-of-two scale of each input row's slices
   const float *row_scale;   // [n] power-of-two scale of each matrix row's slices
   // per field kind (0 AC, 1 CH), per eigen-mode [k][j][i]: ETD1
   // (e = 1 - phi1 H, phi1) and ETD2 (phi2) coefficients computed in FP64
@@ -30,13 +29,10 @@ int tc_kp(int n);
 // Row-major FP64 n x n matrix -> TC_PLANES slice planes [p][n][kp] (zero padded
 // columns) and the power-of-two scale of each row.
 cudaError_t tc_slice_matrix(const double *m, __nv_bfloat16 *planes, float *row_scale, int n, cudaStream_t s);
-// max |x - sub| of each FP32 block [count][n^3] into max_bits[count] (atomicMax on
-// the float bits; zero it first).  `sub` may be null.
-cudaError_t tc_tensor_max(const float *x, const float *sub, unsigned int *max_bits, int n, int count, cudaStream_t s);
-// FP32 blocks (x - sub), rows of n -> slice planes [count][p][n*n][kp], with
-// scale[t] = 2^ceil(log2 max_t) (from max_bits) recorded for the product.
-cudaError_t tc_slice_fields(const float *x, const float *sub, const unsigned int *max_bits, float *scale,
-                            __nv_bfloat16 *planes, int n, int count, cudaStream_t s);
+// FP32 blocks (x - sub; sub may be null), rows of n -> slice planes
+// [count][p][n*n][kp] with the power-of-two scale of each row in scale[count][n*n].
+cudaError_t tc_slice_fields(const float *x, const float *sub, float *scale, __nv_bfloat16 *planes, int n, int count,
+                            cudaStream_t s);
 // ETD coefficient tables of one field kind (see TcArgs::coef)
 cudaError_t tc_make_coefs(float4 *coef, float2 *coef2, int n, int kind, const double *dx, const double *dy,
                           const double *dz, const double *kk, double epn2, double dt, double L, double K,
