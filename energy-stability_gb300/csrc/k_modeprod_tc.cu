@@ -6,12 +6,16 @@
 // slices of 6 bits, x = S * sum_p d_p 64^-(p+1), d_0 in [-64, 64], d_p in
 // [-32, 32] (round to nearest at every level; 24 bits below S).  The slices
 // are small integers held exactly in BF16.  The product keeps every cross term
-// of weight w = p + q <= 3 (ten BF16 MMAs per k-step, the split-precision
-// scheme of Markidis et al. 2018 / Ootomo & Yokota 2022 carried to fixed
-// point, as in the Ozaki scheme), one FP32 accumulator in tensor memory per
-// weight class.  Every partial sum is an integer below 2^24 (|sum| <= 6144 per
-// k times K <= 1040), so the tensor-core accumulation is exact and unbiased;
-// the epilogue combines the four classes with round-to-nearest FP32 adds.
+// of weight w = p + q <= 3 (the split-precision scheme of Markidis et al.
+// 2018 / Ootomo & Yokota 2022 carried to fixed point, as in the Ozaki scheme),
+// one FP32 accumulator in tensor memory per weight class.  In classes 0 and 1
+// every partial sum is an integer below 2^24 (|sum| <= 4096 per k times
+// K <= 1040), so their accumulation is exact and unbiased; classes 2 and 3 sit
+// 2^-12 and 2^-18 below the result, where accumulator rounding is harmless.
+// The matrix carries a fifth slice (its representation error would otherwise
+// act on the leading data slice the same way every step); it is stored
+// pre-scaled by 1/64 and its term M4 x0 joins class 3: eleven BF16 MMAs per
+// k-step.  The epilogue combines the four classes with round-to-nearest adds.
 //
 // Scales: powers of two per matrix row (static) and per input row (one 1-D
 // line along the contracted axis, 2^ceil(log2 max|x|) over the line, found by
@@ -47,10 +51,10 @@ namespace sclet {
 
 namespace tc {
 
-constexpr int BM = 128, BN = 128, BK = 32, STAGES = 3, NP = TC_PLANES;
+constexpr int BM = 128, BN = 128, BK = 32, STAGES = 3, NP = TC_PLANES, NPM = TC_PLANES_M;
 constexpr int PLANE_A = BM * BK * 2;  // 8 KB
 constexpr int PLANE_B = BN * BK * 2;  // 8 KB
-constexpr int STAGE_BYTES = NP * PLANE_A + NP * PLANE_B;
+constexpr int STAGE_BYTES = NPM * PLANE_A + NP * PLANE_B;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;
 constexpr int NACC = 4;  // weight classes w = 0..3
 constexpr int TMEM_COLS = NACC * BN;
@@ -175,7 +179,7 @@ __global__ void __launch_bounds__(128, 1)
   const int nkb = g.kblocks;
 
   if (warp == 0 && lane == 0) {
-    // producer: four A slices and four B slices per stage
+    // producer: five A slices and four B slices per stage
     int issued = 0;
     for (int kb = 0; kb < nkb; kb++) {
       const int s = kb % STAGES;
@@ -186,9 +190,9 @@ __global__ void __launch_bounds__(128, 1)
       if (*(volatile int *)&failed) break;
       uint8_t *st = base + s * STAGE_BYTES;
       mbar_expect_tx(&full_bar[s], STAGE_BYTES);
-      for (int p = 0; p < NP; p++) tma_load_3d(st + p * PLANE_A, &tmA, kb * BK, a_tile * BM, p, &full_bar[s]);
+      for (int p = 0; p < NPM; p++) tma_load_3d(st + p * PLANE_A, &tmA, kb * BK, a_tile * BM, p, &full_bar[s]);
       for (int p = 0; p < NP; p++)
-        tma_load_3d(st + NP * PLANE_A + p * PLANE_B, &tmB, kb * BK, r_tile * BN, t * NP + p, &full_bar[s]);
+        tma_load_3d(st + NPM * PLANE_A + p * PLANE_B, &tmB, kb * BK, r_tile * BN, t * NP + p, &full_bar[s]);
       issued = kb + 1;
     }
     if (*(volatile int *)&failed) {
@@ -197,12 +201,13 @@ __global__ void __launch_bounds__(128, 1)
         mbar_wait(&full_bar[kb % STAGES], (kb / STAGES) & 1);
     }
   } else if (warp == 1 && lane == 0) {
-    // MMA issuer: 2 k-steps of 16 per stage, ten terms each; (matrix slice,
-    // input slice) grouped by weight class, small classes first; the first
-    // term of each class at the first k-step starts its accumulator
+    // MMA issuer: 2 k-steps of 16 per stage, eleven terms each; (matrix
+    // slice, input slice, class) grouped by class, small classes first; the
+    // first term of each class at the first k-step starts its accumulator
     const uint32_t idesc = idesc_bf16(BM, BN);
-    const int pairA[10] = {0, 1, 2, 3, 0, 1, 2, 0, 1, 0};
-    const int pairB[10] = {3, 2, 1, 0, 2, 1, 0, 1, 0, 0};
+    const int pairA[11] = {4, 0, 1, 2, 3, 0, 1, 2, 0, 1, 0};
+    const int pairB[11] = {0, 3, 2, 1, 0, 2, 1, 0, 1, 0, 0};
+    const int cls[11] = {3, 3, 3, 3, 3, 2, 2, 2, 1, 1, 0};
     for (int kb = 0; kb < nkb; kb++) {
       const int s = kb % STAGES;
       if (!mbar_wait(&full_bar[s], (kb / STAGES) & 1)) {
@@ -211,15 +216,15 @@ __global__ void __launch_bounds__(128, 1)
       }
       fence_after();
       const uint32_t sa = smem_u32(base + s * STAGE_BYTES);
-      const uint32_t sb = sa + NP * PLANE_A;
+      const uint32_t sb = sa + NPM * PLANE_A;
 #pragma unroll
       for (int ks = 0; ks < BK / 16; ks++) {
         const uint32_t koff = ks * 32;
         const bool first = (kb == 0 && ks == 0);
 #pragma unroll
-        for (int q = 0; q < 10; q++) {
-          const int pa = pairA[q], pb = pairB[q], w = pa + pb;
-          const bool start = first && (q == 0 || q == 4 || q == 7 || q == 9);
+        for (int q = 0; q < 11; q++) {
+          const int pa = pairA[q], pb = pairB[q], w = cls[q];
+          const bool start = first && (q == 0 || q == 5 || q == 8 || q == 10);
           uint64_t da = smem_desc(sa + pa * PLANE_A + koff);
           uint64_t db = smem_desc(sb + pb * PLANE_B + koff);
           mma_bf16(tmem + (uint32_t)(w * BN), da, db, idesc, start ? 0u : 1u);
@@ -359,11 +364,13 @@ __global__ void slice_matrix_kernel(const double *__restrict__ m, __nv_bfloat16 
     if (threadIdx.x == 0) row_scale[r] = (float)S;
     for (int c = threadIdx.x; c < kp; c += blockDim.x) {
       double v = c < n ? m[(long long)r * n + c] / S : 0.0;
-      for (int p = 0; p < TC_PLANES; p++) {
+      for (int p = 0; p < TC_PLANES_M; p++) {
         double y = v * 64.0;
         double d = rint(y);
         v = y - d;
-        out[((long long)p * n + r) * kp + c] = __float2bfloat16_rn((float)d);
+        // the fifth slice enters class 3, one factor 64 below its own weight
+        float q = p < TC_PLANES ? (float)d : (float)d * (1.0f / 64.0f);
+        out[((long long)p * n + r) * kp + c] = __float2bfloat16_rn(q);
       }
     }
   }
@@ -480,7 +487,7 @@ cudaError_t launch_modeprod_tc(const __nv_bfloat16 *mat, const __nv_bfloat16 *pl
   if ((long long)tc::BK * ((n + tc::BK - 1) / tc::BK) > 1040) return cudaErrorInvalidValue;  // exactness bound
   CUtensorMap ma, mb;
   cudaError_t e;
-  if ((e = make_map(&ma, mat, kp, n, TC_PLANES, tc::BM)) != cudaSuccess) return e;
+  if ((e = make_map(&ma, mat, kp, n, TC_PLANES_M, tc::BM)) != cudaSuccess) return e;
   if ((e = make_map(&mb, planes, kp, (long long)n * n, TC_PLANES * count, tc::BN)) != cudaSuccess) return e;
   TcArgs g = args;
   g.kp = kp;

@@ -404,8 +404,8 @@ int sclet_create(const sclet_params *p, int precision, int device, sclet_ctx **o
     CC(cudaMalloc(&ctx->P, pbytes));
     CC(cudaMemsetAsync(ctx->P, 0, pbytes, s));
     CC(cudaMalloc(&ctx->scaleP, sizeof(float) * 2 * F * n * n));
-    CC(cudaMalloc(&ctx->matV, sizeof(__nv_bfloat16) * TC_PLANES * n * tc_kp(n)));
-    CC(cudaMalloc(&ctx->matVi, sizeof(__nv_bfloat16) * TC_PLANES * n * tc_kp(n)));
+    CC(cudaMalloc(&ctx->matV, sizeof(__nv_bfloat16) * TC_PLANES_M * n * tc_kp(n)));
+    CC(cudaMalloc(&ctx->matVi, sizeof(__nv_bfloat16) * TC_PLANES_M * n * tc_kp(n)));
     CC(cudaMalloc(&ctx->rsV, sizeof(float) * n));
     CC(cudaMalloc(&ctx->rsVi, sizeof(float) * n));
     CC(cudaMalloc(&ctx->stage64, sizeof(double) * ctx->n3));

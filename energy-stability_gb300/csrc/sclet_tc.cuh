@@ -6,7 +6,9 @@
 
 namespace sclet {
 
-constexpr int TC_PLANES = 4;  // fixed-point slices per operand (6 bits each)
+constexpr int TC_PLANES = 4;    // fixed-point slices per data operand (6 bits each)
+constexpr int TC_PLANES_M = 5;  // slices per matrix: four 6-bit slices and a fifth
+                                // stored pre-scaled by 1/64 (see k_modeprod_tc.cu)
 
 struct TcArgs {
   int n, kp, kblocks, count;
@@ -26,7 +28,7 @@ struct TcArgs {
 };
 
 int tc_kp(int n);
-// Row-major FP64 n x n matrix -> TC_PLANES slice planes [p][n][kp] (zero padded
+// Row-major FP64 n x n matrix -> TC_PLANES_M slice planes [p][n][kp] (zero padded
 // columns) and the power-of-two scale of each row.
 cudaError_t tc_slice_matrix(const double *m, __nv_bfloat16 *planes, float *row_scale, int n, cudaStream_t s);
 // FP32 blocks (x - sub; sub may be null), rows of n -> slice planes
