@@ -117,23 +117,30 @@ class ClockSampler:
 
 
 def dist_setup():
+    """Replica ranks from the torchrun environment: NCCL with one GPU per rank,
+    gloo where no GPU is visible (host-side runs of the same code)."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl")
+        else:
+            dist.init_process_group("gloo")
     return world, rank, local
 
 
 def dist_max(x: float, world: int) -> float:
+    """Maximum over ranks (the slowest replica's time)."""
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -144,9 +151,12 @@ def dist_barrier(world: int):
         dist.barrier()
 
 
-def cpu_oracle_rate(case: cases.Case, steps: int, warmup: int):
-    """Times the C oracle (all host threads) on the case; returns
-    (cell-updates/s, cores, seconds)."""
+def cpu_oracle_rate(case: cases.Case, steps: int, warmup: int, budget_s: float = 120.0):
+    """Times the C oracle (all host threads) on the case: `warmup` untimed
+    steps (at most one), then up to `steps` timed steps with the diagnostics
+    of each, stopping once `budget_s` seconds are spent (the sample is then
+    shorter than `steps`).  Returns (cell-updates/s, cores, seconds, steps
+    timed)."""
     import oracle_py
     if not os.path.exists(oracle_py.LIB_PATH):
         oracle_py.build()
@@ -154,27 +164,31 @@ def cpu_oracle_rate(case: cases.Case, steps: int, warmup: int):
         cases.write_case(case, td, fields=False)
         p = oracle_py.load_case_params(td, case.suffix, block_fields(case))
         o = oracle_py.Oracle(p)
-        o.step(warmup)
-        t0 = time.perf_counter()
-        o.step(steps)
-        o.check_soln()
-        dt = time.perf_counter() - t0
-    return case.big_n ** 3 * steps / dt, o.threads(), dt
+        o.step(min(warmup, 1))
+        done, dt = 0, 0.0
+        while done < max(steps, 1) and (done == 0 or dt < budget_s):
+            t0 = time.perf_counter()
+            o.step(1)
+            o.check_soln()
+            dt += time.perf_counter() - t0
+            done += 1
+    return case.big_n ** 3 * done / dt, o.threads(), dt, done
 
 
 def run_reference(args, world, rank):
     if rank != 0:
         return
     case = workload(args.size, seed=1000)
-    rate, cores, secs = cpu_oracle_rate(case, args.steps, args.warmup)
+    rate, cores, secs, done = cpu_oracle_rate(case, args.steps, args.warmup)
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * secs / args.steps,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * secs / done,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": workload_name(args.size), "cells_per_step": args.size ** 3},
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{args.steps} full steps of the workload after {args.warmup} warm-up steps "
-                                   f"(C restatement of the reference's step, OpenMP on {cores} threads)"},
+                         "sample": f"{done} full steps of the workload with diagnostics, after "
+                                   f"{min(args.warmup, 1)} warm-up step (C restatement of the reference's step, "
+                                   f"OpenMP on {cores} threads, {secs:.1f} s)"},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -248,7 +262,7 @@ def run_gpu(args, world, rank, local):
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         small = workload(args.size, seed=1000)
-        rate, cores, secs = cpu_oracle_rate(small, args.cpu_steps, 0)
+        rate, cores, secs, _ = cpu_oracle_rate(small, args.cpu_steps, 0)
         cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"{args.cpu_steps} full steps of the same workload, C restatement of the reference's step "
                          f"on {cores} host threads ({secs:.1f} s)"}

@@ -3,19 +3,21 @@
 // calc.c:631-684).
 //
 // Number format: each operand is a power-of-two scale times four fixed-point
-// slices of 6 bits, x = S * sum_p d_p 64^-(p+1), d_0 in [-64, 64], d_p in
-// [-32, 32] (round to nearest at every level; 24 bits below S).  The slices
-// are small integers held exactly in BF16.  The product keeps every cross term
-// of weight w = p + q <= 3 (the split-precision scheme of Markidis et al.
-// 2018 / Ootomo & Yokota 2022 carried to fixed point, as in the Ozaki scheme),
-// one FP32 accumulator in tensor memory per weight class.  In classes 0 and 1
-// every partial sum is an integer below 2^24 (|sum| <= 4096 per k times
-// K <= 1040), so their accumulation is exact and unbiased; classes 2 and 3 sit
-// 2^-12 and 2^-18 below the result, where accumulator rounding is harmless.
-// The matrix carries a fifth slice (its representation error would otherwise
-// act on the leading data slice the same way every step); it is stored
-// pre-scaled by 1/64 and its term M4 x0 joins class 3: eleven BF16 MMAs per
-// k-step.  The epilogue combines the four classes with round-to-nearest adds.
+// slices of b bits, x = S * sum_p d_p 2^-b(p+1), d_0 in [-2^b, 2^b], d_p in
+// [-2^(b-1), 2^(b-1)] (round to nearest at every level; 4b bits below S).
+// b = 7 while the contraction length K <= 1024, else 6 (tc_slice_bits).  The
+// slices are small integers held exactly in BF16.  The product keeps every
+// cross term of weight w = p + q <= 3 (the split-precision scheme of Markidis
+// et al. 2018 / Ootomo & Yokota 2022 carried to fixed point, as in the Ozaki
+// scheme), one FP32 accumulator in tensor memory per weight class.  In classes
+// 0 and 1 every partial sum is an integer below 2^24 (|sum| <= 2^(2b) per k
+// times K <= 2^(24-2b)), so their accumulation is exact and unbiased; classes
+// 2 and 3 sit 2^-2b and 2^-3b below the result, where accumulator rounding is
+// harmless.  The matrix carries a fifth slice (its representation error would
+// otherwise act on the leading data slice the same way every step); it is
+// stored pre-scaled by 2^-b and its term M4 x0 joins class 3: eleven BF16 MMAs
+// per k-step.  The epilogue combines the four classes with round-to-nearest
+// adds.
 //
 // Scales: powers of two per matrix row (static) and per input row (one 1-D
 // line along the contracted axis, 2^ceil(log2 max|x|) over the line, found by
@@ -245,8 +247,9 @@ __global__ void __launch_bounds__(128, 1)
   __syncthreads();
   if (!failed) {
     const int row = warp * 32 + lane;
-    // class weights 64^-(w+2); exact integers combined small to large
-    const float wt[NACC] = {1.0f / 4096.0f, 1.0f / 262144.0f, 1.0f / 16777216.0f, 1.0f / 1073741824.0f};
+    // class weights 2^-b(w+2); exact integers combined small to large
+    const float wt[NACC] = {ldexpf(1.0f, -2 * g.bits), ldexpf(1.0f, -3 * g.bits), ldexpf(1.0f, -4 * g.bits),
+                            ldexpf(1.0f, -5 * g.bits)};
 #pragma unroll 1
     for (int c = 0; c < BN / 32; c++) {
       float v[32], w[32];
@@ -309,10 +312,11 @@ __device__ __forceinline__ float pow2_scale(float m) {
 }
 
 // FP32 rows of n (x - sub) -> slices, one warp per row: the row's max gives its
-// power-of-two scale S; each slice is exact (the residual is scaled by 64 and
+// power-of-two scale S; each slice is exact (the residual is scaled by 2^b and
 // reduced by its nearest integer).
 __global__ void slice_fields_kernel(const float *__restrict__ x, const float *__restrict__ sub, float *__restrict__ scale,
-                                    __nv_bfloat16 *__restrict__ out, int n, int kp, int count) {
+                                    __nv_bfloat16 *__restrict__ out, int n, int kp, int count, int bits) {
+  const float step = ldexpf(1.0f, bits);
   const long long rows = (long long)n * n, total_rows = rows * count;
   const int lane = threadIdx.x & 31;
   const long long warp0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
@@ -332,7 +336,7 @@ __global__ void slice_fields_kernel(const float *__restrict__ x, const float *__
       float r = (sub ? x[in0 + k] - sub[in0 + k] : x[in0 + k]) * inv;
 #pragma unroll
       for (int p = 0; p < TC_PLANES; p++) {
-        float y = r * 64.0f;
+        float y = r * step;
         float d = rintf(y);
         r = y - d;
         out[o0 + (long long)p * rows * kp + k] = __float2bfloat16_rn(d);
@@ -343,8 +347,9 @@ __global__ void slice_fields_kernel(const float *__restrict__ x, const float *__
 
 // FP64 matrix rows -> slices with a power-of-two scale per row.
 __global__ void slice_matrix_kernel(const double *__restrict__ m, __nv_bfloat16 *__restrict__ out,
-                                    float *__restrict__ row_scale, int n, int kp) {
+                                    float *__restrict__ row_scale, int n, int kp, int bits) {
   __shared__ double smax[128];
+  const double step = ldexp(1.0, bits);
   for (int r = blockIdx.x; r < n; r += gridDim.x) {
     double mx = 0.0;
     for (int c = threadIdx.x; c < n; c += blockDim.x) mx = fmax(mx, fabs(m[(long long)r * n + c]));
@@ -365,11 +370,11 @@ __global__ void slice_matrix_kernel(const double *__restrict__ m, __nv_bfloat16 
     for (int c = threadIdx.x; c < kp; c += blockDim.x) {
       double v = c < n ? m[(long long)r * n + c] / S : 0.0;
       for (int p = 0; p < TC_PLANES_M; p++) {
-        double y = v * 64.0;
+        double y = v * step;
         double d = rint(y);
         v = y - d;
-        // the fifth slice enters class 3, one factor 64 below its own weight
-        float q = p < TC_PLANES ? (float)d : (float)d * (1.0f / 64.0f);
+        // the fifth slice enters class 3, one factor 2^b below its own weight
+        float q = p < TC_PLANES ? (float)d : (float)(d / step);
         out[((long long)p * n + r) * kp + c] = __float2bfloat16_rn(q);
       }
     }
@@ -447,8 +452,15 @@ static cudaError_t make_map(CUtensorMap *map, const void *ptr, int kp, long long
 
 int tc_kp(int n) { return (n + 7) / 8 * 8; }
 
+// Slice width: classes 0 and 1 stay exact while K 2^(2b) <= 2^24, K the
+// contraction length rounded up to whole k-blocks.
+int tc_slice_bits(int n) {
+  const long long K = (long long)tc::BK * ((n + tc::BK - 1) / tc::BK);
+  return K <= 1024 ? 7 : 6;
+}
+
 cudaError_t tc_slice_matrix(const double *m, __nv_bfloat16 *planes, float *row_scale, int n, cudaStream_t s) {
-  tc::slice_matrix_kernel<<<n < 1024 ? n : 1024, 128, 0, s>>>(m, planes, row_scale, n, tc_kp(n));
+  tc::slice_matrix_kernel<<<n < 1024 ? n : 1024, 128, 0, s>>>(m, planes, row_scale, n, tc_kp(n), tc_slice_bits(n));
   launch_counter()++;
   return cudaGetLastError();
 }
@@ -458,7 +470,7 @@ cudaError_t tc_slice_fields(const float *x, const float *sub, float *scale, __nv
   long long warps = (long long)n * n * count;
   long long blocks = (warps * 32 + 255) / 256;
   int g = (int)(blocks > 152 * 32 ? 152 * 32 : blocks);
-  tc::slice_fields_kernel<<<g, 256, 0, s>>>(x, sub, scale, planes, n, tc_kp(n), count);
+  tc::slice_fields_kernel<<<g, 256, 0, s>>>(x, sub, scale, planes, n, tc_kp(n), count, tc_slice_bits(n));
   launch_counter()++;
   return cudaGetLastError();
 }
@@ -484,7 +496,8 @@ cudaError_t launch_modeprod_tc(const __nv_bfloat16 *mat, const __nv_bfloat16 *pl
     attr = true;
   }
   const int n = args.n, kp = tc_kp(n);
-  if ((long long)tc::BK * ((n + tc::BK - 1) / tc::BK) > 1040) return cudaErrorInvalidValue;  // exactness bound
+  const int bits = tc_slice_bits(n);
+  if ((long long)tc::BK * ((n + tc::BK - 1) / tc::BK) > (1LL << (24 - 2 * bits))) return cudaErrorInvalidValue;
   CUtensorMap ma, mb;
   cudaError_t e;
   if ((e = make_map(&ma, mat, kp, n, TC_PLANES_M, tc::BM)) != cudaSuccess) return e;
@@ -492,6 +505,7 @@ cudaError_t launch_modeprod_tc(const __nv_bfloat16 *mat, const __nv_bfloat16 *pl
   TcArgs g = args;
   g.kp = kp;
   g.kblocks = (n + tc::BK - 1) / tc::BK;
+  g.bits = bits;
   dim3 grid((unsigned)(((long long)n * n + tc::BN - 1) / tc::BN), (unsigned)((n + tc::BM - 1) / tc::BM),
             (unsigned)count);
   tc::modeprod_tc_kernel<<<grid, 128, tc::SMEM_BYTES, s>>>(ma, mb, g);

@@ -58,6 +58,9 @@ struct sclet_ctx {
   float4 *coef[2] = {nullptr, nullptr};   // ETD1 coefficient pairs per field kind
   float2 *coef2[2] = {nullptr, nullptr};  // ETD2 phi2 pairs per field kind
   double *stage64 = nullptr;  // n^3 FP64 staging block for host transfers
+  // conserved-field mass of the mixed form: FP64 weights wE, wP (, w2) of n^3
+  // each, target / after partial sums, last (target, before, shift)
+  double *massW = nullptr, *massPart = nullptr, *massRes = nullptr;
   // profiling
   bool profiling = false;
   std::vector<StageEv> evs;
@@ -134,6 +137,8 @@ int fail(sclet_ctx *ctx, int code, const std::string &msg) {
   return code;
 }
 
+int mass_weights_setup(sclet_ctx *ctx, const double *v, const double *vi);
+
 int upload_eigen(sclet_ctx *ctx, const double *d, const double *v, const double *vi) {
   const int n = ctx->n;
   std::vector<double> ds(n);
@@ -159,6 +164,7 @@ int upload_eigen(sclet_ctx *ctx, const double *d, const double *v, const double 
       CK(tc_make_coefs(ctx->coef[kind], ctx->coef2[kind], n, kind, ctx->dd[0], ctx->dd[1], ctx->dd[2], kk, p.epn2,
                        p.dt, p.landau[7 + 2 * kind], p.landau[8 + 2 * kind], ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->nch > 0) return mass_weights_setup(ctx, v, vi);
     return SCLET_OK;
   }
   for (int ax = 0; ax < 3; ax++) {
@@ -174,6 +180,33 @@ int upload_eigen(sclet_ctx *ctx, const double *d, const double *v, const double 
   launch_counter() += 2;
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));
+  return SCLET_OK;
+}
+
+EtdCoef etd_coef(sclet_ctx *ctx);
+
+// FP64 mass weights of the conserved field (see k_mass.cu) from the FP64 basis:
+// g = column sums of V over the owned rows, V^-T as a row-major matrix.
+int mass_weights_setup(sclet_ctx *ctx, const double *v, const double *vi) {
+  const int n = ctx->n;
+  std::vector<double> g(n, 0.0), viT((size_t)n * n);
+  for (int i = 2; i < n - 2; i++)
+    for (int q = 0; q < n; q++) g[q] += v[(size_t)i * n + q];
+  for (int i = 0; i < n; i++)
+    for (int q = 0; q < n; q++) viT[(size_t)i * n + q] = vi[(size_t)q * n + i];
+  double *dg = nullptr, *dm = nullptr;
+  cudaError_t e = cudaMalloc(&dg, sizeof(double) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&dm, sizeof(double) * n * n);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dg, g.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dm, viT.data(), sizeof(double) * n * n, cudaMemcpyHostToDevice, ctx->stream);
+  const EtdCoef ec = etd_coef(ctx);
+  const int nw = ctx->p.etd2 ? 3 : 2;
+  for (int w = 0; w < nw && e == cudaSuccess; w++)
+    e = mass_weight(ctx->massW + w * ctx->n3, ctx->stage64, dg, dm, n, w, ec, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(dg);
+  cudaFree(dm);
+  CK(e);
   return SCLET_OK;
 }
 
@@ -263,7 +296,8 @@ void sclet_destroy(sclet_ctx *ctx) {
                   ctx->partials, ctx->diag, ctx->phi1[0], ctx->phi1[1], ctx->phi2[0], ctx->phi2[1], ctx->dev_err,
                   ctx->fstate2, ctx->frhs2, ctx->ffelas, ctx->fscratch, ctx->fshell, ctx->W1, ctx->W2, ctx->P,
                   ctx->scaleP, ctx->rsV, ctx->rsVi, ctx->matV, ctx->matVi, ctx->stage64,
-                  ctx->coef[0], ctx->coef[1], ctx->coef2[0], ctx->coef2[1]};
+                  ctx->coef[0], ctx->coef[1], ctx->coef2[0], ctx->coef2[1], ctx->massW, ctx->massPart,
+                  ctx->massRes};
   for (void *b : bufs) cudaFree(b);
   for (int a = 0; a < 3; a++) {
     cudaFree(ctx->V[a]);
@@ -412,6 +446,11 @@ int sclet_create(const sclet_params *p, int precision, int device, sclet_ctx **o
     for (int k = 0; k < 2; k++) {
       CC(cudaMalloc(&ctx->coef[k], sizeof(float4) * ctx->n3));
       if (p->etd2) CC(cudaMalloc(&ctx->coef2[k], sizeof(float2) * ctx->n3));
+    }
+    if (ctx->nch > 0) {
+      CC(cudaMalloc(&ctx->massW, sizeof(double) * ctx->n3 * (p->etd2 ? 3 : 2)));
+      CC(cudaMalloc(&ctx->massPart, sizeof(double) * 4 * mass_partials()));
+      CC(cudaMalloc(&ctx->massRes, sizeof(double) * 4));
     }
   }
   {
@@ -569,7 +608,10 @@ static cudaError_t tc_slice(sclet_ctx *ctx, const float *x, const float *sub, in
 // along x, y, z back to the FP32 state.
 static int etd_update_mixed(sclet_ctx *ctx) {
   const int F = ctx->F;
-  const long long ps = plane_stride(ctx), rows = (long long)ctx->n * ctx->n;
+  const long long ps = plane_stride(ctx), rows = (long long)ctx->n * ctx->n, n3 = ctx->n3;
+  if (ctx->nch > 0)  // target mass of the conserved field from (u, N1)
+    CK(mass_target(fu_of(ctx) + ctx->nac * n3, ctx->massW, frhs1_of(ctx) + ctx->nac * n3, nullptr, ctx->massW + n3,
+                   ctx->n, ctx->massPart, ctx->stream));
   CK(tc_slice(ctx, ctx->fstate2, nullptr, 2 * F));
   CK(tc_prod(ctx, false, ctx->P, ctx->scaleP, 2 * F, ctx->W1, 0, nullptr, 1));
   CK(tc_slice(ctx, ctx->W1, nullptr, 2 * F));
@@ -583,12 +625,19 @@ static int etd_update_mixed(sclet_ctx *ctx) {
   CK(tc_prod(ctx, true, ctx->P, ctx->scaleP, F, ctx->W1, 0, nullptr, 1));
   CK(tc_slice(ctx, ctx->W1, nullptr, F));
   CK(tc_prod(ctx, true, ctx->P, ctx->scaleP, F, fu_of(ctx), 0, nullptr, 1));
+  if (ctx->nch > 0)
+    CK(mass_fix(fu_of(ctx) + ctx->nac * n3, ctx->n, ctx->massPart, ctx->massPart + 2 * mass_partials(), ctx->massRes,
+                ctx->stream));
   return SCLET_OK;
 }
 
 // ETD2 corrector (ScLETD.c:159-188): u += V phi2 V^-1 (N2 - N1).
 static int etd2_correct_mixed(sclet_ctx *ctx) {
   const int F = ctx->F;
+  const long long n3 = ctx->n3, off = ctx->nac * n3;
+  if (ctx->nch > 0)  // target: current mass plus <w2, N2 - N1>
+    CK(mass_target(fu_of(ctx) + off, nullptr, ctx->frhs2 + off, frhs1_of(ctx) + off, ctx->massW + 2 * n3, ctx->n,
+                   ctx->massPart, ctx->stream));
   CK(tc_slice(ctx, ctx->frhs2, frhs1_of(ctx), F));
   CK(tc_prod(ctx, false, ctx->P, ctx->scaleP, F, ctx->W1, 0, nullptr, 1));
   CK(tc_slice(ctx, ctx->W1, nullptr, F));
@@ -601,6 +650,9 @@ static int etd2_correct_mixed(sclet_ctx *ctx) {
   CK(tc_prod(ctx, true, ctx->P, ctx->scaleP, F, ctx->W1, 0, nullptr, 1));
   CK(tc_slice(ctx, ctx->W1, nullptr, F));
   CK(tc_prod(ctx, true, ctx->P, ctx->scaleP, F, fu_of(ctx), 0, nullptr, 2));
+  if (ctx->nch > 0)
+    CK(mass_fix(fu_of(ctx) + off, ctx->n, ctx->massPart, ctx->massPart + 2 * mass_partials(), ctx->massRes,
+                ctx->stream));
   return SCLET_OK;
 }
 

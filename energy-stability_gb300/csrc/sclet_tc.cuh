@@ -6,12 +6,13 @@
 
 namespace sclet {
 
-constexpr int TC_PLANES = 4;    // fixed-point slices per data operand (6 bits each)
+constexpr int TC_PLANES = 4;    // fixed-point slices per data operand (tc_slice_bits each)
 constexpr int TC_PLANES_M = 5;  // slices per matrix: four 6-bit slices and a fifth
                                 // stored pre-scaled by 1/64 (see k_modeprod_tc.cu)
 
 struct TcArgs {
   int n, kp, kblocks, count;
+  int bits;                 // slice width (set by launch_modeprod_tc)
   int epi;                  // 0 none, 1 ETD1 update (aux = uhat), 2 phi2 scaling
   int outmode;              // 1 FP32 store, 2 FP32 accumulate
   const float *aux;         // [count][n^3] FP32 uhat, same layout as out
@@ -28,6 +29,7 @@ struct TcArgs {
 };
 
 int tc_kp(int n);
+int tc_slice_bits(int n);
 // Row-major FP64 n x n matrix -> TC_PLANES_M slice planes [p][n][kp] (zero padded
 // columns) and the power-of-two scale of each row.
 cudaError_t tc_slice_matrix(const double *m, __nv_bfloat16 *planes, float *row_scale, int n, cudaStream_t s);
