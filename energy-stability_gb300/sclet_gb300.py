@@ -94,6 +94,8 @@ SIGNATURES = {
     "sclet_launch_count": (ctypes.c_longlong, [ctypes.c_void_p]),
     "sclet_host_alloc": (ctypes.c_void_p, [ctypes.c_size_t]),
     "sclet_host_free": (None, [ctypes.c_void_p]),
+    "sclet_check_soln_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                                ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]),
 }
 
 _LIB = None

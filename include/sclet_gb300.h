@@ -193,6 +193,28 @@ long long sclet_launch_count(const sclet_ctx *ctx);
 void *sclet_host_alloc(size_t bytes);
 void sclet_host_free(void *ptr);
 
+/* ---- diagnostics without allocation ------------------------------------- */
+/* No counterpart in the reference, whose check_soln_new (field.c:407-678)
+ * reads the process-global arrays.  The same diagnostics as sclet_check_soln
+ * (same kernels, default gradient tensors) of a state block the caller holds
+ * on the current device, for callers that must not allocate: a fixed memory
+ * budget or pool, or work already queued on other streams that a cudaMalloc
+ * would stall.  It allocates nothing and needs no context: scratch is a fixed
+ * device array inside the library (about 230 KB per device).
+ *   fields    device, field-count blocks of nx^3 cells, AC fields first:
+ *             double when precision = SCLET_FP64, float when SCLET_MIXED
+ *   out       device, 4 doubles per field: max, min, vol, energy
+ *   stream    cudaStream_t on the current device (NULL: legacy default)
+ *   msg       optional buffer for the error text (msg_len bytes)
+ * Returns after queuing the work (SCLET_OK) or an error code; more than
+ * SCLET_NOALLOC_MAX_FIELDS fields is SCLET_ERR_ARG.  The first call on a
+ * device looks the scratch address up (set-up); make it before any stream
+ * capture.  The scratch is shared: calls that overlap in time on one device
+ * race on it, so order them on one stream. */
+#define SCLET_NOALLOC_MAX_FIELDS 5
+int sclet_check_soln_noalloc(const sclet_params *p, int precision, const void *fields, int energy_form,
+                             double *out, void *stream, char *msg, size_t msg_len);
+
 #ifdef __cplusplus
 }
 #endif
