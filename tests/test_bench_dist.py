@@ -4,7 +4,6 @@ between replicas; the only collectives are the barrier and the max over ranks
 of the timed region."""
 import json
 import os
-import re
 import socket
 import subprocess
 import sys
@@ -33,17 +32,17 @@ def test_two_rank_max_and_barrier(tmp_path):
         "assert world == 2\n"
         "bench.dist_barrier(world)\n"
         "m = bench.dist_max(10.0 + rank, world)\n"
-        "print('RANK', rank, 'MAX', m, flush=True)\n"
-        "import torch.distributed as dist; dist.destroy_process_group()\n" % ROOT)
+        "open(%r + '/rank%%d.txt' %% rank, 'w').write('RANK %%d MAX %%s' %% (rank, m))\n"
+        "import torch.distributed as dist; dist.destroy_process_group()\n" % (ROOT, str(tmp_path)))
     script = tmp_path / "ranks.py"
     script.write_text(code)
     r = subprocess.run([sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=2",
                         "--master-addr=127.0.0.1", f"--master-port={_port()}", str(script)],
                        capture_output=True, text=True, timeout=300, env=_env(), cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
-    # the two ranks share one pipe: match records, not whole lines
-    found = sorted(re.findall(r"RANK (\d) MAX ([0-9.]+)", r.stdout))
-    assert found == [("0", "11.0"), ("1", "11.0")], r.stdout
+    # one record file per rank (the ranks share one stdout pipe)
+    found = sorted((tmp_path / f"rank{k}.txt").read_text() for k in range(2))
+    assert found == ["RANK 0 MAX 11.0", "RANK 1 MAX 11.0"], (found, r.stdout)
 
 
 def test_reference_arm_two_ranks_prints_once(oracle_lib):
