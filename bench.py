@@ -1,7 +1,7 @@
 """Benchmark of the ScLETD ETD step on GB300.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|mixed]
-                    [--impl reference] [--size N3EDGE]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision mixed|fp64]
+                    [--impl reference] [--size N3EDGE] [--accuracy-steps S]
 
 Workload: the beta->alpha coupled case -- one conserved concentration
 c = 0.5 + U(-0.02, 0.02) and four order parameters U(-0.01, 0.01) on a 192^3
@@ -13,9 +13,12 @@ stabiliser kk = 0.5, cubic elasticity C11/C12/C44 = 1.0/0.6/0.4 with four
 A step is one pass of the reference's time loop (ghost exchange, elastic
 force, right-hand sides, eigenbasis transforms and update) plus the
 diagnostics check_soln_new it runs every pass.  `value` is cell-updates/s
-(N^3 owned cells x steps / time) with the state resident in HBM; `e2e` is the
-same through the C ABI with the fields copied in from pinned host memory and
-copied back out (with the diagnostics) every step.
+(N^3 owned cells x steps / time) of the mixed-precision step (default) with
+the state resident in HBM; `e2e` is the same through the C ABI with the
+fields copied in from pinned host memory and copied back out (with the
+diagnostics) every step.  The plain FP64 step is timed beside it ("fp64"),
+and "accuracy_vs_fp64" compares the two forms after --accuracy-steps steps
+from the same state.
 
 --impl reference times the reference's CPU path (the C restatement of
 oracle/, the reference's own build cannot run on this host) on all host
@@ -194,6 +197,112 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+STAGES = ["products", "rhs", "elastic", "halo", "diagnostics", "tc_kernel", "slicing"]
+
+
+def peaks():
+    """Measured HBM copy bandwidth and bf16 GEMM throughput of this GPU model
+    (MEASURED_PEAKS.json beside this file), else the earlier GB300 figures."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fp:
+            d = json.load(fp)
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured (MEASURED_PEAKS.json)"
+    except Exception:
+        return 6800.0, 1900.0, "fallback (no MEASURED_PEAKS.json)"
+
+
+def timed_steps(s, steps, world, local):
+    """K steps, each bracketed by CUDA events on the context's stream, with the
+    diagnostics of every step (the reference runs check_soln_new each pass)."""
+    dist_barrier(world)
+    l0 = s.launch_count()
+    with ClockSampler(local) as clk:
+        s.sync()
+        ms = 0.0
+        for _ in range(steps):
+            ms += s.time_steps(1)
+            s.check_soln()
+    return ms, s.launch_count() - l0, clk.summary()
+
+
+def profiled_stages(s, steps=2):
+    s.set_profiling(True)
+    s.time_steps(steps)
+    ms, launches = s.stage_times(len(STAGES))
+    s.set_profiling(False)
+    return dict(zip(STAGES, ms)), dict(zip(STAGES, launches))
+
+
+def tc_roofline(case, stage_ms, stage_launches, steps):
+    """Roofline of the tensor-core mode-n product kernel over `steps` profiled
+    steps.  Per tensor-product (n x n matrix times an n^3 tensor): algorithmic
+    flops 2 n^4; bytes the kernel must move given its interface: the four BF16
+    slice planes of the input (8 B per element over kp = roundup(n, 8)
+    columns) and the FP32 output (4 B per element); the fused ETD update of one
+    product in nine also reads the other operand (4 B) and the coefficient
+    pairs (16 B).  Physical MMA work: eleven BF16 MMAs over 128-row tiles."""
+    n, F = case.n, case.nac + case.nch
+    kp = (n + 7) // 8 * 8
+    kk = (n + 31) // 32 * 32
+    per_step_products = 9 * F
+    elems = n ** 3
+    bytes_step = per_step_products * elems * (8.0 * kp / n + 4.0) + F * elems * 20.0
+    flops_step = per_step_products * 2.0 * n ** 4
+    a_pad = (n + 127) // 128 * 128
+    r_pad = (n * n + 127) // 128 * 128
+    mma_step = per_step_products * 11 * 2.0 * a_pad * r_pad * kk
+    t = stage_ms["tc_kernel"] / 1000.0
+    launches = max(stage_launches["tc_kernel"], 1)
+    hbm, bf16, src = peaks()
+    gbs = bytes_step * steps / t / 1e9
+    return {
+        "bound": "hbm", "kernel": "modeprod_tc_kernel (split-BF16 tcgen05 eigenbasis products)",
+        "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm, "traffic": None,
+        "peak_source": src, "avg_launch_ms": stage_ms["tc_kernel"] / launches,
+        "bytes_per_step": bytes_step,
+        "tensor": {"algorithmic_tflops": flops_step * steps / t / 1e12,
+                   "mma_tflops": mma_step * steps / t / 1e12, "peak_bf16_tflops": bf16,
+                   "mma_frac": mma_step * steps / t / 1e12 / bf16},
+    }
+
+
+def accuracy_check(sg, params, u0, steps, every, local):
+    """Mixed against FP64 from the same state: at every `every` steps up to
+    `steps`, relative L2 per field over the owned cells, the energy (pointwise
+    and as |dE| / max|E| over the curve so far) and the relative difference of
+    each field's volume integral (the conserved field's mass)."""
+    if steps <= 0:
+        return None
+    every = every if every > 0 else steps
+    a = sg.Solver(params, sg.FP64, device=local)
+    b = sg.Solver(params, sg.MIXED, device=local)
+    for x in (a, b):
+        x.set_fields(u0)
+    own = (slice(2, -2),) * 3
+    e64, e32, rows = [a.check_soln()[0, 3]], [b.check_soln()[0, 3]], []
+    done = 0
+    while done < steps:
+        k = min(every, steps - done)
+        a.step(k)
+        b.step(k)
+        done += k
+        ua, ub = a.get_fields(), b.get_fields()
+        da, db = a.check_soln(), b.check_soln()
+        e64.append(da[0, 3])
+        e32.append(db[0, 3])
+        rel = [float(np.linalg.norm(ub[f][own] - ua[f][own]) / np.linalg.norm(ua[f][own])) for f in range(ua.shape[0])]
+        rows.append({"step": done, "field_rel_l2": rel,
+                     "energy_rel": float(abs(db[0, 3] - da[0, 3]) / abs(da[0, 3])),
+                     "energy_curve_rel": float(np.max(np.abs(np.array(e32) - np.array(e64))) / np.max(np.abs(e64))),
+                     "volume_rel": [float(abs(db[f, 2] - da[f, 2]) / abs(da[f, 2])) for f in range(ua.shape[0])],
+                     "max_abs_eta": float(np.abs(ua[0][own]).max())})
+    a.close()
+    b.close()
+    last = rows[-1]
+    return {"steps": steps, "max_field_rel_l2": max(last["field_rel_l2"]),
+            "energy_curve_rel": max(r["energy_curve_rel"] for r in rows), "checkpoints": rows}
+
+
 def run_gpu(args, world, rank, local):
     import sclet_gb300 as sg
     sg.lib()
@@ -203,28 +312,19 @@ def run_gpu(args, world, rank, local):
     with tempfile.TemporaryDirectory() as td:
         cases.write_case(case, td, eigen=False, fields=False)
         params = sg.read_case(td, case.suffix)
-    s = sg.Solver(params, precision, device=local)
     u0 = block_fields(case)
+    s = sg.Solver(params, precision, device=local)
     s.set_fields(u0)
-    # warm-up
     s.step(args.warmup)
     s.check_soln()
-    # device-resident timed region: K steps, diagnostics every step
-    dist_barrier(world)
-    l0 = s.launch_count()
-    with ClockSampler(local) as clk:
-        s.sync()
-        t0 = time.perf_counter()
-        ms = 0.0
-        for _ in range(args.steps):
-            ms += s.time_steps(1)
-            s.check_soln()
-        wall = time.perf_counter() - t0
-    launches = s.launch_count() - l0
+    # device-resident timed region
+    ms, launches, clocks = timed_steps(s, args.steps, world, local)
     ms_max = dist_max(ms, world)
     cells = case.big_n ** 3 * args.steps * world
     value = cells / (ms_max / 1000.0)
-    # end to end through the C ABI with host buffers
+    # end to end through the C ABI with host buffers: every step copies all
+    # fields in from pinned memory, steps, runs the diagnostics and copies all
+    # fields back out
     pin_in = sg.PinnedArray((F, n, n, n))
     pin_out = sg.PinnedArray((F, n, n, n))
     pin_in.array[...] = u0
@@ -241,40 +341,56 @@ def run_gpu(args, world, rank, local):
     e2e_s = dist_max(time.perf_counter() - t0, world)
     e2e_value = cells / e2e_s
     bytes_step = F * n ** 3 * 8
-    # per-stage timing for the roofline of the dominant kernel class
-    s.set_profiling(True)
-    s.time_steps(2)
-    stage_ms, stage_launches = s.stage_times(5)
-    s.set_profiling(False)
-    s.close()
     pin_in.free()
     pin_out.free()
+    stage_ms, stage_launches = profiled_stages(s, 2)
+    s.close()
+    # the plain FP64 step beside it (same workload, same timing)
+    fp64 = None
+    if precision == sg.MIXED and not args.no_fp64:
+        s64 = sg.Solver(params, sg.FP64, device=local)
+        s64.set_fields(u0)
+        s64.step(args.warmup)
+        ms64, _, _ = timed_steps(s64, args.steps, world, local)
+        st64, _ = profiled_stages(s64, 1)
+        s64.close()
+        ms64 = dist_max(ms64, world)
+        fp64 = {"value": cells / (ms64 / 1000.0), "ms_per_step": ms64 / args.steps,
+                "speedup_of_mixed": ms64 / ms_max, "stage_ms_per_step": st64}
+    accuracy = None
+    if precision == sg.MIXED and rank == 0:
+        accuracy = accuracy_check(sg, params, u0, args.accuracy_steps, args.accuracy_every, local)
     if rank != 0:
         return
-    flops_products = 2.0 * n ** 4 * 9 * F * 2  # 9 rotating products per field per ETD1 step, 2 steps
-    achieved = flops_products / (stage_ms[0] / 1000.0) / 1e12
-    roofline = {"bound": "fp64", "kernel": "modeprod_f64 (eigenbasis mode-n products)",
-                "achieved": achieved, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s", "frac": achieved / FP64_PEAK_TFLOPS,
-                "traffic": None, "peak_source": "measured FP64 FMA probe on GB300",
-                "avg_launch_ms": stage_ms[0] / max(stage_launches[0], 1),
-                "stage_ms": dict(zip(["products", "rhs", "elastic", "halo", "diagnostics"], stage_ms)),
-                "stage_launches": dict(zip(["products", "rhs", "elastic", "halo", "diagnostics"], stage_launches))}
+    if precision == sg.MIXED:
+        roofline = tc_roofline(case, stage_ms, stage_launches, 2)
+    else:
+        flops_products = 2.0 * n ** 4 * 9 * F * 2
+        achieved = flops_products / (stage_ms["products"] / 1000.0) / 1e12
+        roofline = {"bound": "fp64", "kernel": "modeprod_f64 (eigenbasis mode-n products)", "achieved": achieved,
+                    "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s", "frac": achieved / FP64_PEAK_TFLOPS, "traffic": None,
+                    "peak_source": "FP64 FMA throughput measured on GB300",
+                    "avg_launch_ms": stage_ms["products"] / max(stage_launches["products"], 1)}
+    roofline["stage_ms_per_step"] = {k: v / 2 for k, v in stage_ms.items()}
+    roofline["stage_launches_per_step"] = {k: v // 2 for k, v in stage_launches.items()}
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         small = workload(args.size, seed=1000)
-        rate, cores, secs, _ = cpu_oracle_rate(small, args.cpu_steps, 0)
+        rate, cores, secs, done = cpu_oracle_rate(small, args.cpu_steps, 0)
         cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"{args.cpu_steps} full steps of the same workload, C restatement of the reference's step "
-                         f"on {cores} host threads ({secs:.1f} s)"}
+               "sample": f"{done} full steps of the same workload with diagnostics, C restatement of the "
+                         f"reference's step on {cores} host threads ({secs:.1f} s)"}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if precision == sg.FP64 else "bf16x3/f32", "data": "synthetic",
+        "dtype": "f64" if precision == sg.FP64 else "bf16-slices/f32 (f64 eigenbasis, diagnostics, mass)",
+        "data": "synthetic",
         "config": {"workload": workload_name(args.size), "cells_per_step": args.size ** 3,
                    "precision": args.precision, "l2": "inputs larger than L2 (state of a step > 129 MB)",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": bytes_step, "d2h_bytes_per_step": bytes_step},
-        "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
+        "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
+        "fp64": fp64, "accuracy_vs_fp64": accuracy,
     }
     print(json.dumps(line), flush=True)
 
@@ -285,10 +401,14 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--size", type=int, default=192, help="physical grid edge N")
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true", help="skip timing the plain FP64 step beside the mixed one")
+    ap.add_argument("--accuracy-steps", type=int, default=100,
+                    help="steps of the mixed-vs-FP64 check from the same state (0: skip)")
+    ap.add_argument("--accuracy-every", type=int, default=0, help="checkpoint interval of that check (0: end only)")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":

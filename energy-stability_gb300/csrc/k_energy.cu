@@ -59,7 +59,7 @@ __global__ void __launch_bounds__(EB) energy_partial_kernel(Phys ph, const T *__
     int i = 2 + (int)(g % N), j = 2 + (int)((g / N) % N), k = 2 + (int)(g / ((long long)N * N));
     long long l = ((long long)k * n + j) * n + i;
     for (int f = 0; f < F; f++) {
-      double t = (double)u[f * n3 + l];
+      double t = (double)u[f * n3 + l] + (f >= nac ? ph.cshift : 0.0);
       mx[f] = fmax(mx[f], t);
       mn[f] = fmin(mn[f], t);
       ks_add(vol[f], t + 1.0);
@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(EB) energy_partial_kernel(Phys ph, const T *__
       const T *q = u + f * n3;
       double v0 = q[l], v1 = q[l + 1], v2 = q[l + n], v3 = q[l + n + 1];
       double v4 = q[l + n * n], v5 = q[l + n * n + 1], v6 = q[l + n * n + n], v7 = q[l + n * n + n + 1];
-      avg[f] = (v0 + v1 + v2 + v3 + v4 + v5 + v6 + v7) / 8;
+      avg[f] = (v0 + v1 + v2 + v3 + v4 + v5 + v6 + v7) / 8 + (f >= nac ? ph.cshift : 0.0);
       double ux = ((v1 - v0) + (v3 - v2) + (v5 - v4) + (v7 - v6)) / 4 / hx;
       double uy = ((v2 - v0) + (v3 - v1) + (v6 - v4) + (v7 - v5)) / 4 / hy;
       double uz = ((v4 - v0) + (v5 - v1) + (v6 - v2) + (v7 - v3)) / 4 / hz;

@@ -39,7 +39,7 @@ static P<T> to_p(const Phys &ph) {
   p.ih2z = (T)(1.0 / (ph.h[2] * ph.h[2]));
   p.i2hx = (T)(0.5 / ph.h[0]); p.i2hy = (T)(0.5 / ph.h[1]); p.i2hz = (T)(0.5 / ph.h[2]);
   p.LE = (T)ph.LE; p.KE = (T)ph.KE; p.LCI = (T)ph.LCI; p.KCI = (T)ph.KCI; p.es = (T)ph.elastic_scale;
-  p.a2 = (T)ph.a2; p.a4 = (T)ph.a4; p.a6 = (T)ph.a6; p.g = (T)ph.g; p.th = (T)ph.th; p.c0 = (T)ph.c0; p.A = (T)ph.A;
+  p.a2 = (T)ph.a2; p.a4 = (T)ph.a4; p.a6 = (T)ph.a6; p.g = (T)ph.g; p.th = (T)ph.th; p.c0 = (T)(ph.c0 - ph.cshift); p.A = (T)ph.A;
   for (int m = 0; m < 4; m++)
     for (int k = 0; k < 9; k++) p.lam[m][k] = (T)ph.lam[m][k];
   return p;

@@ -118,13 +118,13 @@ __global__ void phi_kernel(double *phi1, double *phi2, int n, int kind, const do
   }
 }
 
-__global__ void f64_to_f32(const double *__restrict__ a, float *__restrict__ b, long long count) {
+__global__ void f64_to_f32(const double *__restrict__ a, float *__restrict__ b, long long count, double shift) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x)
-    b[i] = (float)a[i];
+    b[i] = (float)(a[i] - shift);
 }
-__global__ void f32_to_f64(const float *__restrict__ a, double *__restrict__ b, long long count) {
+__global__ void f32_to_f64(const float *__restrict__ a, double *__restrict__ b, long long count, double shift) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x)
-    b[i] = (double)a[i];
+    b[i] = (double)a[i] + shift;
 }
 
 int grid_of(long long total) {
@@ -250,13 +250,14 @@ int field_index(sclet_ctx *ctx, int kind, int m) {
   return -1;
 }
 
-// host FP64 block -> device block of the working precision
-int put_block(sclet_ctx *ctx, const double *host, double *dst64, float *dst32) {
+// host FP64 block -> device block of the working precision (FP32 blocks store
+// value - shift)
+int put_block(sclet_ctx *ctx, const double *host, double *dst64, float *dst32, double shift = 0.0) {
   if (!mixed(ctx)) {
     CK(cudaMemcpyAsync(dst64, host, sizeof(double) * ctx->n3, cudaMemcpyHostToDevice, ctx->stream));
   } else {
     CK(cudaMemcpyAsync(ctx->stage64, host, sizeof(double) * ctx->n3, cudaMemcpyHostToDevice, ctx->stream));
-    f64_to_f32<<<grid_of(ctx->n3), 256, 0, ctx->stream>>>(ctx->stage64, dst32, ctx->n3);
+    f64_to_f32<<<grid_of(ctx->n3), 256, 0, ctx->stream>>>(ctx->stage64, dst32, ctx->n3, shift);
     launch_counter()++;
     CK(cudaGetLastError());
   }
@@ -264,11 +265,11 @@ int put_block(sclet_ctx *ctx, const double *host, double *dst64, float *dst32) {
   return SCLET_OK;
 }
 
-int get_block(sclet_ctx *ctx, const double *src64, const float *src32, double *host) {
+int get_block(sclet_ctx *ctx, const double *src64, const float *src32, double *host, double shift = 0.0) {
   if (!mixed(ctx)) {
     CK(cudaMemcpyAsync(host, src64, sizeof(double) * ctx->n3, cudaMemcpyDeviceToHost, ctx->stream));
   } else {
-    f32_to_f64<<<grid_of(ctx->n3), 256, 0, ctx->stream>>>(src32, ctx->stage64, ctx->n3);
+    f32_to_f64<<<grid_of(ctx->n3), 256, 0, ctx->stream>>>(src32, ctx->stage64, ctx->n3, shift);
     launch_counter()++;
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(host, ctx->stage64, sizeof(double) * ctx->n3, cudaMemcpyDeviceToHost, ctx->stream));
@@ -376,6 +377,7 @@ int sclet_create(const sclet_params *p, int precision, int device, sclet_ctx **o
   ph.g = p->landau[3];
   ph.th = p->landau[4];
   ph.c0 = p->landau[5];
+  ph.cshift = (precision == SCLET_MIXED && ctx->nch > 0) ? ph.c0 : 0.0;
   ph.A = p->landau[6];
   ph.LE = p->landau[7];
   ph.KE = p->landau[8];
@@ -498,14 +500,14 @@ int sclet_set_energy_tensors(sclet_ctx *ctx, const double *lam) {
 int sclet_set_field(sclet_ctx *ctx, int kind, int m, const double *block) {
   int f = field_index(ctx, kind, m);
   if (f < 0) return fail(ctx, SCLET_ERR_ARG, "no such field");
-  return mixed(ctx) ? put_block(ctx, block, nullptr, fu_of(ctx) + f * ctx->n3)
+  return mixed(ctx) ? put_block(ctx, block, nullptr, fu_of(ctx) + f * ctx->n3, f >= ctx->nac ? ctx->ph.cshift : 0.0)
                     : put_block(ctx, block, u_of(ctx) + f * ctx->n3, nullptr);
 }
 
 int sclet_get_field(sclet_ctx *ctx, int kind, int m, double *block) {
   int f = field_index(ctx, kind, m);
   if (f < 0) return fail(ctx, SCLET_ERR_ARG, "no such field");
-  return mixed(ctx) ? get_block(ctx, nullptr, fu_of(ctx) + f * ctx->n3, block)
+  return mixed(ctx) ? get_block(ctx, nullptr, fu_of(ctx) + f * ctx->n3, block, f >= ctx->nac ? ctx->ph.cshift : 0.0)
                     : get_block(ctx, u_of(ctx) + f * ctx->n3, nullptr, block);
 }
 
@@ -578,6 +580,9 @@ int sclet_calc_rhs(sclet_ctx *ctx, int slot) {
 // `planes`, row scales at `scale`) into FP32 `out`.
 static cudaError_t tc_prod(sclet_ctx *ctx, bool inverse, const __nv_bfloat16 *planes, const float *scale, int count,
                            float *out, int epi, const float *aux, int outmode) {
+  StageEv ev;
+  long long l0 = launch_counter();
+  stage_begin(ctx, 5, ev);
   TcArgs g;
   memset(&g, 0, sizeof g);
   g.n = ctx->n;
@@ -595,12 +600,19 @@ static cudaError_t tc_prod(sclet_ctx *ctx, bool inverse, const __nv_bfloat16 *pl
   g.nac = ctx->nac;
   g.F = ctx->F;
   g.err = ctx->dev_err;
-  return launch_modeprod_tc(inverse ? ctx->matV : ctx->matVi, planes, count, g, ctx->stream);
+  cudaError_t e = launch_modeprod_tc(inverse ? ctx->matV : ctx->matVi, planes, count, g, ctx->stream);
+  stage_end(ctx, ev, l0);
+  return e;
 }
 
 // x (count FP32 blocks, minus sub) -> slice planes P and row scales
 static cudaError_t tc_slice(sclet_ctx *ctx, const float *x, const float *sub, int count) {
-  return tc_slice_fields(x, sub, ctx->scaleP, ctx->P, ctx->n, count, ctx->stream);
+  StageEv ev;
+  long long l0 = launch_counter();
+  stage_begin(ctx, 6, ev);
+  cudaError_t e = tc_slice_fields(x, sub, ctx->scaleP, ctx->P, ctx->n, count, ctx->stream);
+  stage_end(ctx, ev, l0);
+  return e;
 }
 
 // Mixed form of the transforms (ScLETD.c:105-142): V^-1 along x and y for u
@@ -761,12 +773,12 @@ int sclet_mode_product(sclet_ctx *ctx, int inverse, const double *in, double *ou
     // in -> FP32 scratch, slices, product, FP32 -> host FP64
     float *tmp = ctx->fscratch;
     CK(cudaMemcpyAsync(ctx->stage64, in, sizeof(double) * n3, cudaMemcpyHostToDevice, ctx->stream));
-    f64_to_f32<<<grid_of(n3), 256, 0, ctx->stream>>>(ctx->stage64, tmp, n3);
+    f64_to_f32<<<grid_of(n3), 256, 0, ctx->stream>>>(ctx->stage64, tmp, n3, 0.0);
     launch_counter()++;
     CK(cudaGetLastError());
     CK(tc_slice(ctx, tmp, nullptr, 1));
     CK(tc_prod(ctx, inverse != 0, ctx->P, ctx->scaleP, 1, tmp + n3, 0, nullptr, 1));
-    f32_to_f64<<<grid_of(n3), 256, 0, ctx->stream>>>(tmp + n3, ctx->stage64, n3);
+    f32_to_f64<<<grid_of(n3), 256, 0, ctx->stream>>>(tmp + n3, ctx->stage64, n3, 0.0);
     launch_counter()++;
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(out, ctx->stage64, sizeof(double) * n3, cudaMemcpyDeviceToHost, ctx->stream));

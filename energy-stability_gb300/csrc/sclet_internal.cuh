@@ -18,6 +18,12 @@ struct Phys {
   double lam[4][9];      // F2 tensors: diag(kk) - file tensor, row-major
   double elastic_scale;
   double a2, a4, a6, g, th, c0, A, LE, KE, LCI, KCI;
+  // Offset of the stored conserved field: the device holds c - cshift.  The
+  // mixed form stores c - c0 (cshift = c0), which keeps FP32 storage and the
+  // transforms at the scale of the fluctuations; the scheme is linear in c
+  // and the constant state c0 is a fixed point, so this changes nothing in
+  // exact arithmetic.  0 in the FP64 form.
+  double cshift;
 };
 
 // Geometry helpers (owned cells are 2 .. n-3 per axis, period N = n - 4).

@@ -166,7 +166,9 @@ int sclet_check_soln(sclet_ctx *ctx, int energy_form, sclet_diag *out);
 int sclet_set_energy_tensors(sclet_ctx *ctx, const double *lam /* nac*9 */);
 
 /* ---- inspection (host buffers) ------------------------------------------ */
-/* fieldE1/fieldE2 of one field, and the elastic force felas. */
+/* fieldE1/fieldE2 of one field, and the elastic force felas.  In the mixed
+ * form the conserved field is held as c - c0, and its right-hand side is that
+ * of c minus that of the constant state c0 (zero away from the block faces). */
 int sclet_get_rhs(sclet_ctx *ctx, int slot, int kind, int m, double *block);
 int sclet_get_felas(sclet_ctx *ctx, int m, double *block);
 /* One mode-n product with layout rotation (one PUX/PUY/PUZ contraction,
@@ -181,8 +183,10 @@ int sclet_sync(sclet_ctx *ctx);
 int sclet_time_steps(sclet_ctx *ctx, int nsteps, float *ms);
 /* Per-kernel-class timing of the last sclet_time_steps call when profiling
  * was enabled with sclet_set_profiling(ctx, 1): ms[k] for classes
- * 0 mode-n products, 1 right-hand sides, 2 FFT/elastic, 3 halo, 4 diagnostics;
- * launches[k] kernel launches. */
+ * 0 mode-n products (all of the eigenbasis transforms and the update),
+ * 1 right-hand sides, 2 FFT/elastic, 3 halo, 4 diagnostics, and within class
+ * 0 of the mixed form: 5 tensor-core product kernels, 6 slicing kernels;
+ * launches[k] kernel launches.  Up to 8 classes. */
 int sclet_set_profiling(sclet_ctx *ctx, int on);
 int sclet_stage_times(const sclet_ctx *ctx, float *ms, int *launches, int nclasses);
 /* Kernel launches issued by this context so far. */
