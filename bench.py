@@ -51,7 +51,11 @@ import cases  # noqa: E402
 
 METRIC = "cell-updates/s on 1 GB300: mixed/learned vs plain FP64 at ≤1e-5 rel L2"
 UNIT = "cell-updates/s"
-FP64_PEAK_TFLOPS = 1.20  # measured FP64 FMA throughput of this machine's GB300 (profiles/gb300_throughput_probe.md)
+# DRAM bytes (read + write) of one tensor-core product launch over its
+# algorithmic bytes, from an ncu capture at 160^3: (363.0 + 156.2) MB over
+# (361.4 + 176.4) MB.
+TC_TRAFFIC_RATIO = 0.965
+FP64_PEAK_TFLOPS = 1.25  # nominal GB300 FP64 rate (the measured peaks cover HBM and bf16 only)
 
 
 def workload(big_n: int, seed: int) -> cases.Case:
@@ -253,13 +257,17 @@ def tc_roofline(case, stage_ms, stage_launches, steps):
     mma_step = per_step_products * 11 * 2.0 * a_pad * r_pad * kk
     t = stage_ms["tc_kernel"] / 1000.0
     launches = max(stage_launches["tc_kernel"], 1)
+    per_launch = bytes_step * steps / launches
     hbm, bf16, src = peaks()
     gbs = bytes_step * steps / t / 1e9
     return {
         "bound": "hbm", "kernel": "modeprod_tc_kernel (split-BF16 tcgen05 eigenbasis products)",
-        "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm, "traffic": None,
+        "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
+        "traffic": per_launch * TC_TRAFFIC_RATIO,
+        "traffic_source": f"ncu DRAM read+write / algorithmic bytes = {TC_TRAFFIC_RATIO} on a 160^3 capture "
+                          "(profiles/modeprod_tc_160cubed.md), scaled to this launch size",
         "peak_source": src, "avg_launch_ms": stage_ms["tc_kernel"] / launches,
-        "bytes_per_step": bytes_step,
+        "algorithmic_bytes_per_launch": per_launch, "bytes_per_step": bytes_step,
         "tensor": {"algorithmic_tflops": flops_step * steps / t / 1e12,
                    "mma_tflops": mma_step * steps / t / 1e12, "peak_bf16_tflops": bf16,
                    "mma_frac": mma_step * steps / t / 1e12 / bf16},
@@ -369,7 +377,7 @@ def run_gpu(args, world, rank, local):
         achieved = flops_products / (stage_ms["products"] / 1000.0) / 1e12
         roofline = {"bound": "fp64", "kernel": "modeprod_f64 (eigenbasis mode-n products)", "achieved": achieved,
                     "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s", "frac": achieved / FP64_PEAK_TFLOPS, "traffic": None,
-                    "peak_source": "FP64 FMA throughput measured on GB300",
+                    "peak_source": "nominal GB300 FP64",
                     "avg_launch_ms": stage_ms["products"] / max(stage_launches["products"], 1)}
     roofline["stage_ms_per_step"] = {k: v / 2 for k, v in stage_ms.items()}
     roofline["stage_launches_per_step"] = {k: v // 2 for k, v in stage_launches.items()}
