@@ -44,69 +44,110 @@ __host__ __device__ inline int rec_len(int F) { return 4 * F + 4; }
 template <typename T>
 __global__ void __launch_bounds__(EB) energy_partial_kernel(Phys ph, const T *__restrict__ u, const double *__restrict__ elam,
                                                             int form, double *__restrict__ part) {
+  // Per-cell arithmetic in the state's precision T: the cell terms of an FP32
+  // state carry FP32 rounding, which is unbiased and averages out over the
+  // sum; every sum (per thread, per block, over blocks) is FP64, and the
+  // volume integrals add the FP32 values exactly.
   const int n = ph.n, N = n - 4, F = ph.F, nac = ph.nac;
   const long long n3 = (long long)n * n * n, N3 = (long long)N * N * N;
-  const double hx = ph.h[0], hy = ph.h[1], hz = ph.h[2];
-  double mx[MAXF], mn[MAXF];
-  KS vol[MAXF], eac = {0, 0}, ech = {0, 0};
-  for (int f = 0; f < F; f++) {
-    mx[f] = -1.0e30;
-    mn[f] = 1.0e30;
-    vol[f].s = 0;
-    vol[f].c = 0;
+  const T i4hx = (T)(0.25 / ph.h[0]), i4hy = (T)(0.25 / ph.h[1]), i4hz = (T)(0.25 / ph.h[2]);
+  const T half_epn2 = (T)(0.5 * ph.epn2);
+  const double cshift = ph.cshift;
+  T L[4][9];
+  for (int m = 0; m < 4; m++)
+    for (int k = 0; k < 9; k++) L[m][k] = (T)elam[9 * m + k];
+  const T a2h = (T)(ph.a2 / 2.0), a4q = (T)(ph.a4 / 4.0), a6s = (T)(ph.a6 / 6.0), g = (T)ph.g, th = (T)ph.th;
+  const T Ah = (T)(ph.A / 2.0), c0e = (T)(ph.c0 - cshift), cs = (T)cshift;
+  T mx[MAXF], mn[MAXF];
+  double vsum[MAXF];
+  double eac_p = 0.0, ech_p = 0.0;
+  long long cnt = 0;
+#pragma unroll
+  for (int f = 0; f < MAXF; f++) {
+    mx[f] = (T)-1.0e30;
+    mn[f] = (T)1.0e30;
+    vsum[f] = 0.0;
   }
-  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < N3; g += (long long)gridDim.x * blockDim.x) {
-    int i = 2 + (int)(g % N), j = 2 + (int)((g / N) % N), k = 2 + (int)(g / ((long long)N * N));
-    long long l = ((long long)k * n + j) * n + i;
-    for (int f = 0; f < F; f++) {
-      double t = (double)u[f * n3 + l] + (f >= nac ? ph.cshift : 0.0);
-      mx[f] = fmax(mx[f], t);
-      mn[f] = fmin(mn[f], t);
-      ks_add(vol[f], t + 1.0);
+  for (long long gi = blockIdx.x * (long long)blockDim.x + threadIdx.x; gi < N3; gi += (long long)gridDim.x * blockDim.x) {
+    const int i = 2 + (int)(gi % N), j = 2 + (int)((gi / N) % N), k = 2 + (int)(gi / ((long long)N * N));
+    const long long l = ((long long)k * n + j) * n + i;
+    cnt++;
+#pragma unroll
+    for (int f = 0; f < MAXF; f++) {
+      if (f >= F) break;
+      const T t = u[f * n3 + l];
+      mx[f] = t > mx[f] ? t : mx[f];
+      mn[f] = t < mn[f] ? t : mn[f];
+      vsum[f] += (double)t;
     }
     if (i >= n - 3 || j >= n - 3 || k >= n - 3) continue;
-    double avg[MAXF];
-    double cbar = 0.0;
-    for (int f = 0; f < F; f++) {
+    T avg[MAXF];
+    T cbar = (T)0, e_ac = (T)0, e_ch = (T)0;
+#pragma unroll
+    for (int f = 0; f < MAXF; f++) {
+      if (f >= F) break;
       const T *q = u + f * n3;
-      double v0 = q[l], v1 = q[l + 1], v2 = q[l + n], v3 = q[l + n + 1];
-      double v4 = q[l + n * n], v5 = q[l + n * n + 1], v6 = q[l + n * n + n], v7 = q[l + n * n + n + 1];
-      avg[f] = (v0 + v1 + v2 + v3 + v4 + v5 + v6 + v7) / 8 + (f >= nac ? ph.cshift : 0.0);
-      double ux = ((v1 - v0) + (v3 - v2) + (v5 - v4) + (v7 - v6)) / 4 / hx;
-      double uy = ((v2 - v0) + (v3 - v1) + (v6 - v4) + (v7 - v5)) / 4 / hy;
-      double uz = ((v4 - v0) + (v5 - v1) + (v6 - v2) + (v7 - v3)) / 4 / hz;
+      const T v0 = q[l], v1 = q[l + 1], v2 = q[l + n], v3 = q[l + n + 1];
+      const T v4 = q[l + n * n], v5 = q[l + n * n + 1], v6 = q[l + n * n + n], v7 = q[l + n * n + n + 1];
+      avg[f] = (v0 + v1 + v2 + v3 + v4 + v5 + v6 + v7) * (T)0.125;
+      const T ux = ((v1 - v0) + (v3 - v2) + (v5 - v4) + (v7 - v6)) * i4hx;
+      const T uy = ((v2 - v0) + (v3 - v1) + (v6 - v4) + (v7 - v5)) * i4hy;
+      const T uz = ((v4 - v0) + (v5 - v1) + (v6 - v2) + (v7 - v3)) * i4hz;
       if (f < nac) {
-        const double *L = elam + 9 * f;
-        double fx = ux * L[0] + uy * L[3] + uz * L[6];
-        double fy = ux * L[1] + uy * L[4] + uz * L[7];
-        double fz = ux * L[2] + uy * L[5] + uz * L[8];
-        ks_add(eac, ph.epn2 * (fx * ux + fy * uy + fz * uz) / 2);
+        const T *Lm = L[f];
+        const T fx = ux * Lm[0] + uy * Lm[3] + uz * Lm[6];
+        const T fy = ux * Lm[1] + uy * Lm[4] + uz * Lm[7];
+        const T fz = ux * Lm[2] + uy * Lm[5] + uz * Lm[8];
+        e_ac += half_epn2 * (fx * ux + fy * uy + fz * uz);
       } else {
-        double gr = ph.epn2 * (ux * ux + uy * uy + uz * uz) / 2;
-        if (form == 0) ks_add(ech, gr); else ks_add(eac, gr);
-        cbar = avg[f];
+        const T gr = half_epn2 * (ux * ux + uy * uy + uz * uz);
+        if (form == 0) e_ch += gr; else e_ac += gr;
+        cbar = avg[f];  // relative to the stored offset
       }
     }
     if (form == 0) {
-      double e[4] = {0, 0, 0, 0};
-      for (int f = 0; f < nac && f < 4; f++) e[f] = avg[f];
-      double s2 = e[0] * e[0] + e[1] * e[1] + e[2] * e[2] + e[3] * e[3];
-      double s3 = e[0] * e[0] * e[0] + e[1] * e[1] * e[1] + e[2] * e[2] * e[2] + e[3] * e[3] * e[3];
+      T e[4] = {0, 0, 0, 0};
+#pragma unroll
+      for (int f = 0; f < 4; f++)
+        if (f < nac) e[f] = avg[f];
+      const T s2 = e[0] * e[0] + e[1] * e[1] + e[2] * e[2] + e[3] * e[3];
+      const T s3 = e[0] * e[0] * e[0] + e[1] * e[1] * e[1] + e[2] * e[2] * e[2] + e[3] * e[3] * e[3];
       if (nac > 0)
-        ks_add(eac, (2376.0 / 2372.0 / 2.0) * s2 - ((7128.0 + 12.0 * 2372.0) / 2372.0 / 3.0) * s3 +
-                        ((4752.0 + 12.0 * 2372.0) / 2372.0 / 4.0) * s2 * s2);
-      if (ph.nch > 0) ks_add(ech, (cbar * cbar - 1) * (cbar * cbar - 1) / 4);
-    } else {
-      double fl = 0.0, s2 = 0.0;
-      for (int m = 0; m < nac; m++) {
-        double u2 = avg[m] * avg[m];
-        s2 += u2;
-        fl += ph.a2 / 2.0 * u2 + ph.a4 / 4.0 * u2 * u2 + ph.a6 / 6.0 * u2 * u2 * u2;
-        for (int q = m + 1; q < nac; q++) fl += ph.g * u2 * avg[q] * avg[q];
+        e_ac += (T)(2376.0 / 2372.0 / 2.0) * s2 - (T)((7128.0 + 12.0 * 2372.0) / 2372.0 / 3.0) * s3 +
+                (T)((4752.0 + 12.0 * 2372.0) / 2372.0 / 4.0) * s2 * s2;
+      if (ph.nch > 0) {
+        const T c = cbar + cs;
+        e_ch += (c * c - (T)1) * (c * c - (T)1) * (T)0.25;
       }
-      if (ph.nch > 0) fl += ph.A / 2.0 * (cbar - ph.c0) * (cbar - ph.c0) - ph.th * (cbar - ph.c0) * s2;
-      ks_add(eac, fl);
+    } else {
+      T fl = (T)0, s2 = (T)0;
+#pragma unroll
+      for (int m = 0; m < 4; m++) {
+        if (m >= nac) break;
+        const T u2 = avg[m] * avg[m];
+        s2 += u2;
+        fl += a2h * u2 + a4q * u2 * u2 + a6s * u2 * u2 * u2;
+#pragma unroll
+        for (int q = m + 1; q < 4; q++)
+          if (q < nac) fl += g * u2 * avg[q] * avg[q];
+      }
+      if (ph.nch > 0) fl += Ah * (cbar - c0e) * (cbar - c0e) - th * (cbar - c0e) * s2;
+      e_ac += fl;
     }
+    eac_p += (double)e_ac;
+    ech_p += (double)e_ch;
+  }
+  double mxd[MAXF], mnd[MAXF];
+  KS vol[MAXF], eac = {eac_p, 0.0}, ech = {ech_p, 0.0};
+#pragma unroll
+  for (int f = 0; f < MAXF; f++) {
+    const double sh = f >= nac ? cshift : 0.0;
+    mxd[f] = (double)mx[f] + sh;
+    mnd[f] = (double)mn[f] + sh;
+    // sum of (value + 1) over this thread's cells, the constant part exact
+    vol[f].s = vsum[f];
+    vol[f].c = 0.0;
+    ks_add(vol[f], (double)cnt * (sh + 1.0));
   }
   // block reduction through shared memory
   __shared__ double sh[EB];
@@ -141,8 +182,8 @@ __global__ void __launch_bounds__(EB) energy_partial_kernel(Phys ph, const T *__
     return r;
   };
   for (int f = 0; f < F; f++) {
-    double a = reduce_max(mx[f], true);
-    double b = reduce_max(mn[f], false);
+    double a = reduce_max(mxd[f], true);
+    double b = reduce_max(mnd[f], false);
     KS v = reduce_ks(vol[f]);
     if (threadIdx.x == 0) {
       out_rec[4 * f] = a;

@@ -131,11 +131,12 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(typename Cx<T>::t *data,
       C *d = dst + line * N;
       int k = j % Ns;
       C v[5];
+      // twiddle r k N / (Ns R) < N: no reduction needed
+      const int tstep = k * (N / (Ns * R));
       for (int r = 0; r < R; r++) {
         v[r] = s[j + r * nb];
         if (r > 0 && k > 0) {
-          int idx = (int)(((long long)r * k * (N / (Ns * R))) % N);
-          C w = tw[idx];
+          C w = tw[r * tstep];
           if (sign > 0) w.y = -w.y;
           v[r] = cmul(v[r], w);
         }
@@ -159,8 +160,7 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(typename Cx<T>::t *data,
         for (int q = 0; q < R; q++) {
           C acc = v[0];
           for (int r = 1; r < R; r++) {
-            int idx = (int)(((long long)r * q * nb) % N);
-            C w = tw[idx];
+            C w = tw[((r * q) % R) * nb];
             if (sign > 0) w.y = -w.y;
             acc = cadd(acc, cmul(v[r], w));
           }

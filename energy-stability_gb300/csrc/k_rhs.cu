@@ -66,28 +66,48 @@ __device__ inline T ch_f(const P<T> &p, const T *e, T c) {
 
 __device__ inline long long L3(int n, int z, int y, int x) { return ((long long)z * n + y) * n + x; }
 
-// lambda . (central differences) at cell (z,y,x), component `comp`, with
-// values outside the block read as zero (ac_calc_F2 first loop).
-template <typename T>
-__device__ inline T grad_comp(const P<T> &p, const T *__restrict__ u, const T *lam, int z, int y, int x, int comp) {
-  int n = p.n;
-  T al = x > 0 ? u[L3(n, z, y, x - 1)] : (T)0, ar = x < n - 1 ? u[L3(n, z, y, x + 1)] : (T)0;
-  T at = y > 0 ? u[L3(n, z, y - 1, x)] : (T)0, ab = y < n - 1 ? u[L3(n, z, y + 1, x)] : (T)0;
-  T af = z > 0 ? u[L3(n, z - 1, y, x)] : (T)0, ak = z < n - 1 ? u[L3(n, z + 1, y, x)] : (T)0;
-  T gx = (ar - al) * p.i2hx, gy = (at - ab) * p.i2hy, gz = (af - ak) * p.i2hz;
-  return lam[comp * 3 + 0] * gx + lam[comp * 3 + 1] * gy + lam[comp * 3 + 2] * gz;
-}
+// One cell per thread on a 3-D launch: threadIdx.x along x (coalesced),
+// blockIdx.z = z; no index division.
+constexpr int RX = 32, RY = 8;
 
-// div of the above (ac_calc_F2 second loop).
+// Field value at offset (dz, dy, dx) from cell (z, y, x), zero outside the
+// block (ac_calc_F2 reads no ghost beyond the block).
 template <typename T>
-__device__ inline T aniso_f2(const P<T> &p, const T *__restrict__ u, const T *lam, int z, int y, int x) {
-  int n = p.n;
-  T ar = x < n - 1 ? grad_comp(p, u, lam, z, y, x + 1, 0) : (T)0;
-  T al = x > 0 ? grad_comp(p, u, lam, z, y, x - 1, 0) : (T)0;
-  T at = y > 0 ? grad_comp(p, u, lam, z, y - 1, x, 1) : (T)0;
-  T ab = y < n - 1 ? grad_comp(p, u, lam, z, y + 1, x, 1) : (T)0;
-  T af = z > 0 ? grad_comp(p, u, lam, z - 1, y, x, 2) : (T)0;
-  T ak = z < n - 1 ? grad_comp(p, u, lam, z + 1, y, x, 2) : (T)0;
+struct Nb {
+  const T *__restrict__ u;
+  int n, x, y, z;
+  __device__ T operator()(int dz, int dy, int dx) const {
+    const int xx = x + dx, yy = y + dy, zz = z + dz;
+    if (xx < 0 || xx >= n || yy < 0 || yy >= n || zz < 0 || zz >= n) return (T)0;
+    return u[((size_t)zz * n + yy) * n + xx];
+  }
+};
+
+// div(lambda grad eta) of ac_calc_F2 (anisotropic.c:164-628): the flux
+// component c at a neighbour p is lam[c] . (central differences at p), zero
+// when p is outside the block; y and z differences are (previous - next), as
+// the reference writes them.  Each of the 19 stencil values is loaded once.
+template <typename T>
+__device__ inline T aniso_f2(const P<T> &p, const Nb<T> &u, const T *lam) {
+  const int n = p.n, x = u.x, y = u.y, z = u.z;
+  const T c0 = u(0, 0, 0);
+  const T xp2 = u(0, 0, 2), xm2 = u(0, 0, -2), yp2 = u(0, 2, 0), ym2 = u(0, -2, 0), zp2 = u(2, 0, 0), zm2 = u(-2, 0, 0);
+  const T xpym = u(0, -1, 1), xpyp = u(0, 1, 1), xmym = u(0, -1, -1), xmyp = u(0, 1, -1);
+  const T xpzm = u(-1, 0, 1), xpzp = u(1, 0, 1), xmzm = u(-1, 0, -1), xmzp = u(1, 0, -1);
+  const T ymzm = u(-1, -1, 0), ymzp = u(1, -1, 0), ypzm = u(-1, 1, 0), ypzp = u(1, 1, 0);
+  const T *l0 = lam, *l1 = lam + 3, *l2 = lam + 6;
+  const T ar = x < n - 1 ? l0[0] * ((xp2 - c0) * p.i2hx) + l0[1] * ((xpym - xpyp) * p.i2hy) + l0[2] * ((xpzm - xpzp) * p.i2hz)
+                         : (T)0;
+  const T al = x > 0 ? l0[0] * ((c0 - xm2) * p.i2hx) + l0[1] * ((xmym - xmyp) * p.i2hy) + l0[2] * ((xmzm - xmzp) * p.i2hz)
+                     : (T)0;
+  const T at = y > 0 ? l1[0] * ((xpym - xmym) * p.i2hx) + l1[1] * ((ym2 - c0) * p.i2hy) + l1[2] * ((ymzm - ymzp) * p.i2hz)
+                     : (T)0;
+  const T ab = y < n - 1 ? l1[0] * ((xpyp - xmyp) * p.i2hx) + l1[1] * ((c0 - yp2) * p.i2hy) + l1[2] * ((ypzm - ypzp) * p.i2hz)
+                         : (T)0;
+  const T af = z > 0 ? l2[0] * ((xpzm - xmzm) * p.i2hx) + l2[1] * ((ymzm - ypzm) * p.i2hy) + l2[2] * ((zm2 - c0) * p.i2hz)
+                     : (T)0;
+  const T ak = z < n - 1 ? l2[0] * ((xpzp - xmzp) * p.i2hx) + l2[1] * ((ymzp - ypzp) * p.i2hy) + l2[2] * ((c0 - zp2) * p.i2hz)
+                         : (T)0;
   T t = (T)0;
   t += (ar - al) * p.i2hx;
   t += (at - ab) * p.i2hy;
@@ -96,63 +116,69 @@ __device__ inline T aniso_f2(const P<T> &p, const T *__restrict__ u, const T *la
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) rhs_ac_kernel(P<T> p, const T *__restrict__ u, const T *__restrict__ felas,
-                                                     T *__restrict__ out) {
-  int n = p.n;
-  long long n3 = (long long)n * n * n;
-  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < n3; l += (long long)gridDim.x * blockDim.x) {
-    int x = (int)(l % n), y = (int)((l / n) % n), z = (int)(l / ((long long)n * n));
-    T e[4];
-    for (int m = 0; m < p.nac; m++) e[m] = u[m * n3 + l];
-    T c = p.nch > 0 ? u[p.nac * n3 + l] : (T)0;
-    bool face = x == 0 || x == n - 1 || y == 0 || y == n - 1 || z == 0 || z == n - 1;
-    int iz = img(n, z), iy = img(n, y), ix = img(n, x), lo = img(n, -1), hi = img(n, n);
-    for (int m = 0; m < p.nac; m++) {
-      const T *um = u + m * n3;
-      T v = p.LE * p.KE * e[m];
-      v -= p.LE * ac_f(p, e, c, m);
-      if (face) {
-        T w = p.LE * p.epn2;
-        if (x == 0) v += w * um[L3(n, iz, iy, lo)] * p.ih2x;
-        if (x == n - 1) v += w * um[L3(n, iz, iy, hi)] * p.ih2x;
-        if (y == 0) v += w * um[L3(n, iz, lo, ix)] * p.ih2y;
-        if (y == n - 1) v += w * um[L3(n, iz, hi, ix)] * p.ih2y;
-        if (z == 0) v += w * um[L3(n, lo, iy, ix)] * p.ih2z;
-        if (z == n - 1) v += w * um[L3(n, hi, iy, ix)] * p.ih2z;
-      }
-      if (p.aniso) v -= p.epn2 * p.LE * aniso_f2(p, um, p.lam[m], z, y, x);
-      if (p.elastic == 1) v -= p.LE * p.es * felas[m * n3 + l];
-      out[m * n3 + l] = v;
+__global__ void __launch_bounds__(RX * RY) rhs_ac_kernel(P<T> p, const T *__restrict__ u, const T *__restrict__ felas,
+                                                         T *__restrict__ out) {
+  const int n = p.n;
+  const int x = blockIdx.x * RX + threadIdx.x, y = blockIdx.y * RY + threadIdx.y, z = blockIdx.z;
+  if (x >= n || y >= n) return;
+  const size_t n3 = (size_t)n * n * n;
+  const size_t l = ((size_t)z * n + y) * n + x;
+  T e[4] = {(T)0, (T)0, (T)0, (T)0};
+#pragma unroll
+  for (int m = 0; m < 4; m++)
+    if (m < p.nac) e[m] = u[m * n3 + l];
+  const T c = p.nch > 0 ? u[p.nac * n3 + l] : (T)0;
+  const bool face = x == 0 || x == n - 1 || y == 0 || y == n - 1 || z == 0 || z == n - 1;
+#pragma unroll
+  for (int m = 0; m < 4; m++) {
+    if (m >= p.nac) break;
+    const T *um = u + m * n3;
+    T v = p.LE * p.KE * e[m];
+    v -= p.LE * ac_f(p, e, c, m);
+    if (face) {
+      const int iz = img(n, z), iy = img(n, y), ix = img(n, x), lo = img(n, -1), hi = img(n, n);
+      const T w = p.LE * p.epn2;
+      if (x == 0) v += w * um[L3(n, iz, iy, lo)] * p.ih2x;
+      if (x == n - 1) v += w * um[L3(n, iz, iy, hi)] * p.ih2x;
+      if (y == 0) v += w * um[L3(n, iz, lo, ix)] * p.ih2y;
+      if (y == n - 1) v += w * um[L3(n, iz, hi, ix)] * p.ih2y;
+      if (z == 0) v += w * um[L3(n, lo, iy, ix)] * p.ih2z;
+      if (z == n - 1) v += w * um[L3(n, hi, iy, ix)] * p.ih2z;
     }
+    if (p.aniso) v -= p.epn2 * p.LE * aniso_f2(p, Nb<T>{um, n, x, y, z}, p.lam[m]);
+    if (p.elastic == 1) v -= p.LE * p.es * felas[m * n3 + l];
+    out[m * n3 + l] = v;
   }
 }
 
 // t = -LCI KCI c + LCI CH_f, minus the face liftings (first part of
 // ch_calc_FU_ConstantMobility).
 template <typename T>
-__global__ void __launch_bounds__(256) rhs_ch_t_kernel(P<T> p, const T *__restrict__ u, T *__restrict__ t) {
-  int n = p.n;
-  long long n3 = (long long)n * n * n;
+__global__ void __launch_bounds__(RX * RY) rhs_ch_t_kernel(P<T> p, const T *__restrict__ u, T *__restrict__ t) {
+  const int n = p.n;
+  const int x = blockIdx.x * RX + threadIdx.x, y = blockIdx.y * RY + threadIdx.y, z = blockIdx.z;
+  if (x >= n || y >= n) return;
+  const size_t n3 = (size_t)n * n * n;
+  const size_t l = ((size_t)z * n + y) * n + x;
   const T *cf = u + p.nac * n3;
-  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < n3; l += (long long)gridDim.x * blockDim.x) {
-    int x = (int)(l % n), y = (int)((l / n) % n), z = (int)(l / ((long long)n * n));
-    T e[4];
-    for (int m = 0; m < p.nac; m++) e[m] = u[m * n3 + l];
-    T c = cf[l];
-    T v = -p.LCI * p.KCI * c;
-    v += p.LCI * ch_f(p, e, c);
-    if (x == 0 || x == n - 1 || y == 0 || y == n - 1 || z == 0 || z == n - 1) {
-      int iz = img(n, z), iy = img(n, y), ix = img(n, x), lo = img(n, -1), hi = img(n, n);
-      T w = p.LCI * p.epn2;
-      if (x == 0) v -= w * cf[L3(n, iz, iy, lo)] * p.ih2x;
-      if (x == n - 1) v -= w * cf[L3(n, iz, iy, hi)] * p.ih2x;
-      if (y == 0) v -= w * cf[L3(n, iz, lo, ix)] * p.ih2y;
-      if (y == n - 1) v -= w * cf[L3(n, iz, hi, ix)] * p.ih2y;
-      if (z == 0) v -= w * cf[L3(n, lo, iy, ix)] * p.ih2z;
-      if (z == n - 1) v -= w * cf[L3(n, hi, iy, ix)] * p.ih2z;
-    }
-    t[l] = v;
+  T e[4] = {(T)0, (T)0, (T)0, (T)0};
+#pragma unroll
+  for (int m = 0; m < 4; m++)
+    if (m < p.nac) e[m] = u[m * n3 + l];
+  const T c = cf[l];
+  T v = -p.LCI * p.KCI * c;
+  v += p.LCI * ch_f(p, e, c);
+  if (x == 0 || x == n - 1 || y == 0 || y == n - 1 || z == 0 || z == n - 1) {
+    const int iz = img(n, z), iy = img(n, y), ix = img(n, x), lo = img(n, -1), hi = img(n, n);
+    const T w = p.LCI * p.epn2;
+    if (x == 0) v -= w * cf[L3(n, iz, iy, lo)] * p.ih2x;
+    if (x == n - 1) v -= w * cf[L3(n, iz, iy, hi)] * p.ih2x;
+    if (y == 0) v -= w * cf[L3(n, iz, lo, ix)] * p.ih2y;
+    if (y == n - 1) v -= w * cf[L3(n, iz, hi, ix)] * p.ih2y;
+    if (z == 0) v -= w * cf[L3(n, lo, iy, ix)] * p.ih2z;
+    if (z == n - 1) v -= w * cf[L3(n, hi, iy, ix)] * p.ih2z;
   }
+  t[l] = v;
 }
 
 // Boundary chemical potential at periodic image cell (z,y,x) (ch_mu).
@@ -172,48 +198,47 @@ __device__ inline T ch_mu_at(const P<T> &p, const T *__restrict__ u, int z, int 
   return mu;
 }
 
-// N_c = lap(t) with zero outside, minus mu(outside)/h^2 on faces.
+// N_c = lap(t) (zero outside), minus mu(outside)/h^2 on faces.
 template <typename T>
-__global__ void __launch_bounds__(256) rhs_ch_lap_kernel(P<T> p, const T *__restrict__ u, const T *__restrict__ t,
-                                                         T *__restrict__ out) {
-  int n = p.n;
-  long long n3 = (long long)n * n * n, nn = (long long)n * n;
-  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < n3; l += (long long)gridDim.x * blockDim.x) {
-    int x = (int)(l % n), y = (int)((l / n) % n), z = (int)(l / nn);
-    T tc = t[l];
-    T fl = x > 0 ? t[l - 1] : (T)0, fr = x < n - 1 ? t[l + 1] : (T)0;
-    T ft = y > 0 ? t[l - n] : (T)0, fb = y < n - 1 ? t[l + n] : (T)0;
-    T ff = z > 0 ? t[l - nn] : (T)0, fk = z < n - 1 ? t[l + nn] : (T)0;
-    T v = (fl + fr - (T)2 * tc) * p.ih2x;
-    v += (ft + fb - (T)2 * tc) * p.ih2y;
-    v += (ff + fk - (T)2 * tc) * p.ih2z;
-    if (x == 0 || x == n - 1 || y == 0 || y == n - 1 || z == 0 || z == n - 1) {
-      int iz = img(n, z), iy = img(n, y), ix = img(n, x), lo = img(n, -1), hi = img(n, n);
-      if (x == 0) v -= ch_mu_at(p, u, iz, iy, lo) * p.ih2x;
-      if (x == n - 1) v -= ch_mu_at(p, u, iz, iy, hi) * p.ih2x;
-      if (y == 0) v -= ch_mu_at(p, u, iz, lo, ix) * p.ih2y;
-      if (y == n - 1) v -= ch_mu_at(p, u, iz, hi, ix) * p.ih2y;
-      if (z == 0) v -= ch_mu_at(p, u, lo, iy, ix) * p.ih2z;
-      if (z == n - 1) v -= ch_mu_at(p, u, hi, iy, ix) * p.ih2z;
-    }
-    out[l] = v;
+__global__ void __launch_bounds__(RX * RY) rhs_ch_lap_kernel(P<T> p, const T *__restrict__ u, const T *__restrict__ t,
+                                                             T *__restrict__ out) {
+  const int n = p.n;
+  const int x = blockIdx.x * RX + threadIdx.x, y = blockIdx.y * RY + threadIdx.y, z = blockIdx.z;
+  if (x >= n || y >= n) return;
+  const size_t nn = (size_t)n * n;
+  const size_t l = (size_t)z * nn + (size_t)y * n + x;
+  const T tc = t[l];
+  const T fl = x > 0 ? t[l - 1] : (T)0, fr = x < n - 1 ? t[l + 1] : (T)0;
+  const T ft = y > 0 ? t[l - n] : (T)0, fb = y < n - 1 ? t[l + n] : (T)0;
+  const T ff = z > 0 ? t[l - nn] : (T)0, fk = z < n - 1 ? t[l + nn] : (T)0;
+  T v = (fl + fr - (T)2 * tc) * p.ih2x;
+  v += (ft + fb - (T)2 * tc) * p.ih2y;
+  v += (ff + fk - (T)2 * tc) * p.ih2z;
+  if (x == 0 || x == n - 1 || y == 0 || y == n - 1 || z == 0 || z == n - 1) {
+    const int iz = img(n, z), iy = img(n, y), ix = img(n, x), lo = img(n, -1), hi = img(n, n);
+    if (x == 0) v -= ch_mu_at(p, u, iz, iy, lo) * p.ih2x;
+    if (x == n - 1) v -= ch_mu_at(p, u, iz, iy, hi) * p.ih2x;
+    if (y == 0) v -= ch_mu_at(p, u, iz, lo, ix) * p.ih2y;
+    if (y == n - 1) v -= ch_mu_at(p, u, iz, hi, ix) * p.ih2y;
+    if (z == 0) v -= ch_mu_at(p, u, lo, iy, ix) * p.ih2z;
+    if (z == n - 1) v -= ch_mu_at(p, u, hi, iy, ix) * p.ih2z;
   }
+  out[l] = v;
 }
 
 template <typename T>
 cudaError_t launch_rhs(const Phys &ph, const T *u, const T *felas, T *out, T *scratch, cudaStream_t s) {
   P<T> p = to_p<T>(ph);
   long long n3 = (long long)ph.n * ph.n * ph.n;
-  long long blocks = (n3 + 255) / 256;
-  int g = (int)(blocks > 152LL * 32 ? 152LL * 32 : blocks);
+  const dim3 blk(RX, RY), grd((ph.n + RX - 1) / RX, (ph.n + RY - 1) / RY, ph.n);
   if (ph.nac > 0) {
-    rhs_ac_kernel<T><<<g, 256, 0, s>>>(p, u, felas, out);
+    rhs_ac_kernel<T><<<grd, blk, 0, s>>>(p, u, felas, out);
     launch_counter()++;
   }
   for (int m = 0; m < ph.nch; m++) {
     // one conserved field (the plugin's CH_f is defined for c_0 only)
-    rhs_ch_t_kernel<T><<<g, 256, 0, s>>>(p, u, scratch);
-    rhs_ch_lap_kernel<T><<<g, 256, 0, s>>>(p, u, scratch, out + (long long)ph.nac * n3);
+    rhs_ch_t_kernel<T><<<grd, blk, 0, s>>>(p, u, scratch);
+    rhs_ch_lap_kernel<T><<<grd, blk, 0, s>>>(p, u, scratch, out + (long long)ph.nac * n3);
     launch_counter() += 2;
   }
   return cudaGetLastError();
