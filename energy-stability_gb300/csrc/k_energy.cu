@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(EB) energy_partial_kernel(Phys ph, const T *__
   for (int m = 0; m < 4; m++)
     for (int k = 0; k < 9; k++) L[m][k] = (T)elam[9 * m + k];
   const T a2h = (T)(ph.a2 / 2.0), a4q = (T)(ph.a4 / 4.0), a6s = (T)(ph.a6 / 6.0), g = (T)ph.g, th = (T)ph.th;
-  const T Ah = (T)(ph.A / 2.0), c0e = (T)(ph.c0 - cshift), cs = (T)cshift;
+  const T Ah = (T)(ph.A / 2.0);
   T mx[MAXF], mn[MAXF];
   double vsum[MAXF];
   double eac_p = 0.0, ech_p = 0.0;
@@ -82,7 +82,8 @@ __global__ void __launch_bounds__(EB) energy_partial_kernel(Phys ph, const T *__
     }
     if (i >= n - 3 || j >= n - 3 || k >= n - 3) continue;
     T avg[MAXF];
-    T cbar = (T)0, e_ac = (T)0, e_ch = (T)0;
+    double cbar = 0.0;  // true concentration average, exact sum of the 8 values
+    T e_ac = (T)0, e_ch = (T)0;
 #pragma unroll
     for (int f = 0; f < MAXF; f++) {
       if (f >= F) break;
@@ -102,7 +103,8 @@ __global__ void __launch_bounds__(EB) energy_partial_kernel(Phys ph, const T *__
       } else {
         const T gr = half_epn2 * (ux * ux + uy * uy + uz * uz);
         if (form == 0) e_ch += gr; else e_ac += gr;
-        cbar = avg[f];  // relative to the stored offset
+        cbar = ((double)v0 + (double)v1 + (double)v2 + (double)v3 + (double)v4 + (double)v5 + (double)v6 + (double)v7) *
+                   0.125 + cshift;
       }
     }
     if (form == 0) {
@@ -116,7 +118,7 @@ __global__ void __launch_bounds__(EB) energy_partial_kernel(Phys ph, const T *__
         e_ac += (T)(2376.0 / 2372.0 / 2.0) * s2 - (T)((7128.0 + 12.0 * 2372.0) / 2372.0 / 3.0) * s3 +
                 (T)((4752.0 + 12.0 * 2372.0) / 2372.0 / 4.0) * s2 * s2;
       if (ph.nch > 0) {
-        const T c = cbar + cs;
+        const T c = (T)cbar;
         e_ch += (c * c - (T)1) * (c * c - (T)1) * (T)0.25;
       }
     } else {
@@ -131,7 +133,10 @@ __global__ void __launch_bounds__(EB) energy_partial_kernel(Phys ph, const T *__
         for (int q = m + 1; q < 4; q++)
           if (q < nac) fl += g * u2 * avg[q] * avg[q];
       }
-      if (ph.nch > 0) fl += Ah * (cbar - c0e) * (cbar - c0e) - th * (cbar - c0e) * s2;
+      if (ph.nch > 0) {
+        const T cd = (T)(cbar - ph.c0);
+        fl += Ah * cd * cd - th * cd * s2;
+      }
       e_ac += fl;
     }
     eac_p += (double)e_ac;
