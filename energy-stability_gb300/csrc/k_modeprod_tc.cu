@@ -30,16 +30,19 @@
 // out[t][a' * n*n + r] for input row r = c * n + b, i.e. contracted index
 // slowest: three products return to x-fastest order.
 //
-// Tile: D[128 a' x 128 r], 4 accumulators x 128 TMEM columns.  A = matrix
-// slices (128 a' rows x 32 k, 64-byte swizzle), B = input slices (128 r rows x
-// 32 k), both K-major, TMA-loaded into a three-stage mbarrier pipeline.  Warp 0
-// issues TMA, warp 1 issues MMAs (one elected thread each), warp 2 owns the
-// TMEM allocation, all four warps run the epilogue: TMEM -> registers ->
-// shared tile -> coalesced FP32 stores, with the ETD update (ac_updateU_new /
+// Kernel: persistent, one CTA per SM looping over output tiles D[128 a' x 64 r]
+// (a'-tile fastest, so the two a'-tiles of an input tile run together and its
+// slices come from HBM once).  A = matrix slices (128 a' rows x 32 k, 64-byte
+// swizzle), B = input slices (64 r rows x 32 k), both K-major, TMA-loaded into
+// a four-stage mbarrier pipeline.  Warp 0 issues TMA, warp 1 issues MMAs (one
+// elected thread each) and owns the tensor memory: two accumulator sets of
+// 4 classes x 64 columns, so the epilogue of one tile overlaps the MMAs of the
+// next.  Warps 2-5 run the epilogue (TMEM lane quadrant warp % 4): TMEM ->
+// registers -> FP32 stores, with the ETD update (ac_updateU_new /
 // ch_updateU_new, calc.c:489-535) or the phi2 scaling (prepare_U2_new,
-// calc.c:553-567) fused.  Every
-// mbarrier wait is bounded: on timeout the CTA records an error, drains its
-// copies (bounded), frees TMEM and returns.
+// calc.c:553-567) fused.  Every mbarrier wait is bounded: on timeout the CTA
+// records an error, drains its copies and MMAs (bounded), frees TMEM and
+// returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
@@ -53,16 +56,19 @@ namespace sclet {
 
 namespace tc {
 
-constexpr int BM = 128, BN = 128, BK = 32, STAGES = 3, NP = TC_PLANES, NPM = TC_PLANES_M;
+constexpr int BM = 128, BN = 64, BK = 32, STAGES = 4, NP = TC_PLANES, NPM = TC_PLANES_M;
 constexpr int PLANE_A = BM * BK * 2;  // 8 KB
-constexpr int PLANE_B = BN * BK * 2;  // 8 KB
+constexpr int PLANE_B = BN * BK * 2;  // 4 KB
 constexpr int STAGE_BYTES = NPM * PLANE_A + NP * PLANE_B;
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024;
-constexpr int NACC = 4;  // weight classes w = 0..3
-constexpr int TMEM_COLS = NACC * BN;
+constexpr int SMEM_ALIGN = 512;  // period of the 64-byte swizzle pattern
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + SMEM_ALIGN;
+constexpr int NACC = 4;               // weight classes w = 0..3
+constexpr int ACC_COLS = NACC * BN;   // one accumulator set
+constexpr int TMEM_COLS = 2 * ACC_COLS;
+constexpr int THREADS = 192;          // producer, MMA, four epilogue warps
 constexpr long long WAIT_LIMIT = 1LL << 22;  // polls (with backoff) before giving up
 static_assert(TMEM_COLS <= 512, "tensor memory holds 512 columns");
-static_assert(BM * (BN + 1) * 4 <= STAGES * STAGE_BYTES, "epilogue tile reuses the stage buffers");
+static_assert(SMEM_BYTES <= 227 * 1024, "shared memory per CTA");
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -144,31 +150,56 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
   for (int j = 0; j < 32; j++) v[j] = __uint_as_float(r[j]);
 }
 
-__global__ void __launch_bounds__(128, 1)
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+struct TileIdx {
+  int a_tile, r_tile, t;
+};
+__device__ __forceinline__ TileIdx tile_of(int tau, int a_tiles, int r_tiles) {
+  TileIdx x;
+  x.a_tile = tau % a_tiles;
+  const int rest = tau / a_tiles;
+  x.r_tile = rest % r_tiles;
+  x.t = rest / r_tiles;
+  return x;
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
     modeprod_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcArgs g) {
   extern __shared__ uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t full_bar[STAGES];
   __shared__ __align__(8) uint64_t empty_bar[STAGES];
-  __shared__ __align__(8) uint64_t acc_bar;
+  __shared__ __align__(8) uint64_t tfull_bar[2];   // accumulator set ready (MMA -> epilogue)
+  __shared__ __align__(8) uint64_t tempty_bar[2];  // accumulator set drained (epilogue -> MMA)
+  __shared__ __align__(8) uint64_t done_bar;       // every MMA of this CTA completed
   __shared__ uint32_t tmem_slot;
   __shared__ int failed;
 
-  uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + SMEM_ALIGN - 1) & ~(uintptr_t)(SMEM_ALIGN - 1));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int r_tile = blockIdx.x, a_tile = blockIdx.y, t = blockIdx.z;
   const long long rows = (long long)g.n * g.n;
+  const int a_tiles = (g.n + BM - 1) / BM;
+  const int r_tiles = (int)((rows + BN - 1) / BN);
+  const int total = a_tiles * r_tiles * g.count;
+  const int nkb = g.kblocks;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; s++) {
       mbar_init(&full_bar[s], 1);
       mbar_init(&empty_bar[s], 1);
     }
-    mbar_init(&acc_bar, 1);
+    for (int b = 0; b < 2; b++) {
+      mbar_init(&tfull_bar[b], 1);
+      mbar_init(&tempty_bar[b], 4);  // one arrival per epilogue warp
+    }
+    mbar_init(&done_bar, 1);
     failed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
-  if (warp == 2) {
+  if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
                  "r"(TMEM_COLS)
                  : "memory");
@@ -178,126 +209,194 @@ __global__ void __launch_bounds__(128, 1)
   __syncthreads();
   fence_after();
   const uint32_t tmem = tmem_slot;
-  const int nkb = g.kblocks;
 
-  if (warp == 0 && lane == 0) {
-    // producer: five A slices and four B slices per stage
-    int issued = 0;
-    for (int kb = 0; kb < nkb; kb++) {
-      const int s = kb % STAGES;
-      if (kb >= STAGES && !mbar_wait(&empty_bar[s], ((kb / STAGES) & 1) ^ 1)) {
-        failed = 1;
-        break;
-      }
-      if (*(volatile int *)&failed) break;
-      uint8_t *st = base + s * STAGE_BYTES;
-      mbar_expect_tx(&full_bar[s], STAGE_BYTES);
-      for (int p = 0; p < NPM; p++) tma_load_3d(st + p * PLANE_A, &tmA, kb * BK, a_tile * BM, p, &full_bar[s]);
-      for (int p = 0; p < NP; p++)
-        tma_load_3d(st + NPM * PLANE_A + p * PLANE_B, &tmB, kb * BK, r_tile * BN, t * NP + p, &full_bar[s]);
-      issued = kb + 1;
-    }
-    if (*(volatile int *)&failed) {
-      // drain: wait (bounded) for copies still in flight into this CTA
-      for (int kb = issued - STAGES < 0 ? 0 : issued - STAGES; kb < issued; kb++)
-        mbar_wait(&full_bar[kb % STAGES], (kb / STAGES) & 1);
-    }
-  } else if (warp == 1 && lane == 0) {
-    // MMA issuer: 2 k-steps of 16 per stage, eleven terms each; (matrix
-    // slice, input slice, class) grouped by class, small classes first; the
-    // first term of each class at the first k-step starts its accumulator
-    const uint32_t idesc = idesc_bf16(BM, BN);
-    const int pairA[11] = {4, 0, 1, 2, 3, 0, 1, 2, 0, 1, 0};
-    const int pairB[11] = {0, 3, 2, 1, 0, 2, 1, 0, 1, 0, 0};
-    const int cls[11] = {3, 3, 3, 3, 3, 2, 2, 2, 1, 1, 0};
-    for (int kb = 0; kb < nkb; kb++) {
-      const int s = kb % STAGES;
-      if (!mbar_wait(&full_bar[s], (kb / STAGES) & 1)) {
-        failed = 1;
-        break;
-      }
-      fence_after();
-      const uint32_t sa = smem_u32(base + s * STAGE_BYTES);
-      const uint32_t sb = sa + NPM * PLANE_A;
-#pragma unroll
-      for (int ks = 0; ks < BK / 16; ks++) {
-        const uint32_t koff = ks * 32;
-        const bool first = (kb == 0 && ks == 0);
-#pragma unroll
-        for (int q = 0; q < 11; q++) {
-          const int pa = pairA[q], pb = pairB[q], w = cls[q];
-          const bool start = first && (q == 0 || q == 5 || q == 8 || q == 10);
-          uint64_t da = smem_desc(sa + pa * PLANE_A + koff);
-          uint64_t db = smem_desc(sb + pb * PLANE_B + koff);
-          mma_bf16(tmem + (uint32_t)(w * BN), da, db, idesc, start ? 0u : 1u);
+  if (warp == 0) {
+    if (lane == 0) {
+      // producer: five A slices and four B slices per stage, k-blocks of all
+      // this CTA's tiles in one stream
+      int it = 0;
+      for (int tau = blockIdx.x; tau < total; tau += gridDim.x) {
+        const TileIdx ti = tile_of(tau, a_tiles, r_tiles);
+        for (int kb = 0; kb < nkb; kb++, it++) {
+          const int s = it % STAGES;
+          if (it >= STAGES && !mbar_wait(&empty_bar[s], ((it / STAGES) & 1) ^ 1)) {
+            failed = 1;
+            break;
+          }
+          if (*(volatile int *)&failed) break;
+          uint8_t *st = base + s * STAGE_BYTES;
+          mbar_expect_tx(&full_bar[s], STAGE_BYTES);
+          for (int p = 0; p < NPM; p++) tma_load_3d(st + p * PLANE_A, &tmA, kb * BK, ti.a_tile * BM, p, &full_bar[s]);
+          for (int p = 0; p < NP; p++)
+            tma_load_3d(st + NPM * PLANE_A + p * PLANE_B, &tmB, kb * BK, ti.r_tile * BN, ti.t * NP + p, &full_bar[s]);
         }
+        if (*(volatile int *)&failed) break;
       }
-      mma_commit(&empty_bar[s]);
+      if (*(volatile int *)&failed) {
+        // drain: wait (bounded) for copies still in flight into this CTA
+        for (int i = it - STAGES < 0 ? 0 : it - STAGES; i < it; i++) mbar_wait(&full_bar[i % STAGES], (i / STAGES) & 1);
+      }
     }
-    mma_commit(&acc_bar);
-  }
-  __syncwarp();
-
-  // ---- epilogue ---------------------------------------------------------
-  bool ok = mbar_wait(&acc_bar, 0);
-  if (!ok) failed = 1;
-  fence_after();
-  float *tile = reinterpret_cast<float *>(base);  // [128][BN + 1] after the mainloop
-  constexpr int TS = BN + 1;
-  __syncthreads();
-  if (!failed) {
-    const int row = warp * 32 + lane;
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // MMA issuer: 2 k-steps of 16 per stage, eleven terms each; (matrix
+      // slice, input slice, class) grouped by class, small classes first; the
+      // first term of each class at a tile's first k-step starts its accumulator
+      const uint32_t idesc = idesc_bf16(BM, BN);
+      const int pairA[11] = {4, 0, 1, 2, 3, 0, 1, 2, 0, 1, 0};
+      const int pairB[11] = {0, 3, 2, 1, 0, 2, 1, 0, 1, 0, 0};
+      const int cls[11] = {3, 3, 3, 3, 3, 2, 2, 2, 1, 1, 0};
+      int it = 0, j = 0;
+      for (int tau = blockIdx.x; tau < total && !*(volatile int *)&failed; tau += gridDim.x, j++) {
+        const int b = j & 1;
+        // accumulator set b was last used by tile j - 2
+        if (j >= 2 && !mbar_wait(&tempty_bar[b], ((j >> 1) & 1) ^ 1)) {
+          failed = 1;
+          break;
+        }
+        fence_after();
+        const uint32_t acc = tmem + (uint32_t)(b * ACC_COLS);
+        bool ok = true;
+        for (int kb = 0; kb < nkb; kb++, it++) {
+          const int s = it % STAGES;
+          if (!mbar_wait(&full_bar[s], (it / STAGES) & 1)) {
+            ok = false;
+            break;
+          }
+          fence_after();
+          const uint32_t sa = smem_u32(base + s * STAGE_BYTES);
+          const uint32_t sb = sa + NPM * PLANE_A;
+#pragma unroll
+          for (int ks = 0; ks < BK / 16; ks++) {
+            const uint32_t koff = ks * 32;
+            const bool first = (kb == 0 && ks == 0);
+#pragma unroll
+            for (int q = 0; q < 11; q++) {
+              const int pa = pairA[q], pb = pairB[q], w = cls[q];
+              const bool start = first && (q == 0 || q == 5 || q == 8 || q == 10);
+              uint64_t da = smem_desc(sa + pa * PLANE_A + koff);
+              uint64_t db = smem_desc(sb + pb * PLANE_B + koff);
+              mma_bf16(acc + (uint32_t)(w * BN), da, db, idesc, start ? 0u : 1u);
+            }
+          }
+          mma_commit(&empty_bar[s]);
+        }
+        if (!ok) {
+          failed = 1;
+          break;
+        }
+        mma_commit(&tfull_bar[b]);
+      }
+      // every MMA issued so far must complete before the memory is freed
+      mma_commit(&done_bar);
+      if (!mbar_wait(&done_bar, 0)) failed = 1;
+    }
+  } else {
+    // epilogue warps 2-5: TMEM lane quadrant q = warp % 4 holds a' rows q*32..
+    const int q = warp & 3;
+    const int row = q * 32 + lane;
     // class weights 2^-b(w+2); exact integers combined small to large
     const float wt[NACC] = {ldexpf(1.0f, -2 * g.bits), ldexpf(1.0f, -3 * g.bits), ldexpf(1.0f, -4 * g.bits),
                             ldexpf(1.0f, -5 * g.bits)};
-#pragma unroll 1
-    for (int c = 0; c < BN / 32; c++) {
-      float v[32], w[32];
-      const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32);
-      tmem_ld32(ta + 3 * BN, v);
-#pragma unroll
-      for (int j = 0; j < 32; j++) v[j] *= wt[3];
-#pragma unroll
-      for (int k = 2; k >= 0; k--) {
-        tmem_ld32(ta + k * BN, w);
-#pragma unroll
-        for (int j = 0; j < 32; j++) v[j] = fmaf(w[j], wt[k], v[j]);
+    const bool vec = (rows & 3) == 0;
+    int j = 0;
+    for (int tau = blockIdx.x; tau < total; tau += gridDim.x, j++) {
+      const int b = j & 1;
+      // one lane waits, the warp follows its verdict (tcgen05.ld below needs
+      // the whole warp converged)
+      int ok = 1;
+      if (lane == 0) ok = mbar_wait(&tfull_bar[b], (j >> 1) & 1) ? 1 : 0;
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) {
+        if (lane == 0) failed = 1;
+        break;
       }
-#pragma unroll
-      for (int j = 0; j < 32; j++) tile[row * TS + c * 32 + j] = v[j];
-    }
-  }
-  fence_before();
-  __syncthreads();
-  if (!failed) {
-    const int col = threadIdx.x;
-    const long long r = (long long)r_tile * BN + col;
-    const int kind = (t % g.F) >= g.nac ? 1 : 0;
-    if (r < rows) {
-      const float sin_r = g.in_scale[(long long)t * rows + r];
-      const long long tb = (long long)t * g.n * rows;
+      fence_after();
+      const TileIdx ti = tile_of(tau, a_tiles, r_tiles);
+      const int a = ti.a_tile * BM + row;
+      const int kind = (ti.t % g.F) >= g.nac ? 1 : 0;
+      const long long tb = (long long)ti.t * g.n * rows;
+      const float sa = a < g.n ? g.row_scale[a] : 0.0f;
+      const float *isc = g.in_scale + (long long)ti.t * rows;
 #pragma unroll 1
-      for (int rr = 0; rr < BM; rr++) {
-        const int a = a_tile * BM + rr;
-        if (a >= g.n) break;
-        float v = tile[rr * TS + col] * (sin_r * g.row_scale[a]);
-        const long long o = (long long)a * rows + r;  // = eigen-mode [k][j][i] of a z-contraction
-        if (g.epi == 1) {
-          const float uh = g.aux[tb + o];
-          const float4 c = g.coef[kind][o];  // (e_hi, e_lo, phi1_hi, phi1_lo)
-          v = fmaf(c.x, uh, fmaf(c.y, uh, fmaf(c.z, v, c.w * v)));
-        } else if (g.epi == 2) {
-          const float2 c = g.coef2[kind][o];  // (phi2_hi, phi2_lo)
-          v = fmaf(c.x, v, c.y * v);
+      for (int c = 0; c < BN / 32; c++) {
+        __syncwarp();
+        float v[32], w[32];
+        const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * ACC_COLS + c * 32);
+        tmem_ld32(ta + 3 * BN, v);
+#pragma unroll
+        for (int jj = 0; jj < 32; jj++) v[jj] *= wt[3];
+#pragma unroll
+        for (int k = 2; k >= 0; k--) {
+          tmem_ld32(ta + k * BN, w);
+#pragma unroll
+          for (int jj = 0; jj < 32; jj++) v[jj] = fmaf(w[jj], wt[k], v[jj]);
         }
-        if (g.outmode == 1) g.out[tb + o] = v;
-        else g.out[tb + o] += v;
+        if (a < g.n) {
+        const long long r0 = (long long)ti.r_tile * BN + c * 32;
+        const long long o0 = (long long)a * rows + r0;  // eigen-mode [k][j][i] of a z-contraction
+        if (vec && r0 + 32 <= rows) {
+#pragma unroll
+          for (int jj = 0; jj < 32; jj += 4) {
+            const float4 si = *reinterpret_cast<const float4 *>(isc + r0 + jj);
+            float4 y = make_float4(v[jj] * (si.x * sa), v[jj + 1] * (si.y * sa), v[jj + 2] * (si.z * sa),
+                                   v[jj + 3] * (si.w * sa));
+            const long long o = o0 + jj;
+            if (g.epi == 1) {
+              const float4 uh = *reinterpret_cast<const float4 *>(g.aux + tb + o);
+              const float4 c0 = g.coef[kind][o], c1 = g.coef[kind][o + 1], c2 = g.coef[kind][o + 2],
+                           c3 = g.coef[kind][o + 3];  // (e_hi, e_lo, phi1_hi, phi1_lo)
+              y.x = fmaf(c0.x, uh.x, fmaf(c0.y, uh.x, fmaf(c0.z, y.x, c0.w * y.x)));
+              y.y = fmaf(c1.x, uh.y, fmaf(c1.y, uh.y, fmaf(c1.z, y.y, c1.w * y.y)));
+              y.z = fmaf(c2.x, uh.z, fmaf(c2.y, uh.z, fmaf(c2.z, y.z, c2.w * y.z)));
+              y.w = fmaf(c3.x, uh.w, fmaf(c3.y, uh.w, fmaf(c3.z, y.w, c3.w * y.w)));
+            } else if (g.epi == 2) {
+              const float2 c0 = g.coef2[kind][o], c1 = g.coef2[kind][o + 1], c2 = g.coef2[kind][o + 2],
+                           c3 = g.coef2[kind][o + 3];  // (phi2_hi, phi2_lo)
+              y.x = fmaf(c0.x, y.x, c0.y * y.x);
+              y.y = fmaf(c1.x, y.y, c1.y * y.y);
+              y.z = fmaf(c2.x, y.z, c2.y * y.z);
+              y.w = fmaf(c3.x, y.w, c3.y * y.w);
+            }
+            float4 *dst = reinterpret_cast<float4 *>(g.out + tb + o);
+            if (g.outmode == 2) {
+              const float4 old = *dst;
+              y.x += old.x;
+              y.y += old.y;
+              y.z += old.z;
+              y.w += old.w;
+            }
+            *dst = y;
+          }
+        } else {
+          for (int jj = 0; jj < 32; jj++) {
+            const long long r = r0 + jj;
+            if (r >= rows) break;
+            float y = v[jj] * (isc[r] * sa);
+            const long long o = o0 + jj;
+            if (g.epi == 1) {
+              const float uh = g.aux[tb + o];
+              const float4 cc = g.coef[kind][o];
+              y = fmaf(cc.x, uh, fmaf(cc.y, uh, fmaf(cc.z, y, cc.w * y)));
+            } else if (g.epi == 2) {
+              const float2 cc = g.coef2[kind][o];
+              y = fmaf(cc.x, y, cc.y * y);
+            }
+            if (g.outmode == 1) g.out[tb + o] = y;
+            else g.out[tb + o] += y;
+          }
+        }
+        }  // a < n
       }
+      fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&tempty_bar[b]);
+      if (__any_sync(0xffffffffu, *(volatile int *)&failed != 0)) break;
     }
   }
   __syncthreads();
   if (threadIdx.x == 0 && failed) atomicExch(g.err, 1);
-  if (warp == 2) {
+  if (warp == 1) {
     fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
   }
@@ -493,6 +592,9 @@ cudaError_t launch_modeprod_tc(const __nv_bfloat16 *mat, const __nv_bfloat16 *pl
     cudaError_t e = cudaFuncSetAttribute(tc::modeprod_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          tc::SMEM_BYTES);
     if (e != cudaSuccess) return e;
+    // all of the unified L1/shared capacity as shared memory: two CTAs per SM
+    e = cudaFuncSetAttribute(tc::modeprod_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (e != cudaSuccess) return e;
     attr = true;
   }
   const int n = args.n, kp = tc_kp(n);
@@ -506,9 +608,12 @@ cudaError_t launch_modeprod_tc(const __nv_bfloat16 *mat, const __nv_bfloat16 *pl
   g.kp = kp;
   g.kblocks = (n + tc::BK - 1) / tc::BK;
   g.bits = bits;
-  dim3 grid((unsigned)(((long long)n * n + tc::BN - 1) / tc::BN), (unsigned)((n + tc::BM - 1) / tc::BM),
-            (unsigned)count);
-  tc::modeprod_tc_kernel<<<grid, 128, tc::SMEM_BYTES, s>>>(ma, mb, g);
+  static int sms = 0;
+  if (!sms && (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0)) != cudaSuccess) return e;
+  const long long tiles = (long long)((n + tc::BM - 1) / tc::BM) * (((long long)n * n + tc::BN - 1) / tc::BN) * count;
+  if (tiles > 0x7fffffffLL) return cudaErrorInvalidValue;
+  const int grid = (int)(tiles < sms ? tiles : sms);
+  tc::modeprod_tc_kernel<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(ma, mb, g);
   launch_counter()++;
   return cudaGetLastError();
 }
