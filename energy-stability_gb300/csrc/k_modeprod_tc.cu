@@ -30,19 +30,21 @@
 // out[t][a' * n*n + r] for input row r = c * n + b, i.e. contracted index
 // slowest: three products return to x-fastest order.
 //
-// Kernel: persistent, one CTA per SM looping over output tiles D[128 a' x 64 r]
+// Kernel: persistent, one CTA per SM looping over output tiles D[128 a' x 128 r]
 // (a'-tile fastest, so the two a'-tiles of an input tile run together and its
 // slices come from HBM once).  A = matrix slices (128 a' rows x 32 k, 64-byte
-// swizzle), B = input slices (64 r rows x 32 k), both K-major, TMA-loaded into
-// a four-stage mbarrier pipeline.  Warp 0 issues TMA, warp 1 issues MMAs (one
-// elected thread each) and owns the tensor memory: two accumulator sets of
-// 4 classes x 64 columns, so the epilogue of one tile overlaps the MMAs of the
-// next.  Warps 2-5 run the epilogue (TMEM lane quadrant warp % 4): TMEM ->
-// registers -> FP32 stores, with the ETD update (ac_updateU_new /
-// ch_updateU_new, calc.c:489-535) or the phi2 scaling (prepare_U2_new,
-// calc.c:553-567) fused.  Every mbarrier wait is bounded: on timeout the CTA
-// records an error, drains its copies and MMAs (bounded), frees TMEM and
-// returns.
+// swizzle), B = input slices (128 r rows x 32 k), both K-major, TMA-loaded into
+// a three-stage mbarrier pipeline that runs ahead across tiles.  Warp 0 issues
+// TMA, warp 1 issues MMAs (one elected thread each) and owns the tensor memory
+// (4 classes x 128 columns; with narrower tiles, two sets alternate).  Warps
+// 2-5 run the epilogue (TMEM lane quadrant warp % 4): TMEM -> registers ->
+// FP32 stores, with the ETD update (ac_updateU_new / ch_updateU_new,
+// calc.c:489-535) or the phi2 scaling (prepare_U2_new, calc.c:553-567) fused,
+// while the next tile's copies proceed.  The operand planes per MMA set the
+// pace (nine 8 KB planes per k-block): 128-wide tiles halve the matrix-slice
+// traffic per output against 64-wide ones.  Every mbarrier wait is bounded: on
+// timeout the CTA records an error, drains its copies and MMAs (bounded),
+// frees TMEM and returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
@@ -56,15 +58,16 @@ namespace sclet {
 
 namespace tc {
 
-constexpr int BM = 128, BN = 64, BK = 32, STAGES = 4, NP = TC_PLANES, NPM = TC_PLANES_M;
+constexpr int BM = 128, BN = 128, BK = 32, STAGES = 3, NP = TC_PLANES, NPM = TC_PLANES_M;
 constexpr int PLANE_A = BM * BK * 2;  // 8 KB
-constexpr int PLANE_B = BN * BK * 2;  // 4 KB
+constexpr int PLANE_B = BN * BK * 2;  // 8 KB
 constexpr int STAGE_BYTES = NPM * PLANE_A + NP * PLANE_B;
 constexpr int SMEM_ALIGN = 512;  // period of the 64-byte swizzle pattern
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + SMEM_ALIGN;
 constexpr int NACC = 4;               // weight classes w = 0..3
 constexpr int ACC_COLS = NACC * BN;   // one accumulator set
-constexpr int TMEM_COLS = 2 * ACC_COLS;
+constexpr int NBUF = 512 / ACC_COLS;   // accumulator sets in tensor memory (1 or 2)
+constexpr int TMEM_COLS = NBUF * ACC_COLS;
 constexpr int THREADS = 192;          // producer, MMA, four epilogue warps
 constexpr long long WAIT_LIMIT = 1LL << 22;  // polls (with backoff) before giving up
 static_assert(TMEM_COLS <= 512, "tensor memory holds 512 columns");
@@ -171,8 +174,8 @@ __global__ void __launch_bounds__(THREADS, 1)
   extern __shared__ uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t full_bar[STAGES];
   __shared__ __align__(8) uint64_t empty_bar[STAGES];
-  __shared__ __align__(8) uint64_t tfull_bar[2];   // accumulator set ready (MMA -> epilogue)
-  __shared__ __align__(8) uint64_t tempty_bar[2];  // accumulator set drained (epilogue -> MMA)
+  __shared__ __align__(8) uint64_t tfull_bar[NBUF];   // accumulator set ready (MMA -> epilogue)
+  __shared__ __align__(8) uint64_t tempty_bar[NBUF];  // accumulator set drained (epilogue -> MMA)
   __shared__ __align__(8) uint64_t done_bar;       // every MMA of this CTA completed
   __shared__ uint32_t tmem_slot;
   __shared__ int failed;
@@ -190,7 +193,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       mbar_init(&full_bar[s], 1);
       mbar_init(&empty_bar[s], 1);
     }
-    for (int b = 0; b < 2; b++) {
+    for (int b = 0; b < NBUF; b++) {
       mbar_init(&tfull_bar[b], 1);
       mbar_init(&tempty_bar[b], 4);  // one arrival per epilogue warp
     }
@@ -248,9 +251,9 @@ __global__ void __launch_bounds__(THREADS, 1)
       const int cls[11] = {3, 3, 3, 3, 3, 2, 2, 2, 1, 1, 0};
       int it = 0, j = 0;
       for (int tau = blockIdx.x; tau < total && !*(volatile int *)&failed; tau += gridDim.x, j++) {
-        const int b = j & 1;
-        // accumulator set b was last used by tile j - 2
-        if (j >= 2 && !mbar_wait(&tempty_bar[b], ((j >> 1) & 1) ^ 1)) {
+        const int b = j % NBUF;
+        // accumulator set b was last used by tile j - NBUF
+        if (j >= NBUF && !mbar_wait(&tempty_bar[b], ((j / NBUF) & 1) ^ 1)) {
           failed = 1;
           break;
         }
@@ -301,11 +304,11 @@ __global__ void __launch_bounds__(THREADS, 1)
     const bool vec = (rows & 3) == 0;
     int j = 0;
     for (int tau = blockIdx.x; tau < total; tau += gridDim.x, j++) {
-      const int b = j & 1;
+      const int b = j % NBUF;
       // one lane waits, the warp follows its verdict (tcgen05.ld below needs
       // the whole warp converged)
       int ok = 1;
-      if (lane == 0) ok = mbar_wait(&tfull_bar[b], (j >> 1) & 1) ? 1 : 0;
+      if (lane == 0) ok = mbar_wait(&tfull_bar[b], (j / NBUF) & 1) ? 1 : 0;
       ok = __shfl_sync(0xffffffffu, ok, 0);
       if (!ok) {
         if (lane == 0) failed = 1;
