@@ -80,44 +80,107 @@ static Radices factor(int n) {
   return f;
 }
 
-// One batch of line FFTs.  axis 0: lines along x (contiguous); 1: along y;
-// 2: along z.  sign -1 forward, +1 backward (unscaled).  tw[j] = exp(-2 pi i j / N).
+// One batch of line FFTs over one or two grids (blockIdx.y selects data0 /
+// data1).  axis 0: lines along x (contiguous); 1: along y; 2: along z.  sign
+// -1 forward, +1 backward (unscaled).  tw[j] = exp(-2 pi i j / N).  A CTA
+// keeps 2^ltile lines in shared memory; element-to-line maps use shifts, and
+// the per-stage quotients use a float reciprocal, exact for these ranges (a
+// quotient's fractional part stays >= 0.5 / divisor away from the next
+// integer, far above float rounding at operands below 2^16).
+struct StageDiv {
+  float inv_nb[16], inv_ns[16];
+};
+
+__device__ __forceinline__ int fdiv(int e, float inv) { return __float2int_rd(((float)e + 0.5f) * inv); }
+
+// One Stockham stage of radix R over all lines of the tile (src -> dst).
+template <int R, typename C>
+__device__ __forceinline__ void fft_stage(const C *__restrict__ src, C *__restrict__ dst, int tile, int N, int Ns,
+                                          float inv_nb, float inv_ns, const C *__restrict__ tw, int sign) {
+  const int nb = N / R;
+  for (int e = threadIdx.x; e < tile * nb; e += blockDim.x) {
+    const int line = fdiv(e, inv_nb), j = e - line * nb;
+    const int jq = fdiv(j, inv_ns), k = j - jq * Ns;
+    const C *s = src + line * N;
+    C *d = dst + line * N;
+    C v[R];
+    // twiddle r k N / (Ns R) < N: no reduction needed
+    const int tstep = k * (N / (Ns * R));
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      v[r] = s[j + r * nb];
+      if (r > 0 && k > 0) {
+        C w = tw[r * tstep];
+        if (sign > 0) w.y = -w.y;
+        v[r] = cmul(v[r], w);
+      }
+    }
+    C o[R];
+    if (R == 2) {
+      o[0] = cadd(v[0], v[1]);
+      o[1] = csub(v[0], v[1]);
+    } else if (R == 4) {
+      C a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
+      C c = cadd(v[1], v[3 % R]), d2 = csub(v[1], v[3 % R]);
+      // multiply d2 by -i (forward) or +i (backward)
+      C dj;
+      if (sign < 0) { dj.x = d2.y; dj.y = -d2.x; }
+      else { dj.x = -d2.y; dj.y = d2.x; }
+      o[0] = cadd(a, c);
+      o[2 % R] = csub(a, c);
+      o[1] = cadd(b, dj);
+      o[3 % R] = csub(b, dj);
+    } else {
+#pragma unroll
+      for (int q = 0; q < R; q++) {
+        C acc = v[0];
+#pragma unroll
+        for (int r = 1; r < R; r++) {
+          C w = tw[((r * q) % R) * nb];
+          if (sign > 0) w.y = -w.y;
+          acc = cadd(acc, cmul(v[r], w));
+        }
+        o[q] = acc;
+      }
+    }
+    const int idxD = jq * Ns * R + k;
+#pragma unroll
+    for (int r = 0; r < R; r++) d[idxD + r * Ns] = o[r];
+  }
+}
+
 template <typename T>
-__global__ void __launch_bounds__(256) fft_lines_kernel(typename Cx<T>::t *data, int N, int axis, int tile,
-                                                        const typename Cx<T>::t *__restrict__ tw, int sign,
-                                                        Radices rad) {
+__global__ void __launch_bounds__(256) fft_lines_kernel(typename Cx<T>::t *data0, typename Cx<T>::t *data1, int N,
+                                                        int axis, int ltile, const typename Cx<T>::t *__restrict__ tw,
+                                                        int sign, Radices rad, StageDiv sd) {
   typedef typename Cx<T>::t C;
   extern __shared__ unsigned char smem_raw[];
+  const int tile = 1 << ltile;
   C *buf0 = reinterpret_cast<C *>(smem_raw);
   C *buf1 = buf0 + (size_t)tile * N;
+  C *data = blockIdx.y == 0 ? data0 : data1;
   const long long NN = (long long)N * N;
   // Line set of this CTA
-  long long base;
-  long long stride, lstride;
+  long long base, stride, lstride;
   if (axis == 0) {
-    long long line0 = (long long)blockIdx.x * tile;  // lines indexed by (z*N + y)
-    base = line0 * N;
+    base = (long long)blockIdx.x * tile * N;  // lines indexed by (z*N + y)
     stride = 1;
     lstride = N;
-  } else if (axis == 1) {
-    int xt = blockIdx.x % (N / tile);
-    int z = blockIdx.x / (N / tile);
-    base = (long long)z * NN + (long long)xt * tile;
-    stride = N;
-    lstride = 1;
   } else {
-    int xt = blockIdx.x % (N / tile);
-    int y = blockIdx.x / (N / tile);
-    base = (long long)y * N + (long long)xt * tile;
-    stride = NN;
+    const int ntx = N >> ltile;
+    const int xt = blockIdx.x % ntx, w = blockIdx.x / ntx;  // w = z (axis 1) or y (axis 2)
+    base = (axis == 1 ? (long long)w * NN : (long long)w * N) + (long long)xt * tile;
+    stride = axis == 1 ? N : NN;
     lstride = 1;
   }
   const int total = tile * N;
-  for (int e = threadIdx.x; e < total; e += blockDim.x) {
-    int line, pos;
-    if (axis == 0) { line = e / N; pos = e % N; }
-    else { line = e % tile; pos = e / tile; }
-    buf0[line * N + pos] = data[base + line * lstride + pos * stride];
+  if (axis == 0) {
+    for (int e = threadIdx.x; e < total; e += blockDim.x) buf0[e] = data[base + e];
+  } else {
+    for (int e = threadIdx.x; e < total; e += blockDim.x) {
+      const int line = e & (tile - 1), pos = e >> ltile;
+      buf0[line * N + pos] = data[base + line * lstride + (long long)pos * stride];
+    }
   }
   __syncthreads();
   C *src = buf0, *dst = buf1;
@@ -125,50 +188,12 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(typename Cx<T>::t *data,
   for (int st = 0; st < rad.count; st++) {
     const int R = rad.r[st];
     const int nb = N / R;
-    for (int e = threadIdx.x; e < tile * nb; e += blockDim.x) {
-      int line = e / nb, j = e % nb;
-      const C *s = src + line * N;
-      C *d = dst + line * N;
-      int k = j % Ns;
-      C v[5];
-      // twiddle r k N / (Ns R) < N: no reduction needed
-      const int tstep = k * (N / (Ns * R));
-      for (int r = 0; r < R; r++) {
-        v[r] = s[j + r * nb];
-        if (r > 0 && k > 0) {
-          C w = tw[r * tstep];
-          if (sign > 0) w.y = -w.y;
-          v[r] = cmul(v[r], w);
-        }
-      }
-      C o[5];
-      if (R == 2) {
-        o[0] = cadd(v[0], v[1]);
-        o[1] = csub(v[0], v[1]);
-      } else if (R == 4) {
-        C a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
-        C c = cadd(v[1], v[3]), d2 = csub(v[1], v[3]);
-        // multiply d2 by -i (forward) or +i (backward)
-        C dj;
-        if (sign < 0) { dj.x = d2.y; dj.y = -d2.x; }
-        else { dj.x = -d2.y; dj.y = d2.x; }
-        o[0] = cadd(a, c);
-        o[2] = csub(a, c);
-        o[1] = cadd(b, dj);
-        o[3] = csub(b, dj);
-      } else {
-        for (int q = 0; q < R; q++) {
-          C acc = v[0];
-          for (int r = 1; r < R; r++) {
-            C w = tw[((r * q) % R) * nb];
-            if (sign > 0) w.y = -w.y;
-            acc = cadd(acc, cmul(v[r], w));
-          }
-          o[q] = acc;
-        }
-      }
-      int idxD = (j / Ns) * Ns * R + k;
-      for (int r = 0; r < R; r++) d[idxD + r * Ns] = o[r];
+    const float inb = sd.inv_nb[st], ins = sd.inv_ns[st];
+    switch (R) {
+      case 4: fft_stage<4, C>(src, dst, tile, N, Ns, inb, ins, tw, sign); break;
+      case 2: fft_stage<2, C>(src, dst, tile, N, Ns, inb, ins, tw, sign); break;
+      case 3: fft_stage<3, C>(src, dst, tile, N, Ns, inb, ins, tw, sign); break;
+      default: fft_stage<5, C>(src, dst, tile, N, Ns, inb, ins, tw, sign); break;
     }
     __syncthreads();
     C *t = src;
@@ -176,11 +201,13 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(typename Cx<T>::t *data,
     dst = t;
     Ns *= R;
   }
-  for (int e = threadIdx.x; e < total; e += blockDim.x) {
-    int line, pos;
-    if (axis == 0) { line = e / N; pos = e % N; }
-    else { line = e % tile; pos = e / tile; }
-    data[base + line * lstride + pos * stride] = src[line * N + pos];
+  if (axis == 0) {
+    for (int e = threadIdx.x; e < total; e += blockDim.x) data[base + e] = src[e];
+  } else {
+    for (int e = threadIdx.x; e < total; e += blockDim.x) {
+      const int line = e & (tile - 1), pos = e >> ltile;
+      data[base + line * lstride + (long long)pos * stride] = src[line * N + pos];
+    }
   }
 }
 
@@ -345,7 +372,8 @@ struct ElasticPlan {
   void *tw;       // twiddles, complex of the working precision
   void *z01, *z23;
   double *bn;     // 10 * N^3
-  int tile;
+  int tile, ltile;
+  StageDiv sd;
   size_t smem;
   bool first;     // no previous elastic call: scratch ghosts are zero
 };
@@ -429,7 +457,15 @@ cudaError_t elastic_plan_create(ElasticPlan **out, int N, int nac, const double 
     while (tile > 1 && 2 * (size_t)tile * N * csz > 96 * 1024) tile /= 2;
     while (N % tile) tile /= 2;
     p->tile = tile;
+    p->ltile = 0;
+    while ((1 << p->ltile) < tile) p->ltile++;
     p->smem = 2 * (size_t)tile * N * csz;
+    int ns = 1;
+    for (int st = 0; st < p->rad.count; st++) {
+      p->sd.inv_nb[st] = 1.0f / (float)(N / p->rad.r[st]);
+      p->sd.inv_ns[st] = 1.0f / (float)ns;
+      ns *= p->rad.r[st];
+    }
   }
   *out = p;
   return cudaSuccess;
@@ -447,8 +483,10 @@ void elastic_plan_destroy(ElasticPlan *p) {
   delete p;
 }
 
+// 3-D transform of one or two complex grids (z1 may be null): one launch per
+// axis, x, y, z forward and z, y, x backward.
 template <typename T>
-static cudaError_t fft3d(ElasticPlan *p, typename Cx<T>::t *z, int sign, cudaStream_t s) {
+static cudaError_t fft3d(ElasticPlan *p, typename Cx<T>::t *z0, typename Cx<T>::t *z1, int sign, cudaStream_t s) {
   const int N = p->N;
   static bool attr_set[2] = {false, false};
   int which = sizeof(T) == 4 ? 1 : 0;
@@ -456,12 +494,12 @@ static cudaError_t fft3d(ElasticPlan *p, typename Cx<T>::t *z, int sign, cudaStr
     cudaFuncSetAttribute(fft_lines_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     attr_set[which] = true;
   }
-  const int lines_blocks = (int)((long long)N * N / p->tile);
+  const dim3 grid((unsigned)((long long)N * N / p->tile), z1 ? 2u : 1u);
   const typename Cx<T>::t *tw = (const typename Cx<T>::t *)p->tw;
   int order[3] = {0, 1, 2};
   if (sign > 0) { order[0] = 2; order[2] = 0; }
   for (int k = 0; k < 3; k++) {
-    fft_lines_kernel<T><<<lines_blocks, 256, p->smem, s>>>(z, N, order[k], p->tile, tw, sign, p->rad);
+    fft_lines_kernel<T><<<grid, 256, p->smem, s>>>(z0, z1, N, order[k], p->ltile, tw, sign, p->rad, p->sd);
     launch_counter()++;
   }
   return cudaGetLastError();
@@ -475,12 +513,10 @@ cudaError_t elastic_compute(ElasticPlan *p, const T *u, T *felas, int n, T *shel
   C *z01 = (C *)p->z01, *z23 = (C *)p->z23;
   pack_kernel<T><<<grid1(N3), 256, 0, s>>>(u, z01, z23, N, p->nac);
   launch_counter()++;
-  fft3d<T>(p, z01, -1, s);
-  if (z23) fft3d<T>(p, z23, -1, s);
+  fft3d<T>(p, z01, z23, -1, s);
   contract_kernel<T><<<grid1(N3), 256, 0, s>>>(z01, z23, p->bn, N, p->nac);
   launch_counter()++;
-  fft3d<T>(p, z01, +1, s);
-  if (z23) fft3d<T>(p, z23, +1, s);
+  fft3d<T>(p, z01, z23, +1, s);
   unpack_kernel<T><<<grid1(N3), 256, 0, s>>>(z01, z23, felas, N, p->nac);
   launch_counter()++;
   // ghost cells: the shared-scratch semantics, field by field in order

@@ -35,11 +35,6 @@ struct Ks {
   }
 };
 
-__device__ inline bool owned(int n, long long l) {
-  const int x = (int)(l % n), y = (int)((l / n) % n), z = (int)(l / ((long long)n * n));
-  return x >= 2 && x < n - 2 && y >= 2 && y < n - 2 && z >= 2 && z < n - 2;
-}
-
 // block-wide compensated reduction; thread 0 receives the pair
 __device__ Ks block_reduce(Ks v) {
   __shared__ double sa[MB], sb[MB];
@@ -85,19 +80,27 @@ __global__ void seed_kernel(double *X, const double *g, int n, int which, const 
 }
 
 // Partial target per block: sum of wa*a (or of a over owned cells when wa is
-// null) plus sum of wb*(b - bsub).
+// null) plus sum of wb*(b - bsub).  Rows of x (z*n + y) are spread over the
+// grid; each thread accumulates a plain FP64 sum of its cells, and the blocks
+// and the final fold are compensated.
 __global__ void __launch_bounds__(MB) target_kernel(const float *__restrict__ a, const double *__restrict__ wa,
                                                     const float *__restrict__ b, const float *__restrict__ bsub,
                                                     const double *__restrict__ wb, int n, double *__restrict__ part) {
-  const long long n3 = (long long)n * n * n;
-  Ks acc = {0.0, 0.0};
-  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < n3; l += (long long)gridDim.x * blockDim.x) {
-    if (wa) acc.add(wa[l] * (double)a[l]);
-    else if (owned(n, l)) acc.add((double)a[l]);
-    const double d = bsub ? (double)b[l] - (double)bsub[l] : (double)b[l];
-    acc.add(wb[l] * d);
+  const int nrows = n * n;
+  double acc = 0.0;
+  for (int row = blockIdx.x; row < nrows; row += gridDim.x) {
+    const int y = row % n, z = row / n;
+    const bool own_row = y >= 2 && y < n - 2 && z >= 2 && z < n - 2;
+    const size_t l0 = (size_t)row * n;
+    for (int x = threadIdx.x; x < n; x += blockDim.x) {
+      const size_t l = l0 + x;
+      if (wa) acc += wa[l] * (double)a[l];
+      else if (own_row && x >= 2 && x < n - 2) acc += (double)a[l];
+      const double d = bsub ? (double)b[l] - (double)bsub[l] : (double)b[l];
+      acc += wb[l] * d;
+    }
   }
-  Ks r = block_reduce(acc);
+  Ks r = block_reduce(Ks{acc, 0.0});
   if (threadIdx.x == 0) {
     part[2 * blockIdx.x] = r.s;
     part[2 * blockIdx.x + 1] = r.c;
@@ -106,11 +109,14 @@ __global__ void __launch_bounds__(MB) target_kernel(const float *__restrict__ a,
 
 // Partial owned-cell sum of u per block.
 __global__ void __launch_bounds__(MB) owned_sum_kernel(const float *__restrict__ u, int n, double *__restrict__ part) {
-  const long long n3 = (long long)n * n * n;
-  Ks acc = {0.0, 0.0};
-  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < n3; l += (long long)gridDim.x * blockDim.x)
-    if (owned(n, l)) acc.add((double)u[l]);
-  Ks r = block_reduce(acc);
+  double acc = 0.0;
+  const int N = n - 4;
+  for (int row = blockIdx.x; row < N * N; row += gridDim.x) {
+    const int y = 2 + row % N, z = 2 + row / N;
+    const size_t l0 = ((size_t)z * n + y) * n + 2;
+    for (int x = threadIdx.x; x < N; x += blockDim.x) acc += (double)u[l0 + x];
+  }
+  Ks r = block_reduce(Ks{acc, 0.0});
   if (threadIdx.x == 0) {
     part[2 * blockIdx.x] = r.s;
     part[2 * blockIdx.x + 1] = r.c;
@@ -145,9 +151,12 @@ __global__ void __launch_bounds__(MB) shift_kernel(float *__restrict__ u, int n,
   }
   __syncthreads();
   const float d = (float)delta;
-  const long long n3 = (long long)n * n * n;
-  for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < n3; l += (long long)gridDim.x * blockDim.x)
-    if (owned(n, l)) u[l] += d;
+  const int N = n - 4;
+  for (int row = blockIdx.x; row < N * N; row += gridDim.x) {
+    const int y = 2 + row % N, z = 2 + row / N;
+    const size_t l0 = ((size_t)z * n + y) * n + 2;
+    for (int x = threadIdx.x; x < N; x += blockDim.x) u[l0 + x] += d;
+  }
 }
 
 }  // namespace

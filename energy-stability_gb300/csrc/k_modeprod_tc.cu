@@ -434,14 +434,19 @@ __global__ void slice_fields_kernel(const float *__restrict__ x, const float *__
     const float S = pow2_scale(m), inv = 1.0f / S;
     if (lane == 0) scale[wr] = S;
     const long long o0 = ((long long)t * TC_PLANES * rows + row) * kp;
-    for (int k = lane; k < n; k += 32) {
-      float r = (sub ? x[in0 + k] - sub[in0 + k] : x[in0 + k]) * inv;
+    // two columns per lane, stored as bf16 pairs (kp is even; a pad column
+    // beyond n receives zero slices)
+    for (int k = 2 * lane; k < n; k += 64) {
+      float r0 = (sub ? x[in0 + k] - sub[in0 + k] : x[in0 + k]) * inv;
+      float r1 = 0.0f;
+      if (k + 1 < n) r1 = (sub ? x[in0 + k + 1] - sub[in0 + k + 1] : x[in0 + k + 1]) * inv;
 #pragma unroll
       for (int p = 0; p < TC_PLANES; p++) {
-        float y = r * step;
-        float d = rintf(y);
-        r = y - d;
-        out[o0 + (long long)p * rows * kp + k] = __float2bfloat16_rn(d);
+        const float y0 = r0 * step, y1 = r1 * step;
+        const float d0 = rintf(y0), d1 = rintf(y1);
+        r0 = y0 - d0;
+        r1 = y1 - d1;
+        *reinterpret_cast<__nv_bfloat162 *>(out + o0 + (long long)p * rows * kp + k) = __floats2bfloat162_rn(d0, d1);
       }
     }
   }

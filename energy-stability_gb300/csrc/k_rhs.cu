@@ -70,84 +70,118 @@ __device__ inline long long L3(int n, int z, int y, int x) { return ((long long)
 // blockIdx.z = z; no index division.
 constexpr int RX = 32, RY = 8;
 
-// Field value at offset (dz, dy, dx) from cell (z, y, x), zero outside the
-// block (ac_calc_F2 reads no ghost beyond the block).
-template <typename T>
-struct Nb {
-  const T *__restrict__ u;
-  int n, x, y, z;
-  __device__ T operator()(int dz, int dy, int dx) const {
-    const int xx = x + dx, yy = y + dy, zz = z + dz;
-    if (xx < 0 || xx >= n || yy < 0 || yy >= n || zz < 0 || zz >= n) return (T)0;
-    return u[((size_t)zz * n + yy) * n + xx];
-  }
-};
+// Allen-Cahn right-hand side, 2.5-D: a CTA owns a 32 x 8 (x, y) tile and
+// marches over ZC planes in z, keeping for every order parameter a ring of five
+// planes (z-2 .. z+2) with a two-cell halo in x and y in shared memory (zero
+// outside the block, as ac_calc_F2 reads it).  Each value comes from global
+// memory about once per CTA instead of once per stencil tap.
+constexpr int ZC = 32;             // planes per CTA
+constexpr int HX = RX + 4, HY = RY + 4;
+constexpr int PLANE = HX * HY;     // one haloed plane
 
-// div(lambda grad eta) of ac_calc_F2 (anisotropic.c:164-628): the flux
-// component c at a neighbour p is lam[c] . (central differences at p), zero
-// when p is outside the block; y and z differences are (previous - next), as
-// the reference writes them.  Each of the 19 stencil values is loaded once.
 template <typename T>
-__device__ inline T aniso_f2(const P<T> &p, const Nb<T> &u, const T *lam) {
-  const int n = p.n, x = u.x, y = u.y, z = u.z;
-  const T c0 = u(0, 0, 0);
-  const T xp2 = u(0, 0, 2), xm2 = u(0, 0, -2), yp2 = u(0, 2, 0), ym2 = u(0, -2, 0), zp2 = u(2, 0, 0), zm2 = u(-2, 0, 0);
-  const T xpym = u(0, -1, 1), xpyp = u(0, 1, 1), xmym = u(0, -1, -1), xmyp = u(0, 1, -1);
-  const T xpzm = u(-1, 0, 1), xpzp = u(1, 0, 1), xmzm = u(-1, 0, -1), xmzp = u(1, 0, -1);
-  const T ymzm = u(-1, -1, 0), ymzp = u(1, -1, 0), ypzm = u(-1, 1, 0), ypzp = u(1, 1, 0);
-  const T *l0 = lam, *l1 = lam + 3, *l2 = lam + 6;
-  const T ar = x < n - 1 ? l0[0] * ((xp2 - c0) * p.i2hx) + l0[1] * ((xpym - xpyp) * p.i2hy) + l0[2] * ((xpzm - xpzp) * p.i2hz)
-                         : (T)0;
-  const T al = x > 0 ? l0[0] * ((c0 - xm2) * p.i2hx) + l0[1] * ((xmym - xmyp) * p.i2hy) + l0[2] * ((xmzm - xmzp) * p.i2hz)
-                     : (T)0;
-  const T at = y > 0 ? l1[0] * ((xpym - xmym) * p.i2hx) + l1[1] * ((ym2 - c0) * p.i2hy) + l1[2] * ((ymzm - ymzp) * p.i2hz)
-                     : (T)0;
-  const T ab = y < n - 1 ? l1[0] * ((xpyp - xmyp) * p.i2hx) + l1[1] * ((c0 - yp2) * p.i2hy) + l1[2] * ((ypzm - ypzp) * p.i2hz)
-                         : (T)0;
-  const T af = z > 0 ? l2[0] * ((xpzm - xmzm) * p.i2hx) + l2[1] * ((ymzm - ypzm) * p.i2hy) + l2[2] * ((zm2 - c0) * p.i2hz)
-                     : (T)0;
-  const T ak = z < n - 1 ? l2[0] * ((xpzp - xmzp) * p.i2hx) + l2[1] * ((ymzp - ypzp) * p.i2hy) + l2[2] * ((c0 - zp2) * p.i2hz)
-                         : (T)0;
-  T t = (T)0;
-  t += (ar - al) * p.i2hx;
-  t += (at - ab) * p.i2hy;
-  t += (af - ak) * p.i2hz;
-  return t;
+__device__ inline T sm_at(const T *ring, int z, int ly, int lx) {
+  // ring slot of plane z, local (ly, lx) with the halo offset applied by the caller
+  return ring[((z + 5 * 1024) % 5) * PLANE + ly * HX + lx];
 }
 
 template <typename T>
 __global__ void __launch_bounds__(RX * RY) rhs_ac_kernel(P<T> p, const T *__restrict__ u, const T *__restrict__ felas,
                                                          T *__restrict__ out) {
+  extern __shared__ unsigned char smem_raw[];
+  T *ring = reinterpret_cast<T *>(smem_raw);  // [nac][5][HY][HX]
   const int n = p.n;
-  const int x = blockIdx.x * RX + threadIdx.x, y = blockIdx.y * RY + threadIdx.y, z = blockIdx.z;
-  if (x >= n || y >= n) return;
   const size_t n3 = (size_t)n * n * n;
-  const size_t l = ((size_t)z * n + y) * n + x;
-  T e[4] = {(T)0, (T)0, (T)0, (T)0};
-#pragma unroll
-  for (int m = 0; m < 4; m++)
-    if (m < p.nac) e[m] = u[m * n3 + l];
-  const T c = p.nch > 0 ? u[p.nac * n3 + l] : (T)0;
-  const bool face = x == 0 || x == n - 1 || y == 0 || y == n - 1 || z == 0 || z == n - 1;
-#pragma unroll
-  for (int m = 0; m < 4; m++) {
-    if (m >= p.nac) break;
-    const T *um = u + m * n3;
-    T v = p.LE * p.KE * e[m];
-    v -= p.LE * ac_f(p, e, c, m);
-    if (face) {
-      const int iz = img(n, z), iy = img(n, y), ix = img(n, x), lo = img(n, -1), hi = img(n, n);
-      const T w = p.LE * p.epn2;
-      if (x == 0) v += w * um[L3(n, iz, iy, lo)] * p.ih2x;
-      if (x == n - 1) v += w * um[L3(n, iz, iy, hi)] * p.ih2x;
-      if (y == 0) v += w * um[L3(n, iz, lo, ix)] * p.ih2y;
-      if (y == n - 1) v += w * um[L3(n, iz, hi, ix)] * p.ih2y;
-      if (z == 0) v += w * um[L3(n, lo, iy, ix)] * p.ih2z;
-      if (z == n - 1) v += w * um[L3(n, hi, iy, ix)] * p.ih2z;
+  const int x0 = blockIdx.x * RX, y0 = blockIdx.y * RY;
+  const int zb = blockIdx.z * ZC, ze = zb + ZC < n ? zb + ZC : n;
+  const int tid = threadIdx.y * RX + threadIdx.x;
+  const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
+  auto load_plane = [&](int z) {
+    for (int m = 0; m < p.nac; m++) {
+      T *dst = ring + (size_t)m * 5 * PLANE + ((z + 5 * 1024) % 5) * PLANE;
+      const T *um = u + m * n3;
+      for (int i = tid; i < PLANE; i += RX * RY) {
+        const int ly = i / HX, lx = i - ly * HX;
+        const int gx = x0 + lx - 2, gy = y0 + ly - 2;
+        T v = (T)0;
+        if (z >= 0 && z < n && gx >= 0 && gx < n && gy >= 0 && gy < n) v = um[((size_t)z * n + gy) * n + gx];
+        dst[i] = v;
+      }
     }
-    if (p.aniso) v -= p.epn2 * p.LE * aniso_f2(p, Nb<T>{um, n, x, y, z}, p.lam[m]);
-    if (p.elastic == 1) v -= p.LE * p.es * felas[m * n3 + l];
-    out[m * n3 + l] = v;
+  };
+  for (int z = zb - 2; z < zb + 2; z++) load_plane(z);
+  const int lx = threadIdx.x + 2, ly = threadIdx.y + 2;
+  for (int z = zb; z < ze; z++) {
+    load_plane(z + 2);
+    __syncthreads();
+    if (x < n && y < n) {
+      const size_t l = ((size_t)z * n + y) * n + x;
+      T e[4] = {(T)0, (T)0, (T)0, (T)0};
+#pragma unroll
+      for (int m = 0; m < 4; m++)
+        if (m < p.nac) e[m] = sm_at(ring + (size_t)m * 5 * PLANE, z, ly, lx);
+      const T c = p.nch > 0 ? u[p.nac * n3 + l] : (T)0;
+      const bool face = x == 0 || x == n - 1 || y == 0 || y == n - 1 || z == 0 || z == n - 1;
+#pragma unroll
+      for (int m = 0; m < 4; m++) {
+        if (m >= p.nac) break;
+        const T *um = u + m * n3;
+        const T *rg = ring + (size_t)m * 5 * PLANE;
+        T v = p.LE * p.KE * e[m];
+        v -= p.LE * ac_f(p, e, c, m);
+        if (face) {
+          const int iz = img(n, z), iy = img(n, y), ix = img(n, x), lo = img(n, -1), hi = img(n, n);
+          const T w = p.LE * p.epn2;
+          if (x == 0) v += w * um[L3(n, iz, iy, lo)] * p.ih2x;
+          if (x == n - 1) v += w * um[L3(n, iz, iy, hi)] * p.ih2x;
+          if (y == 0) v += w * um[L3(n, iz, lo, ix)] * p.ih2y;
+          if (y == n - 1) v += w * um[L3(n, iz, hi, ix)] * p.ih2y;
+          if (z == 0) v += w * um[L3(n, lo, iy, ix)] * p.ih2z;
+          if (z == n - 1) v += w * um[L3(n, hi, iy, ix)] * p.ih2z;
+        }
+        if (p.aniso) {
+          // div(lambda grad eta), ac_calc_F2 (anisotropic.c:164-628): the flux
+          // component c at a neighbour q is lam[c] . (central differences at q),
+          // zero when q is outside the block; y and z differences are
+          // (previous - next), as the reference writes them
+          auto U = [&](int dz, int dy, int dx) { return sm_at(rg, z + dz, ly + dy, lx + dx); };
+          const T *lam = p.lam[m];
+          const T c0 = U(0, 0, 0);
+          const T xp2 = U(0, 0, 2), xm2 = U(0, 0, -2), yp2 = U(0, 2, 0), ym2 = U(0, -2, 0), zp2 = U(2, 0, 0),
+                  zm2 = U(-2, 0, 0);
+          const T xpym = U(0, -1, 1), xpyp = U(0, 1, 1), xmym = U(0, -1, -1), xmyp = U(0, 1, -1);
+          const T xpzm = U(-1, 0, 1), xpzp = U(1, 0, 1), xmzm = U(-1, 0, -1), xmzp = U(1, 0, -1);
+          const T ymzm = U(-1, -1, 0), ymzp = U(1, -1, 0), ypzm = U(-1, 1, 0), ypzp = U(1, 1, 0);
+          const T *l0 = lam, *l1 = lam + 3, *l2 = lam + 6;
+          const T ar = x < n - 1 ? l0[0] * ((xp2 - c0) * p.i2hx) + l0[1] * ((xpym - xpyp) * p.i2hy) +
+                                       l0[2] * ((xpzm - xpzp) * p.i2hz)
+                                 : (T)0;
+          const T al = x > 0 ? l0[0] * ((c0 - xm2) * p.i2hx) + l0[1] * ((xmym - xmyp) * p.i2hy) +
+                                   l0[2] * ((xmzm - xmzp) * p.i2hz)
+                             : (T)0;
+          const T at = y > 0 ? l1[0] * ((xpym - xmym) * p.i2hx) + l1[1] * ((ym2 - c0) * p.i2hy) +
+                                   l1[2] * ((ymzm - ymzp) * p.i2hz)
+                             : (T)0;
+          const T ab = y < n - 1 ? l1[0] * ((xpyp - xmyp) * p.i2hx) + l1[1] * ((c0 - yp2) * p.i2hy) +
+                                       l1[2] * ((ypzm - ypzp) * p.i2hz)
+                                 : (T)0;
+          const T af = z > 0 ? l2[0] * ((xpzm - xmzm) * p.i2hx) + l2[1] * ((ymzm - ypzm) * p.i2hy) +
+                                   l2[2] * ((zm2 - c0) * p.i2hz)
+                             : (T)0;
+          const T ak = z < n - 1 ? l2[0] * ((xpzp - xmzp) * p.i2hx) + l2[1] * ((ymzp - ypzp) * p.i2hy) +
+                                       l2[2] * ((c0 - zp2) * p.i2hz)
+                                 : (T)0;
+          T t = (T)0;
+          t += (ar - al) * p.i2hx;
+          t += (at - ab) * p.i2hy;
+          t += (af - ak) * p.i2hz;
+          v -= p.epn2 * p.LE * t;
+        }
+        if (p.elastic == 1) v -= p.LE * p.es * felas[m * n3 + l];
+        out[m * n3 + l] = v;
+      }
+    }
+    __syncthreads();
   }
 }
 
@@ -232,7 +266,16 @@ cudaError_t launch_rhs(const Phys &ph, const T *u, const T *felas, T *out, T *sc
   long long n3 = (long long)ph.n * ph.n * ph.n;
   const dim3 blk(RX, RY), grd((ph.n + RX - 1) / RX, (ph.n + RY - 1) / RY, ph.n);
   if (ph.nac > 0) {
-    rhs_ac_kernel<T><<<grd, blk, 0, s>>>(p, u, felas, out);
+    const size_t smem = sizeof(T) * ph.nac * 5 * PLANE;
+    static bool attr[2] = {false, false};
+    if (!attr[sizeof(T) == 8]) {
+      cudaError_t e = cudaFuncSetAttribute(rhs_ac_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)(sizeof(T) * 4 * 5 * PLANE));
+      if (e != cudaSuccess) return e;
+      attr[sizeof(T) == 8] = true;
+    }
+    const dim3 gac((ph.n + RX - 1) / RX, (ph.n + RY - 1) / RY, (ph.n + ZC - 1) / ZC);
+    rhs_ac_kernel<T><<<gac, blk, smem, s>>>(p, u, felas, out);
     launch_counter()++;
   }
   for (int m = 0; m < ph.nch; m++) {

@@ -33,6 +33,7 @@ struct StageEv {
 struct sclet_ctx {
   sclet_params p;
   int precision = SCLET_FP64, device = 0;
+  int step_diag = -1;  // energy form of the diagnostics sclet_step queues after each step; -1 none
   int n = 0, F = 0, nac = 0, nch = 0;
   long long n3 = 0;
   Phys ph;
@@ -138,6 +139,8 @@ int fail(sclet_ctx *ctx, int code, const std::string &msg) {
 }
 
 int mass_weights_setup(sclet_ctx *ctx, const double *v, const double *vi);
+int queue_diagnostics(sclet_ctx *ctx, int energy_form);
+int read_diagnostics(sclet_ctx *ctx, sclet_diag *out);
 
 int upload_eigen(sclet_ctx *ctx, const double *d, const double *v, const double *vi) {
   const int n = ctx->n;
@@ -742,11 +745,30 @@ int sclet_step(sclet_ctx *ctx, int nsteps) {
       if ((rc = sclet_calc_rhs(ctx, 2)) != SCLET_OK) return rc;
       if ((rc = sclet_etd2_correct(ctx)) != SCLET_OK) return rc;
     }
+    if (ctx->step_diag >= 0 && (rc = queue_diagnostics(ctx, ctx->step_diag)) != SCLET_OK) return rc;
   }
   return SCLET_OK;
 }
 
+int sclet_set_step_diagnostics(sclet_ctx *ctx, int energy_form) {
+  if (energy_form < -1 || energy_form > 1) return fail(ctx, SCLET_ERR_ARG, "energy_form must be -1, 0 or 1");
+  ctx->step_diag = energy_form;
+  return SCLET_OK;
+}
+
+int sclet_last_diagnostics(sclet_ctx *ctx, sclet_diag *out) { return read_diagnostics(ctx, out); }
+
 int sclet_check_soln(sclet_ctx *ctx, int energy_form, sclet_diag *out) {
+  int rc = queue_diagnostics(ctx, energy_form);
+  if (rc != SCLET_OK) return rc;
+  return read_diagnostics(ctx, out);
+}
+
+}  // extern "C"
+
+namespace {
+// check_soln_new's reductions on the context's stream into the device record
+int queue_diagnostics(sclet_ctx *ctx, int energy_form) {
   StageEv ev;
   long long l0 = launch_counter();
   stage_begin(ctx, 4, ev);
@@ -757,6 +779,11 @@ int sclet_check_soln(sclet_ctx *ctx, int energy_form, sclet_diag *out) {
     CK(launch_check_soln<double>(ctx->ph, u_of(ctx), ctx->elam, energy_form, ctx->partials, ctx->npart, ctx->diag,
                                  ctx->stream));
   stage_end(ctx, ev, l0);
+  return SCLET_OK;
+}
+
+// waits for the stream and copies the last diagnostics record out
+int read_diagnostics(sclet_ctx *ctx, sclet_diag *out) {
   std::vector<double> h(4 * ctx->F);
   CK(cudaMemcpyAsync(h.data(), ctx->diag, sizeof(double) * 4 * ctx->F, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
@@ -771,6 +798,9 @@ int sclet_check_soln(sclet_ctx *ctx, int energy_form, sclet_diag *out) {
   if (nonfinite) return fail(ctx, SCLET_ERR_NONFINITE, "non-finite value in the state");
   return SCLET_OK;
 }
+}  // namespace
+
+extern "C" {
 
 int sclet_mode_product(sclet_ctx *ctx, int inverse, const double *in, double *out) {
   const long long n3 = ctx->n3;

@@ -82,6 +82,8 @@ SIGNATURES = {
     "sclet_etd2_correct": (ctypes.c_int, [ctypes.c_void_p]),
     "sclet_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "sclet_check_soln": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "sclet_set_step_diagnostics": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "sclet_last_diagnostics": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "sclet_set_energy_tensors": (ctypes.c_int, [ctypes.c_void_p, _c_dp]),
     "sclet_get_rhs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _c_dp]),
     "sclet_get_felas": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, _c_dp]),
@@ -247,6 +249,15 @@ class Solver:
     def check_soln(self, form: int = 1) -> np.ndarray:
         d = (Diag * self.F)()
         self._ck(self.L.sclet_check_soln(self.h, form, d), "check_soln")
+        return np.array([[x.max, x.min, x.vol, x.energy] for x in d])
+
+    def set_step_diagnostics(self, form: int = 1):
+        """Queue check_soln_new after every step (form -1: none)."""
+        self._ck(self.L.sclet_set_step_diagnostics(self.h, form), "set_step_diagnostics")
+
+    def last_diagnostics(self) -> np.ndarray:
+        d = (Diag * self.F)()
+        self._ck(self.L.sclet_last_diagnostics(self.h, d), "last_diagnostics")
         return np.array([[x.max, x.min, x.vol, x.energy] for x in d])
 
     def set_energy_tensors(self, lam: np.ndarray):

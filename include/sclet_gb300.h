@@ -160,6 +160,13 @@ int sclet_step(sclet_ctx *ctx, int nsteps);
  * AC fields first).  energy_form 0: the reference's hard-coded polynomial and
  * its per-kind energies; 1: the plugin's total free energy. */
 int sclet_check_soln(sclet_ctx *ctx, int energy_form, sclet_diag *out);
+/* The reference's loop runs check_soln_new after every pass (ScLETD.c:86-190).
+ * With energy_form 0 or 1, sclet_step queues the same reductions after each
+ * step on the context's stream (no host synchronisation); -1 (the default)
+ * queues none.  sclet_last_diagnostics waits for the stream and returns the
+ * most recent record. */
+int sclet_set_step_diagnostics(sclet_ctx *ctx, int energy_form);
+int sclet_last_diagnostics(sclet_ctx *ctx, sclet_diag *out);
 /* Gradient tensors used by the energy (per AC field, 3x3 row-major).  The
  * default is the gradient operator of the dynamics: lambda_file when
  * anisotropic, else diag(kk). */

@@ -75,3 +75,19 @@ def test_mixed_matches_fp64_beta_alpha_192(sclet_lib):
     errs, eerr = _mixed_vs_fp64(sclet_lib, case, 50)
     assert max(errs) <= 1e-5, errs
     assert eerr <= 1e-6, eerr
+
+
+@pytest.mark.parametrize("precision_name", ["FP64", "MIXED"])
+def test_step_diagnostics_match_check_soln(precision_name, sclet_lib):
+    """Diagnostics queued inside sclet_step (as the reference's loop runs
+    check_soln_new every pass) equal a separate sclet_check_soln."""
+    sg = sclet_lib
+    case = bench.workload(32, seed=11)
+    s = sg.Solver(params_for(sg, case), getattr(sg, precision_name))
+    s.set_fields(bench.block_fields(case))
+    s.set_step_diagnostics(1)
+    s.step(3)
+    queued = s.last_diagnostics()
+    s.set_step_diagnostics(-1)
+    np.testing.assert_array_equal(queued, s.check_soln(1))
+    s.close()
