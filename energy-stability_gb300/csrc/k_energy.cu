@@ -35,6 +35,30 @@ __device__ inline KS ks_merge(KS a, KS b) {
 }
 
 constexpr int EB = 256;  // threads per block
+
+// Per-thread sum of T values with FP64-class accuracy.  For FP32 values the
+// running sum is a float pair (s, e) updated by the error-free TwoSum (Knuth),
+// about 48 bits, so a thread's few dozen terms cost FP32 instructions, not
+// FP64 ones (the FP64 pipe of this GPU is 1/64 of the FP32 rate).
+template <typename T>
+struct Acc;
+template <>
+struct Acc<double> {
+  double s = 0.0;
+  __device__ void add(double v) { s += v; }
+  __device__ double value() const { return s; }
+};
+template <>
+struct Acc<float> {
+  float s = 0.0f, e = 0.0f;
+  __device__ void add(float v) {
+    const float t = s + v;
+    const float bp = t - s;
+    e += (s - (t - bp)) + (v - bp);
+    s = t;
+  }
+  __device__ double value() const { return (double)s + (double)e; }
+};
 constexpr int MAXF = 5;
 
 // partial record per block: for f < F: max, min, vol.s, vol.c; then
@@ -59,14 +83,12 @@ __global__ void __launch_bounds__(EB) energy_partial_kernel(Phys ph, const T *__
   const T a2h = (T)(ph.a2 / 2.0), a4q = (T)(ph.a4 / 4.0), a6s = (T)(ph.a6 / 6.0), g = (T)ph.g, th = (T)ph.th;
   const T Ah = (T)(ph.A / 2.0);
   T mx[MAXF], mn[MAXF];
-  double vsum[MAXF];
-  double eac_p = 0.0, ech_p = 0.0;
+  Acc<T> vsum[MAXF], eac_p, ech_p;
   long long cnt = 0;
 #pragma unroll
   for (int f = 0; f < MAXF; f++) {
     mx[f] = (T)-1.0e30;
     mn[f] = (T)1.0e30;
-    vsum[f] = 0.0;
   }
   for (long long gi = blockIdx.x * (long long)blockDim.x + threadIdx.x; gi < N3; gi += (long long)gridDim.x * blockDim.x) {
     const int i = 2 + (int)(gi % N), j = 2 + (int)((gi / N) % N), k = 2 + (int)(gi / ((long long)N * N));
@@ -78,7 +100,7 @@ __global__ void __launch_bounds__(EB) energy_partial_kernel(Phys ph, const T *__
       const T t = u[f * n3 + l];
       mx[f] = t > mx[f] ? t : mx[f];
       mn[f] = t < mn[f] ? t : mn[f];
-      vsum[f] += (double)t;
+      vsum[f].add(t);
     }
     if (i >= n - 3 || j >= n - 3 || k >= n - 3) continue;
     T avg[MAXF];
@@ -103,8 +125,16 @@ __global__ void __launch_bounds__(EB) energy_partial_kernel(Phys ph, const T *__
       } else {
         const T gr = half_epn2 * (ux * ux + uy * uy + uz * uz);
         if (form == 0) e_ch += gr; else e_ac += gr;
-        cbar = ((double)v0 + (double)v1 + (double)v2 + (double)v3 + (double)v4 + (double)v5 + (double)v6 + (double)v7) *
-                   0.125 + cshift;
+        Acc<T> cs;
+        cs.add(v0);
+        cs.add(v1);
+        cs.add(v2);
+        cs.add(v3);
+        cs.add(v4);
+        cs.add(v5);
+        cs.add(v6);
+        cs.add(v7);
+        cbar = cs.value() * 0.125 + cshift;
       }
     }
     if (form == 0) {
@@ -139,18 +169,18 @@ __global__ void __launch_bounds__(EB) energy_partial_kernel(Phys ph, const T *__
       }
       e_ac += fl;
     }
-    eac_p += (double)e_ac;
-    ech_p += (double)e_ch;
+    eac_p.add(e_ac);
+    ech_p.add(e_ch);
   }
   double mxd[MAXF], mnd[MAXF];
-  KS vol[MAXF], eac = {eac_p, 0.0}, ech = {ech_p, 0.0};
+  KS vol[MAXF], eac = {eac_p.value(), 0.0}, ech = {ech_p.value(), 0.0};
 #pragma unroll
   for (int f = 0; f < MAXF; f++) {
     const double sh = f >= nac ? cshift : 0.0;
     mxd[f] = (double)mx[f] + sh;
     mnd[f] = (double)mn[f] + sh;
     // sum of (value + 1) over this thread's cells, the constant part exact
-    vol[f].s = vsum[f];
+    vol[f].s = vsum[f].value();
     vol[f].c = 0.0;
     ks_add(vol[f], (double)cnt * (sh + 1.0));
   }

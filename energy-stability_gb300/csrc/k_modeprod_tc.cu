@@ -416,37 +416,56 @@ __device__ __forceinline__ float pow2_scale(float m) {
 // FP32 rows of n (x - sub) -> slices, one warp per row: the row's max gives its
 // power-of-two scale S; each slice is exact (the residual is scaled by 2^b and
 // reduced by its nearest integer).
+constexpr int SLICE_MAXC = 17;  // column pairs per lane: rows of up to 32 * 2 * 17 = 1088 values
+
+// C = column-pair chunks per lane held in registers (C >= ceil(n / 64)).
+template <int C>
 __global__ void slice_fields_kernel(const float *__restrict__ x, const float *__restrict__ sub, float *__restrict__ scale,
                                     __nv_bfloat16 *__restrict__ out, int n, int kp, int count, int bits) {
   const float step = ldexpf(1.0f, bits);
   const long long rows = (long long)n * n, total_rows = rows * count;
   const int lane = threadIdx.x & 31;
+  const int chunks = (n + 63) / 64;
   const long long warp0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   for (long long wr = warp0; wr < total_rows; wr += nwarps) {
     const int t = (int)(wr / rows);
     const long long row = wr - (long long)t * rows;
     const long long in0 = wr * n;  // rows are contiguous lines of n
+    // the whole line in registers (one read), two columns per lane and chunk
+    float v0[C], v1[C];
     float m = 0.0f;
-    for (int k = lane; k < n; k += 32) m = fmaxf(m, fabsf(sub ? x[in0 + k] - sub[in0 + k] : x[in0 + k]));
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+      v0[c] = 0.0f;
+      v1[c] = 0.0f;
+      if (c < chunks) {
+        const int k = 2 * lane + 64 * c;
+        if (k < n) v0[c] = sub ? x[in0 + k] - sub[in0 + k] : x[in0 + k];
+        if (k + 1 < n) v1[c] = sub ? x[in0 + k + 1] - sub[in0 + k + 1] : x[in0 + k + 1];
+        m = fmaxf(m, fmaxf(fabsf(v0[c]), fabsf(v1[c])));
+      }
+    }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
     const float S = pow2_scale(m), inv = 1.0f / S;
     if (lane == 0) scale[wr] = S;
     const long long o0 = ((long long)t * TC_PLANES * rows + row) * kp;
-    // two columns per lane, stored as bf16 pairs (kp is even; a pad column
-    // beyond n receives zero slices)
-    for (int k = 2 * lane; k < n; k += 64) {
-      float r0 = (sub ? x[in0 + k] - sub[in0 + k] : x[in0 + k]) * inv;
-      float r1 = 0.0f;
-      if (k + 1 < n) r1 = (sub ? x[in0 + k + 1] - sub[in0 + k + 1] : x[in0 + k + 1]) * inv;
+    // stored as bf16 pairs (kp is even; a pad column beyond n receives zero
+    // slices)
 #pragma unroll
-      for (int p = 0; p < TC_PLANES; p++) {
-        const float y0 = r0 * step, y1 = r1 * step;
-        const float d0 = rintf(y0), d1 = rintf(y1);
-        r0 = y0 - d0;
-        r1 = y1 - d1;
-        *reinterpret_cast<__nv_bfloat162 *>(out + o0 + (long long)p * rows * kp + k) = __floats2bfloat162_rn(d0, d1);
+    for (int c = 0; c < C; c++) {
+      const int k = 2 * lane + 64 * c;
+      if (c < chunks && k < n) {
+        float r0 = v0[c] * inv, r1 = v1[c] * inv;
+#pragma unroll
+        for (int p = 0; p < TC_PLANES; p++) {
+          const float y0 = r0 * step, y1 = r1 * step;
+          const float d0 = rintf(y0), d1 = rintf(y1);
+          r0 = y0 - d0;
+          r1 = y1 - d1;
+          *reinterpret_cast<__nv_bfloat162 *>(out + o0 + (long long)p * rows * kp + k) = __floats2bfloat162_rn(d0, d1);
+        }
       }
     }
   }
@@ -574,10 +593,15 @@ cudaError_t tc_slice_matrix(const double *m, __nv_bfloat16 *planes, float *row_s
 
 cudaError_t tc_slice_fields(const float *x, const float *sub, float *scale, __nv_bfloat16 *planes, int n, int count,
                             cudaStream_t s) {
+  if (n > 64 * tc::SLICE_MAXC) return cudaErrorInvalidValue;
   long long warps = (long long)n * n * count;
   long long blocks = (warps * 32 + 255) / 256;
   int g = (int)(blocks > 152 * 32 ? 152 * 32 : blocks);
-  tc::slice_fields_kernel<<<g, 256, 0, s>>>(x, sub, scale, planes, n, tc_kp(n), count, tc_slice_bits(n));
+  const int chunks = (n + 63) / 64, kp = tc_kp(n), bits = tc_slice_bits(n);
+  if (chunks <= 2) tc::slice_fields_kernel<2><<<g, 256, 0, s>>>(x, sub, scale, planes, n, kp, count, bits);
+  else if (chunks <= 4) tc::slice_fields_kernel<4><<<g, 256, 0, s>>>(x, sub, scale, planes, n, kp, count, bits);
+  else if (chunks <= 8) tc::slice_fields_kernel<8><<<g, 256, 0, s>>>(x, sub, scale, planes, n, kp, count, bits);
+  else tc::slice_fields_kernel<tc::SLICE_MAXC><<<g, 256, 0, s>>>(x, sub, scale, planes, n, kp, count, bits);
   launch_counter()++;
   return cudaGetLastError();
 }

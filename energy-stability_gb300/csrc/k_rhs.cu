@@ -45,11 +45,12 @@ static P<T> to_p(const Phys &ph) {
   return p;
 }
 
-// dF/deta_m of the plugin (AC_f).
-template <typename T>
-__device__ inline T ac_f(const P<T> &p, const T *e, T c, int m) {
+// dF/deta_m of the plugin (AC_f), NAC fields known at compile time.
+template <typename T, int NAC>
+__device__ __forceinline__ T ac_f_n(const P<T> &p, const T *e, T c, int m) {
   T u = e[m], u2 = u * u, others = (T)0;
-  for (int k = 0; k < p.nac; k++)
+#pragma unroll
+  for (int k = 0; k < NAC; k++)
     if (k != m) others += e[k] * e[k];
   T f = p.a2 * u + p.a4 * u2 * u + p.a6 * u2 * u2 * u + (T)2 * p.g * u * others;
   if (p.nch > 0) f -= (T)2 * p.th * (c - p.c0) * u;
@@ -79,13 +80,7 @@ constexpr int ZC = 32;             // planes per CTA
 constexpr int HX = RX + 4, HY = RY + 4;
 constexpr int PLANE = HX * HY;     // one haloed plane
 
-template <typename T>
-__device__ inline T sm_at(const T *ring, int z, int ly, int lx) {
-  // ring slot of plane z, local (ly, lx) with the halo offset applied by the caller
-  return ring[((z + 5 * 1024) % 5) * PLANE + ly * HX + lx];
-}
-
-template <typename T>
+template <typename T, int NAC, bool ANISO>
 __global__ void __launch_bounds__(RX * RY) rhs_ac_kernel(P<T> p, const T *__restrict__ u, const T *__restrict__ felas,
                                                          T *__restrict__ out) {
   extern __shared__ unsigned char smem_raw[];
@@ -96,39 +91,63 @@ __global__ void __launch_bounds__(RX * RY) rhs_ac_kernel(P<T> p, const T *__rest
   const int zb = blockIdx.z * ZC, ze = zb + ZC < n ? zb + ZC : n;
   const int tid = threadIdx.y * RX + threadIdx.x;
   const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
-  auto load_plane = [&](int z) {
-    for (int m = 0; m < p.nac; m++) {
-      T *dst = ring + (size_t)m * 5 * PLANE + ((z + 5 * 1024) % 5) * PLANE;
+  // this thread's share of one haloed plane of every order parameter:
+  // PLANE / 256 rounded up values per field
+  constexpr int PER = (PLANE + RX * RY - 1) / (RX * RY);
+  auto fetch = [&](int z, T *reg) {
+#pragma unroll
+    for (int m = 0; m < NAC; m++) {
       const T *um = u + m * n3;
-      for (int i = tid; i < PLANE; i += RX * RY) {
+#pragma unroll
+      for (int q = 0; q < PER; q++) {
+        const int i = tid + q * RX * RY;
         const int ly = i / HX, lx = i - ly * HX;
         const int gx = x0 + lx - 2, gy = y0 + ly - 2;
         T v = (T)0;
-        if (z >= 0 && z < n && gx >= 0 && gx < n && gy >= 0 && gy < n) v = um[((size_t)z * n + gy) * n + gx];
-        dst[i] = v;
+        if (i < PLANE && z >= 0 && z < n && gx >= 0 && gx < n && gy >= 0 && gy < n) v = um[((size_t)z * n + gy) * n + gx];
+        reg[m * PER + q] = v;
       }
     }
   };
-  for (int z = zb - 2; z < zb + 2; z++) load_plane(z);
+  auto store = [&](int z, const T *reg) {
+#pragma unroll
+    for (int m = 0; m < NAC; m++) {
+      T *dst = ring + (size_t)m * 5 * PLANE + ((z + 5 * 1024) % 5) * PLANE;
+#pragma unroll
+      for (int q = 0; q < PER; q++) {
+        const int i = tid + q * RX * RY;
+        if (i < PLANE) dst[i] = reg[m * PER + q];
+      }
+    }
+  };
+  T pre[NAC * PER];
+  for (int z = zb - 2; z < zb + 2; z++) {
+    fetch(z, pre);
+    store(z, pre);
+  }
+  fetch(zb + 2, pre);  // plane z + 2 of the first pass, in flight
   const int lx = threadIdx.x + 2, ly = threadIdx.y + 2;
   for (int z = zb; z < ze; z++) {
-    load_plane(z + 2);
+    store(z + 2, pre);
     __syncthreads();
+    if (z + 3 < ze + 2) fetch(z + 3, pre);  // next plane loads overlap this plane's work
     if (x < n && y < n) {
       const size_t l = ((size_t)z * n + y) * n + x;
-      T e[4] = {(T)0, (T)0, (T)0, (T)0};
+      // ring slots of planes z-2 .. z+2, with this thread's (ly, lx) applied
+      int so[5];
 #pragma unroll
-      for (int m = 0; m < 4; m++)
-        if (m < p.nac) e[m] = sm_at(ring + (size_t)m * 5 * PLANE, z, ly, lx);
+      for (int d = 0; d < 5; d++) so[d] = ((z + d - 2 + 5 * 1024) % 5) * PLANE + ly * HX + lx;
+      T e[NAC];
+#pragma unroll
+      for (int m = 0; m < NAC; m++) e[m] = ring[(size_t)m * 5 * PLANE + so[2]];
       const T c = p.nch > 0 ? u[p.nac * n3 + l] : (T)0;
       const bool face = x == 0 || x == n - 1 || y == 0 || y == n - 1 || z == 0 || z == n - 1;
 #pragma unroll
-      for (int m = 0; m < 4; m++) {
-        if (m >= p.nac) break;
+      for (int m = 0; m < NAC; m++) {
         const T *um = u + m * n3;
         const T *rg = ring + (size_t)m * 5 * PLANE;
         T v = p.LE * p.KE * e[m];
-        v -= p.LE * ac_f(p, e, c, m);
+        v -= p.LE * ac_f_n<T, NAC>(p, e, c, m);
         if (face) {
           const int iz = img(n, z), iy = img(n, y), ix = img(n, x), lo = img(n, -1), hi = img(n, n);
           const T w = p.LE * p.epn2;
@@ -139,12 +158,12 @@ __global__ void __launch_bounds__(RX * RY) rhs_ac_kernel(P<T> p, const T *__rest
           if (z == 0) v += w * um[L3(n, lo, iy, ix)] * p.ih2z;
           if (z == n - 1) v += w * um[L3(n, hi, iy, ix)] * p.ih2z;
         }
-        if (p.aniso) {
+        if (ANISO) {
           // div(lambda grad eta), ac_calc_F2 (anisotropic.c:164-628): the flux
           // component c at a neighbour q is lam[c] . (central differences at q),
           // zero when q is outside the block; y and z differences are
           // (previous - next), as the reference writes them
-          auto U = [&](int dz, int dy, int dx) { return sm_at(rg, z + dz, ly + dy, lx + dx); };
+          auto U = [&](int dz, int dy, int dx) { return rg[so[dz + 2] + dy * HX + dx]; };
           const T *lam = p.lam[m];
           const T c0 = U(0, 0, 0);
           const T xp2 = U(0, 0, 2), xm2 = U(0, 0, -2), yp2 = U(0, 2, 0), ym2 = U(0, -2, 0), zp2 = U(2, 0, 0),
@@ -267,15 +286,20 @@ cudaError_t launch_rhs(const Phys &ph, const T *u, const T *felas, T *out, T *sc
   const dim3 blk(RX, RY), grd((ph.n + RX - 1) / RX, (ph.n + RY - 1) / RY, ph.n);
   if (ph.nac > 0) {
     const size_t smem = sizeof(T) * ph.nac * 5 * PLANE;
-    static bool attr[2] = {false, false};
-    if (!attr[sizeof(T) == 8]) {
-      cudaError_t e = cudaFuncSetAttribute(rhs_ac_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)(sizeof(T) * 4 * 5 * PLANE));
-      if (e != cudaSuccess) return e;
-      attr[sizeof(T) == 8] = true;
-    }
     const dim3 gac((ph.n + RX - 1) / RX, (ph.n + RY - 1) / RY, (ph.n + ZC - 1) / ZC);
-    rhs_ac_kernel<T><<<gac, blk, smem, s>>>(p, u, felas, out);
+    cudaError_t e = cudaSuccess;
+    switch (ph.nac * 2 + (ph.anisotropic ? 1 : 0)) {
+#define SCLET_RHS_AC(NAC, AN)                                                                                   \
+  case NAC * 2 + AN:                                                                                            \
+    e = cudaFuncSetAttribute(rhs_ac_kernel<T, NAC, AN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    if (e == cudaSuccess) rhs_ac_kernel<T, NAC, AN><<<gac, blk, smem, s>>>(p, u, felas, out);                    \
+    break;
+      SCLET_RHS_AC(1, 0) SCLET_RHS_AC(1, 1) SCLET_RHS_AC(2, 0) SCLET_RHS_AC(2, 1)
+      SCLET_RHS_AC(3, 0) SCLET_RHS_AC(3, 1) SCLET_RHS_AC(4, 0) SCLET_RHS_AC(4, 1)
+#undef SCLET_RHS_AC
+      default: e = cudaErrorInvalidValue;
+    }
+    if (e != cudaSuccess) return e;
     launch_counter()++;
   }
   for (int m = 0; m < ph.nch; m++) {
