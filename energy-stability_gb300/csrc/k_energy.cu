@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(EB) energy_partial_kernel(Phys ph, const T *__
   // sum; every sum (per thread, per block, over blocks) is FP64, and the
   // volume integrals add the FP32 values exactly.
   const int n = ph.n, N = n - 4, F = ph.F, nac = ph.nac;
-  const long long n3 = (long long)n * n * n, N3 = (long long)N * N * N;
+  const long long n3 = (long long)n * n * n;
   const T i4hx = (T)(0.25 / ph.h[0]), i4hy = (T)(0.25 / ph.h[1]), i4hz = (T)(0.25 / ph.h[2]);
   const T half_epn2 = (T)(0.5 * ph.epn2);
   const double cshift = ph.cshift;
@@ -90,8 +90,10 @@ __global__ void __launch_bounds__(EB) energy_partial_kernel(Phys ph, const T *__
     mx[f] = (T)-1.0e30;
     mn[f] = (T)1.0e30;
   }
-  for (long long gi = blockIdx.x * (long long)blockDim.x + threadIdx.x; gi < N3; gi += (long long)gridDim.x * blockDim.x) {
-    const int i = 2 + (int)(gi % N), j = 2 + (int)((gi / N) % N), k = 2 + (int)(gi / ((long long)N * N));
+  // rows (j, k) of owned cells over the grid, x across the block: no index division per cell
+  for (int row = blockIdx.x; row < N * N; row += gridDim.x) {
+  const int j = 2 + row % N, k = 2 + row / N;
+  for (int i = 2 + threadIdx.x; i < n - 2; i += blockDim.x) {
     const long long l = ((long long)k * n + j) * n + i;
     cnt++;
 #pragma unroll
@@ -172,6 +174,7 @@ __global__ void __launch_bounds__(EB) energy_partial_kernel(Phys ph, const T *__
     eac_p.add(e_ac);
     ech_p.add(e_ch);
   }
+  }
   double mxd[MAXF], mnd[MAXF];
   KS vol[MAXF], eac = {eac_p.value(), 0.0}, ech = {ech_p.value(), 0.0};
 #pragma unroll
@@ -184,57 +187,75 @@ __global__ void __launch_bounds__(EB) energy_partial_kernel(Phys ph, const T *__
     vol[f].c = 0.0;
     ks_add(vol[f], (double)cnt * (sh + 1.0));
   }
-  // block reduction through shared memory
-  __shared__ double sh[EB];
-  __shared__ double out_rec[4 * MAXF + 4];
-  auto reduce_max = [&](double v, bool is_max) -> double {
-    sh[threadIdx.x] = v;
-    __syncthreads();
-    for (int w = EB / 2; w > 0; w >>= 1) {
-      if (threadIdx.x < w) sh[threadIdx.x] = is_max ? fmax(sh[threadIdx.x], sh[threadIdx.x + w]) : fmin(sh[threadIdx.x], sh[threadIdx.x + w]);
-      __syncthreads();
-    }
-    double r = sh[0];
-    __syncthreads();
-    return r;
+  // Reduction of the record (per field max, min, vol; two energies): warp
+  // butterflies, then the block's warps in lane order; fixed shape, so the
+  // result is deterministic.  TwoSum is exact and symmetric, so every lane of
+  // a butterfly holds the same pair.
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  constexpr int NW = EB / 32;
+  __shared__ double wrec[NW][4 * MAXF + 4];
+  auto shfl_ks = [](KS v, int off) {
+    KS o;
+    o.s = __shfl_xor_sync(0xffffffffu, v.s, off);
+    o.c = __shfl_xor_sync(0xffffffffu, v.c, off);
+    return ks_merge(v, o);
   };
-  __shared__ double shc[EB];
-  auto reduce_ks = [&](KS v) -> KS {
-    sh[threadIdx.x] = v.s;
-    shc[threadIdx.x] = v.c;
-    __syncthreads();
-    for (int w = EB / 2; w > 0; w >>= 1) {
-      if (threadIdx.x < w) {
-        KS a = {sh[threadIdx.x], shc[threadIdx.x]}, b = {sh[threadIdx.x + w], shc[threadIdx.x + w]};
-        KS r = ks_merge(a, b);
-        sh[threadIdx.x] = r.s;
-        shc[threadIdx.x] = r.c;
-      }
-      __syncthreads();
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+    for (int f = 0; f < MAXF; f++) {
+      mxd[f] = fmax(mxd[f], __shfl_xor_sync(0xffffffffu, mxd[f], off));
+      mnd[f] = fmin(mnd[f], __shfl_xor_sync(0xffffffffu, mnd[f], off));
+      vol[f] = shfl_ks(vol[f], off);
     }
-    KS r = {sh[0], shc[0]};
-    __syncthreads();
-    return r;
-  };
-  for (int f = 0; f < F; f++) {
-    double a = reduce_max(mxd[f], true);
-    double b = reduce_max(mnd[f], false);
-    KS v = reduce_ks(vol[f]);
-    if (threadIdx.x == 0) {
-      out_rec[4 * f] = a;
-      out_rec[4 * f + 1] = b;
-      out_rec[4 * f + 2] = v.s;
-      out_rec[4 * f + 3] = v.c;
-    }
+    eac = shfl_ks(eac, off);
+    ech = shfl_ks(ech, off);
   }
-  KS a = reduce_ks(eac), b = reduce_ks(ech);
-  if (threadIdx.x == 0) {
+  if (lane == 0) {
+    for (int f = 0; f < F; f++) {
+      wrec[wid][4 * f] = mxd[f];
+      wrec[wid][4 * f + 1] = mnd[f];
+      wrec[wid][4 * f + 2] = vol[f].s;
+      wrec[wid][4 * f + 3] = vol[f].c;
+    }
+    wrec[wid][4 * F] = eac.s;
+    wrec[wid][4 * F + 1] = eac.c;
+    wrec[wid][4 * F + 2] = ech.s;
+    wrec[wid][4 * F + 3] = ech.c;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    const int src = lane < NW ? lane : 0;  // lanes beyond the warp count repeat warp 0 (idempotent for max/min)
     double *dst = part + (long long)blockIdx.x * rec_len(F);
-    for (int q = 0; q < 4 * F; q++) dst[q] = out_rec[q];
-    dst[4 * F] = a.s;
-    dst[4 * F + 1] = a.c;
-    dst[4 * F + 2] = b.s;
-    dst[4 * F + 3] = b.c;
+    for (int f = 0; f < F; f++) {
+      double a = wrec[src][4 * f], b = wrec[src][4 * f + 1];
+      KS v = {lane < NW ? wrec[src][4 * f + 2] : 0.0, lane < NW ? wrec[src][4 * f + 3] : 0.0};
+#pragma unroll
+      for (int off = NW / 2; off > 0; off >>= 1) {
+        a = fmax(a, __shfl_xor_sync(0xffffffffu, a, off));
+        b = fmin(b, __shfl_xor_sync(0xffffffffu, b, off));
+        v = shfl_ks(v, off);
+      }
+      if (lane == 0) {
+        dst[4 * f] = a;
+        dst[4 * f + 1] = b;
+        dst[4 * f + 2] = v.s;
+        dst[4 * f + 3] = v.c;
+      }
+    }
+    KS ea = {lane < NW ? wrec[src][4 * F] : 0.0, lane < NW ? wrec[src][4 * F + 1] : 0.0};
+    KS eb = {lane < NW ? wrec[src][4 * F + 2] : 0.0, lane < NW ? wrec[src][4 * F + 3] : 0.0};
+#pragma unroll
+    for (int off = NW / 2; off > 0; off >>= 1) {
+      ea = shfl_ks(ea, off);
+      eb = shfl_ks(eb, off);
+    }
+    if (lane == 0) {
+      dst[4 * F] = ea.s;
+      dst[4 * F + 1] = ea.c;
+      dst[4 * F + 2] = eb.s;
+      dst[4 * F + 3] = eb.c;
+    }
   }
 }
 
@@ -292,7 +313,7 @@ __global__ void __launch_bounds__(EB) energy_final_kernel(Phys ph, int form, con
 int check_soln_partials(int n) {
   long long N3 = (long long)(n - 4) * (n - 4) * (n - 4);
   long long b = (N3 + EB - 1) / EB;
-  return (int)(b > 152 * 8 ? 152 * 8 : b);
+  return (int)(b > 152 * 2 ? 152 * 2 : b);
 }
 
 template <typename T>
