@@ -30,21 +30,25 @@
 // out[t][a' * n*n + r] for input row r = c * n + b, i.e. contracted index
 // slowest: three products return to x-fastest order.
 //
-// Kernel: persistent, one CTA per SM looping over output tiles D[128 a' x 128 r]
-// (a'-tile fastest, so the two a'-tiles of an input tile run together and its
-// slices come from HBM once).  A = matrix slices (128 a' rows x 32 k, 64-byte
-// swizzle), B = input slices (128 r rows x 32 k), both K-major, TMA-loaded into
-// a three-stage mbarrier pipeline that runs ahead across tiles.  Warp 0 issues
-// TMA, warp 1 issues MMAs (one elected thread each) and owns the tensor memory
-// (4 classes x 128 columns; with narrower tiles, two sets alternate).  Warps
-// 2-5 run the epilogue (TMEM lane quadrant warp % 4): TMEM -> registers ->
-// FP32 stores, with the ETD update (ac_updateU_new / ch_updateU_new,
-// calc.c:489-535) or the phi2 scaling (prepare_U2_new, calc.c:553-567) fused,
-// while the next tile's copies proceed.  The operand planes per MMA set the
-// pace (nine 8 KB planes per k-block): 128-wide tiles halve the matrix-slice
-// traffic per output against 64-wide ones.  Every mbarrier wait is bounded: on
-// timeout the CTA records an error, drains its copies and MMAs (bounded),
-// frees TMEM and returns.
+// Kernel: persistent clusters of CL = 4 CTAs (one CTA per SM) looping over
+// groups of output tiles D[128 a' x 128 r]: the four CTAs of a cluster take
+// four consecutive input tiles of the same a'-tile, and each loads a share of
+// the matrix slice planes for all four by TMA multicast (the matrix operand
+// then costs a quarter of the L2 reads).  Groups go a'-tile fastest, so the
+// two a'-tiles of an input tile run together and its slices come from HBM
+// once.  A = matrix slices (128 a' rows x 32 k, 64-byte swizzle), B = input
+// slices (128 r rows x 32 k), both K-major, in a three-stage mbarrier pipeline
+// that runs ahead across tiles; a stage is refilled once all four CTAs have
+// consumed it (MMA completion is signalled to every CTA of the cluster).
+// Warp 0 issues TMA, warp 1 issues MMAs (one elected thread each) and owns the
+// tensor memory (4 classes x 128 columns).  Warps 2-5 run the epilogue (TMEM
+// lane quadrant warp % 4): the four classes of the tile are combined into
+// registers and the tensor memory is released at once, then the scaling, the
+// fused ETD update (ac_updateU_new / ch_updateU_new, calc.c:489-535) or phi2
+// scaling (prepare_U2_new, calc.c:553-567) and the FP32 stores overlap the
+// next tile's MMAs.  Every mbarrier wait is bounded: on timeout the CTA
+// records an error, drains its copies and MMAs (bounded), waits for its
+// cluster, frees TMEM and returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
@@ -69,6 +73,12 @@ constexpr int ACC_COLS = NACC * BN;   // one accumulator set
 constexpr int NBUF = 512 / ACC_COLS;   // accumulator sets in tensor memory (1 or 2)
 constexpr int TMEM_COLS = NBUF * ACC_COLS;
 constexpr int THREADS = 192;          // producer, MMA, four epilogue warps
+// CTAs per cluster: they take CL consecutive 128-wide input tiles of the same
+// a'-tile and share the matrix slices, each CTA loading some of the planes
+// for all of them (TMA multicast), which divides the L2 reads of the matrix
+// operand by CL.  The input slices stay per CTA.
+constexpr int CL = 4;
+constexpr uint16_t CL_MASK = (1u << CL) - 1;
 constexpr long long WAIT_LIMIT = 1LL << 22;  // polls (with backoff) before giving up
 static_assert(TMEM_COLS <= 512, "tensor memory holds 512 columns");
 static_assert(SMEM_BYTES <= 227 * 1024, "shared memory per CTA");
@@ -153,6 +163,43 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
   for (int j = 0; j < 32; j++) v[j] = __uint_as_float(r[j]);
 }
 
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t cluster_index() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t cluster_count() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(r));
+  return r;
+}
+// every thread of every CTA of the cluster
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+}
+// TMA load delivered to the same shared-memory offset of every CTA in mask,
+// each CTA's barrier at the same offset receiving the bytes
+__device__ __forceinline__ void tma_load_3d_mc(void *dst, const CUtensorMap *map, int x, int y, int z, uint64_t *bar,
+                                               uint16_t mask) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster [%0], [%1, {%2, "
+      "%3, %4}], [%5], %6;" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar)), "h"(mask)
+      : "memory");
+}
+// MMA completion signalled on the barrier at the same offset in every CTA of mask
+__device__ __forceinline__ void mma_commit_mc(uint64_t *bar, uint16_t mask) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+                   smem_u32(bar)),
+               "h"(mask)
+               : "memory");
+}
+
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
@@ -160,12 +207,15 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
 struct TileIdx {
   int a_tile, r_tile, t;
 };
-__device__ __forceinline__ TileIdx tile_of(int tau, int a_tiles, int r_tiles) {
+// Tile of CTA `rank` in group gam: a'-tile fastest, then the group of CL
+// input tiles, then the tensor.  The last group of a tensor may name input
+// tiles past the end: their loads read zeros and their stores are skipped.
+__device__ __forceinline__ TileIdx tile_of(int gam, int rank, int a_tiles, int r_groups) {
   TileIdx x;
-  x.a_tile = tau % a_tiles;
-  const int rest = tau / a_tiles;
-  x.r_tile = rest % r_tiles;
-  x.t = rest / r_tiles;
+  x.a_tile = gam % a_tiles;
+  const int rest = gam / a_tiles;
+  x.r_tile = (rest % r_groups) * CL + rank;
+  x.t = rest / r_groups;
   return x;
 }
 
@@ -185,13 +235,15 @@ __global__ void __launch_bounds__(THREADS, 1)
   const long long rows = (long long)g.n * g.n;
   const int a_tiles = (g.n + BM - 1) / BM;
   const int r_tiles = (int)((rows + BN - 1) / BN);
-  const int total = a_tiles * r_tiles * g.count;
+  const int r_groups = (r_tiles + CL - 1) / CL;
+  const int total = a_tiles * r_groups * g.count;  // tile groups, one per cluster pass
   const int nkb = g.kblocks;
+  const int rank = (int)cluster_rank(), cid = (int)cluster_index(), ncl = (int)cluster_count();
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; s++) {
       mbar_init(&full_bar[s], 1);
-      mbar_init(&empty_bar[s], 1);
+      mbar_init(&empty_bar[s], CL);  // consumed by the MMAs of every CTA in the cluster
     }
     for (int b = 0; b < NBUF; b++) {
       mbar_init(&tfull_bar[b], 1);
@@ -212,14 +264,19 @@ __global__ void __launch_bounds__(THREADS, 1)
   __syncthreads();
   fence_after();
   const uint32_t tmem = tmem_slot;
+  // every barrier of the cluster is initialised before any copy or arrival crosses CTAs
+  cluster_sync_all();
 
   if (warp == 0) {
     if (lane == 0) {
       // producer: five A slices and four B slices per stage, k-blocks of all
       // this CTA's tiles in one stream
+      // A stage is refilled once every CTA of the cluster has consumed it (its
+      // empty barrier counts CL arrivals): the matrix planes this CTA sends
+      // land in all of them.
       int it = 0;
-      for (int tau = blockIdx.x; tau < total; tau += gridDim.x) {
-        const TileIdx ti = tile_of(tau, a_tiles, r_tiles);
+      for (int gam = cid; gam < total; gam += ncl) {
+        const TileIdx ti = tile_of(gam, rank, a_tiles, r_groups);
         for (int kb = 0; kb < nkb; kb++, it++) {
           const int s = it % STAGES;
           if (it >= STAGES && !mbar_wait(&empty_bar[s], ((it / STAGES) & 1) ^ 1)) {
@@ -228,8 +285,10 @@ __global__ void __launch_bounds__(THREADS, 1)
           }
           if (*(volatile int *)&failed) break;
           uint8_t *st = base + s * STAGE_BYTES;
+          // this CTA's planes + the matrix planes every CTA sends to it
           mbar_expect_tx(&full_bar[s], STAGE_BYTES);
-          for (int p = 0; p < NPM; p++) tma_load_3d(st + p * PLANE_A, &tmA, kb * BK, ti.a_tile * BM, p, &full_bar[s]);
+          for (int p = rank; p < NPM; p += CL)
+            tma_load_3d_mc(st + p * PLANE_A, &tmA, kb * BK, ti.a_tile * BM, p, &full_bar[s], CL_MASK);
           for (int p = 0; p < NP; p++)
             tma_load_3d(st + NPM * PLANE_A + p * PLANE_B, &tmB, kb * BK, ti.r_tile * BN, ti.t * NP + p, &full_bar[s]);
         }
@@ -238,6 +297,12 @@ __global__ void __launch_bounds__(THREADS, 1)
       if (*(volatile int *)&failed) {
         // drain: wait (bounded) for copies still in flight into this CTA
         for (int i = it - STAGES < 0 ? 0 : it - STAGES; i < it; i++) mbar_wait(&full_bar[i % STAGES], (i / STAGES) & 1);
+      }
+      // tail: the last consumption of every stage, by every CTA of the
+      // cluster, has arrived here, so no peer signals this CTA after it exits
+      for (int s = 0; s < STAGES && s < it; s++) {
+        const int last = it - 1 - ((it - 1 - s) % STAGES);
+        if (!mbar_wait(&empty_bar[s], (last / STAGES) & 1)) failed = 1;
       }
     }
   } else if (warp == 1) {
@@ -250,7 +315,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       const int pairB[11] = {0, 3, 2, 1, 0, 2, 1, 0, 1, 0, 0};
       const int cls[11] = {3, 3, 3, 3, 3, 2, 2, 2, 1, 1, 0};
       int it = 0, j = 0;
-      for (int tau = blockIdx.x; tau < total && !*(volatile int *)&failed; tau += gridDim.x, j++) {
+      for (int gam = cid; gam < total && !*(volatile int *)&failed; gam += ncl, j++) {
         const int b = j % NBUF;
         // accumulator set b was last used by tile j - NBUF
         if (j >= NBUF && !mbar_wait(&tempty_bar[b], ((j / NBUF) & 1) ^ 1)) {
@@ -282,7 +347,7 @@ __global__ void __launch_bounds__(THREADS, 1)
               mma_bf16(acc + (uint32_t)(w * BN), da, db, idesc, start ? 0u : 1u);
             }
           }
-          mma_commit(&empty_bar[s]);
+          mma_commit_mc(&empty_bar[s], CL_MASK);
         }
         if (!ok) {
           failed = 1;
@@ -296,6 +361,10 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
   } else {
     // epilogue warps 2-5: TMEM lane quadrant q = warp % 4 holds a' rows q*32..
+    // Each tile: combine the four classes of all BN columns into registers,
+    // free the accumulators at once (the MMA warp starts the next tile), then
+    // scale, apply the fused update and store while those MMAs run.
+    __shared__ float s_isc[4][BN];  // per warp: the tile's input-row scales
     const int q = warp & 3;
     const int row = q * 32 + lane;
     // class weights 2^-b(w+2); exact integers combined small to large
@@ -303,7 +372,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                             ldexpf(1.0f, -5 * g.bits)};
     const bool vec = (rows & 3) == 0;
     int j = 0;
-    for (int tau = blockIdx.x; tau < total; tau += gridDim.x, j++) {
+    for (int gam = cid; gam < total; gam += ncl, j++) {
       const int b = j % NBUF;
       // one lane waits, the warp follows its verdict (tcgen05.ld below needs
       // the whole warp converged)
@@ -315,35 +384,44 @@ __global__ void __launch_bounds__(THREADS, 1)
         break;
       }
       fence_after();
-      const TileIdx ti = tile_of(tau, a_tiles, r_tiles);
+      float acc[BN / 32][32];
+#pragma unroll
+      for (int c = 0; c < BN / 32; c++) {
+        float w[32];
+        const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * ACC_COLS + c * 32);
+        tmem_ld32(ta + 3 * BN, acc[c]);
+#pragma unroll
+        for (int jj = 0; jj < 32; jj++) acc[c][jj] *= wt[3];
+#pragma unroll
+        for (int k = 2; k >= 0; k--) {
+          tmem_ld32(ta + k * BN, w);
+#pragma unroll
+          for (int jj = 0; jj < 32; jj++) acc[c][jj] = fmaf(w[jj], wt[k], acc[c][jj]);
+        }
+      }
+      fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&tempty_bar[b]);
+      const TileIdx ti = tile_of(gam, rank, a_tiles, r_groups);
       const int a = ti.a_tile * BM + row;
       const int kind = (ti.t % g.F) >= g.nac ? 1 : 0;
       const long long tb = (long long)ti.t * g.n * rows;
       const float sa = a < g.n ? g.row_scale[a] : 0.0f;
       const float *isc = g.in_scale + (long long)ti.t * rows;
-#pragma unroll 1
+      const long long rt0 = (long long)ti.r_tile * BN;
+      for (int i = lane; i < BN; i += 32) s_isc[q][i] = rt0 + i < rows ? isc[rt0 + i] : 0.0f;
+      __syncwarp();
+#pragma unroll
       for (int c = 0; c < BN / 32; c++) {
-        __syncwarp();
-        float v[32], w[32];
-        const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * ACC_COLS + c * 32);
-        tmem_ld32(ta + 3 * BN, v);
-#pragma unroll
-        for (int jj = 0; jj < 32; jj++) v[jj] *= wt[3];
-#pragma unroll
-        for (int k = 2; k >= 0; k--) {
-          tmem_ld32(ta + k * BN, w);
-#pragma unroll
-          for (int jj = 0; jj < 32; jj++) v[jj] = fmaf(w[jj], wt[k], v[jj]);
-        }
         if (a < g.n) {
-        const long long r0 = (long long)ti.r_tile * BN + c * 32;
+        const long long r0 = rt0 + c * 32;
         const long long o0 = (long long)a * rows + r0;  // eigen-mode [k][j][i] of a z-contraction
+        const float *si = &s_isc[q][c * 32];
         if (vec && r0 + 32 <= rows) {
 #pragma unroll
           for (int jj = 0; jj < 32; jj += 4) {
-            const float4 si = *reinterpret_cast<const float4 *>(isc + r0 + jj);
-            float4 y = make_float4(v[jj] * (si.x * sa), v[jj + 1] * (si.y * sa), v[jj + 2] * (si.z * sa),
-                                   v[jj + 3] * (si.w * sa));
+            float4 y = make_float4(acc[c][jj] * (si[jj] * sa), acc[c][jj + 1] * (si[jj + 1] * sa),
+                                   acc[c][jj + 2] * (si[jj + 2] * sa), acc[c][jj + 3] * (si[jj + 3] * sa));
             const long long o = o0 + jj;
             if (g.epi == 1) {
               const float4 uh = *reinterpret_cast<const float4 *>(g.aux + tb + o);
@@ -372,33 +450,35 @@ __global__ void __launch_bounds__(THREADS, 1)
             *dst = y;
           }
         } else {
+#pragma unroll
           for (int jj = 0; jj < 32; jj++) {
             const long long r = r0 + jj;
-            if (r >= rows) break;
-            float y = v[jj] * (isc[r] * sa);
-            const long long o = o0 + jj;
-            if (g.epi == 1) {
-              const float uh = g.aux[tb + o];
-              const float4 cc = g.coef[kind][o];
-              y = fmaf(cc.x, uh, fmaf(cc.y, uh, fmaf(cc.z, y, cc.w * y)));
-            } else if (g.epi == 2) {
-              const float2 cc = g.coef2[kind][o];
-              y = fmaf(cc.x, y, cc.y * y);
+            if (r < rows) {
+              float y = acc[c][jj] * (si[jj] * sa);
+              const long long o = o0 + jj;
+              if (g.epi == 1) {
+                const float uh = g.aux[tb + o];
+                const float4 cc = g.coef[kind][o];
+                y = fmaf(cc.x, uh, fmaf(cc.y, uh, fmaf(cc.z, y, cc.w * y)));
+              } else if (g.epi == 2) {
+                const float2 cc = g.coef2[kind][o];
+                y = fmaf(cc.x, y, cc.y * y);
+              }
+              if (g.outmode == 1) g.out[tb + o] = y;
+              else g.out[tb + o] += y;
             }
-            if (g.outmode == 1) g.out[tb + o] = y;
-            else g.out[tb + o] += y;
           }
         }
         }  // a < n
       }
-      fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&tempty_bar[b]);
+      __syncwarp();  // s_isc is rewritten for the next tile
       if (__any_sync(0xffffffffu, *(volatile int *)&failed != 0)) break;
     }
   }
   __syncthreads();
   if (threadIdx.x == 0 && failed) atomicExch(g.err, 1);
+  // no CTA leaves while a peer may still send to it
+  cluster_sync_all();
   if (warp == 1) {
     fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
@@ -640,13 +720,32 @@ cudaError_t launch_modeprod_tc(const __nv_bfloat16 *mat, const __nv_bfloat16 *pl
   g.kp = kp;
   g.kblocks = (n + tc::BK - 1) / tc::BK;
   g.bits = bits;
-  static int sms = 0;
-  if (!sms && (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0)) != cudaSuccess) return e;
-  const long long tiles = (long long)((n + tc::BM - 1) / tc::BM) * (((long long)n * n + tc::BN - 1) / tc::BN) * count;
-  if (tiles > 0x7fffffffLL) return cudaErrorInvalidValue;
-  const int grid = (int)(tiles < sms ? tiles : sms);
-  tc::modeprod_tc_kernel<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(ma, mb, g);
+  const long long r_groups = (((long long)n * n + tc::BN - 1) / tc::BN + tc::CL - 1) / tc::CL;
+  const long long groups = (long long)((n + tc::BM - 1) / tc::BM) * r_groups * count;
+  if (groups > 0x7fffffffLL) return cudaErrorInvalidValue;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = tc::CL;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.blockDim = dim3(tc::THREADS);
+  cfg.dynamicSmemBytes = tc::SMEM_BYTES;
+  cfg.stream = s;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  // persistent: as many clusters as can be resident at once
+  static int max_clusters = 0;
+  if (!max_clusters) {
+    cfg.gridDim = dim3(tc::CL * 256);
+    if ((e = cudaOccupancyMaxActiveClusters(&max_clusters, tc::modeprod_tc_kernel, &cfg)) != cudaSuccess) return e;
+    if (max_clusters < 1) return cudaErrorInvalidConfiguration;
+  }
+  const int clusters = (int)(groups < max_clusters ? groups : max_clusters);
+  cfg.gridDim = dim3(tc::CL * clusters);
+  e = cudaLaunchKernelEx(&cfg, tc::modeprod_tc_kernel, ma, mb, g);
   launch_counter()++;
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 
