@@ -30,16 +30,17 @@
 // out[t][a' * n*n + r] for input row r = c * n + b, i.e. contracted index
 // slowest: three products return to x-fastest order.
 //
-// Kernel: persistent clusters of CL = 4 CTAs (one CTA per SM) looping over
-// groups of output tiles D[128 a' x 128 r]: the four CTAs of a cluster take
-// four consecutive input tiles of the same a'-tile, and each loads a share of
-// the matrix slice planes for all four by TMA multicast (the matrix operand
-// then costs a quarter of the L2 reads).  Groups go a'-tile fastest, so the
-// two a'-tiles of an input tile run together and its slices come from HBM
-// once.  A = matrix slices (128 a' rows x 32 k, 64-byte swizzle), B = input
+// Kernel: persistent clusters of CA x 4 CTAs (one CTA per SM) looping over
+// groups of output tiles D[128 a' x 128 r]: a cluster takes four consecutive
+// input tiles of CA consecutive a'-tiles (CA = 2 for an even a'-tile count,
+// else 1).  Each CTA loads a share of the matrix slice planes for the CTAs of
+// its a'-tile and a share of the input slice planes for the CTAs of its input
+// tile, by TMA multicast: the L2 reads of the matrix operand drop by 4 and of
+// the input operand by CA, and the input slices come from HBM once.
+// A = matrix slices (128 a' rows x 32 k, 64-byte swizzle), B = input
 // slices (128 r rows x 32 k), both K-major, in a three-stage mbarrier pipeline
-// that runs ahead across tiles; a stage is refilled once all four CTAs have
-// consumed it (MMA completion is signalled to every CTA of the cluster).
+// that runs ahead across tiles; a stage is refilled once every CTA of the
+// cluster has consumed it (MMA completion is signalled to all of them).
 // Warp 0 issues TMA, warp 1 issues MMAs (one elected thread each) and owns the
 // tensor memory (4 classes x 128 columns).  Warps 2-5 run the epilogue (TMEM
 // lane quadrant warp % 4): the four classes of the tile are combined into
@@ -73,12 +74,12 @@ constexpr int ACC_COLS = NACC * BN;   // one accumulator set
 constexpr int NBUF = 512 / ACC_COLS;   // accumulator sets in tensor memory (1 or 2)
 constexpr int TMEM_COLS = NBUF * ACC_COLS;
 constexpr int THREADS = 192;          // producer, MMA, four epilogue warps
-// CTAs per cluster: they take CL consecutive 128-wide input tiles of the same
-// a'-tile and share the matrix slices, each CTA loading some of the planes
-// for all of them (TMA multicast), which divides the L2 reads of the matrix
-// operand by CL.  The input slices stay per CTA.
-constexpr int CL = 4;
-constexpr uint16_t CL_MASK = (1u << CL) - 1;
+// Cluster of CA x CR CTAs: CR consecutive 128-wide input tiles times CA
+// consecutive a'-tiles.  CTAs of the same a'-tile share the matrix slices and
+// CTAs of the same input tile share the input slices: each CTA loads a share
+// of the planes for its partners (TMA multicast), dividing the L2 reads of
+// the matrix operand by CR and of the input operand by CA.  CA = 2 when the
+// a'-tile count is even (with CR = 2), else 1 (with CR = 4): four CTAs.
 constexpr long long WAIT_LIMIT = 1LL << 22;  // polls (with backoff) before giving up
 static_assert(TMEM_COLS <= 512, "tensor memory holds 512 columns");
 static_assert(SMEM_BYTES <= 227 * 1024, "shared memory per CTA");
@@ -207,20 +208,25 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
 struct TileIdx {
   int a_tile, r_tile, t;
 };
-// Tile of CTA `rank` in group gam: a'-tile fastest, then the group of CL
-// input tiles, then the tensor.  The last group of a tensor may name input
-// tiles past the end: their loads read zeros and their stores are skipped.
-__device__ __forceinline__ TileIdx tile_of(int gam, int rank, int a_tiles, int r_groups) {
+// Tile of the CTA with a'-rank ra and r-rank rr in group gam: groups of CA
+// a'-tiles fastest, then groups of CR input tiles, then the tensor.  The last
+// group of a tensor may name input tiles past the end: their loads read zeros
+// and their stores are skipped.
+template <int CA, int CR>
+__device__ __forceinline__ TileIdx tile_of(int gam, int ra, int rr, int a_groups, int r_groups) {
   TileIdx x;
-  x.a_tile = gam % a_tiles;
-  const int rest = gam / a_tiles;
-  x.r_tile = (rest % r_groups) * CL + rank;
+  x.a_tile = (gam % a_groups) * CA + ra;
+  const int rest = gam / a_groups;
+  x.r_tile = (rest % r_groups) * CR + rr;
   x.t = rest / r_groups;
   return x;
 }
 
+template <int CA, int CR>
 __global__ void __launch_bounds__(THREADS, 1)
     modeprod_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcArgs g) {
+  constexpr int CL = CA * CR;
+  constexpr uint16_t ALL = (uint16_t)((1u << CL) - 1);
   extern __shared__ uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t full_bar[STAGES];
   __shared__ __align__(8) uint64_t empty_bar[STAGES];
@@ -235,10 +241,16 @@ __global__ void __launch_bounds__(THREADS, 1)
   const long long rows = (long long)g.n * g.n;
   const int a_tiles = (g.n + BM - 1) / BM;
   const int r_tiles = (int)((rows + BN - 1) / BN);
-  const int r_groups = (r_tiles + CL - 1) / CL;
-  const int total = a_tiles * r_groups * g.count;  // tile groups, one per cluster pass
+  const int r_groups = (r_tiles + CR - 1) / CR;
+  const int a_groups = (a_tiles + CA - 1) / CA;
+  const int total = a_groups * r_groups * g.count;  // tile groups, one per cluster pass
   const int nkb = g.kblocks;
   const int rank = (int)cluster_rank(), cid = (int)cluster_index(), ncl = (int)cluster_count();
+  const int ra = rank % CA, rr = rank / CA;
+  // partners sharing this CTA's a'-tile (matrix planes) and input tile (input planes)
+  uint16_t mask_a = 0, mask_b = 0;
+  for (int k = 0; k < CR; k++) mask_a |= (uint16_t)(1u << (ra + CA * k));
+  for (int k = 0; k < CA; k++) mask_b |= (uint16_t)(1u << (k + CA * rr));
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; s++) {
@@ -272,11 +284,11 @@ __global__ void __launch_bounds__(THREADS, 1)
       // producer: five A slices and four B slices per stage, k-blocks of all
       // this CTA's tiles in one stream
       // A stage is refilled once every CTA of the cluster has consumed it (its
-      // empty barrier counts CL arrivals): the matrix planes this CTA sends
-      // land in all of them.
+      // empty barrier counts CL arrivals): the planes this CTA sends land in
+      // its partners.
       int it = 0;
       for (int gam = cid; gam < total; gam += ncl) {
-        const TileIdx ti = tile_of(gam, rank, a_tiles, r_groups);
+        const TileIdx ti = tile_of<CA, CR>(gam, ra, rr, a_groups, r_groups);
         for (int kb = 0; kb < nkb; kb++, it++) {
           const int s = it % STAGES;
           if (it >= STAGES && !mbar_wait(&empty_bar[s], ((it / STAGES) & 1) ^ 1)) {
@@ -287,10 +299,15 @@ __global__ void __launch_bounds__(THREADS, 1)
           uint8_t *st = base + s * STAGE_BYTES;
           // this CTA's planes + the matrix planes every CTA sends to it
           mbar_expect_tx(&full_bar[s], STAGE_BYTES);
-          for (int p = rank; p < NPM; p += CL)
-            tma_load_3d_mc(st + p * PLANE_A, &tmA, kb * BK, ti.a_tile * BM, p, &full_bar[s], CL_MASK);
-          for (int p = 0; p < NP; p++)
-            tma_load_3d(st + NPM * PLANE_A + p * PLANE_B, &tmB, kb * BK, ti.r_tile * BN, ti.t * NP + p, &full_bar[s]);
+          for (int p = rr; p < NPM; p += CR)
+            tma_load_3d_mc(st + p * PLANE_A, &tmA, kb * BK, ti.a_tile * BM, p, &full_bar[s], mask_a);
+          for (int p = ra; p < NP; p += CA) {
+            if (CA == 1)
+              tma_load_3d(st + NPM * PLANE_A + p * PLANE_B, &tmB, kb * BK, ti.r_tile * BN, ti.t * NP + p, &full_bar[s]);
+            else
+              tma_load_3d_mc(st + NPM * PLANE_A + p * PLANE_B, &tmB, kb * BK, ti.r_tile * BN, ti.t * NP + p,
+                             &full_bar[s], mask_b);
+          }
         }
         if (*(volatile int *)&failed) break;
       }
@@ -347,7 +364,7 @@ __global__ void __launch_bounds__(THREADS, 1)
               mma_bf16(acc + (uint32_t)(w * BN), da, db, idesc, start ? 0u : 1u);
             }
           }
-          mma_commit_mc(&empty_bar[s], CL_MASK);
+          mma_commit_mc(&empty_bar[s], ALL);
         }
         if (!ok) {
           failed = 1;
@@ -402,7 +419,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&tempty_bar[b]);
-      const TileIdx ti = tile_of(gam, rank, a_tiles, r_groups);
+      const TileIdx ti = tile_of<CA, CR>(gam, ra, rr, a_groups, r_groups);
       const int a = ti.a_tile * BM + row;
       const int kind = (ti.t % g.F) >= g.nac ? 1 : 0;
       const long long tb = (long long)ti.t * g.n * rows;
@@ -701,12 +718,14 @@ cudaError_t launch_modeprod_tc(const __nv_bfloat16 *mat, const __nv_bfloat16 *pl
                                cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(tc::modeprod_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         tc::SMEM_BYTES);
-    if (e != cudaSuccess) return e;
-    // all of the unified L1/shared capacity as shared memory: two CTAs per SM
-    e = cudaFuncSetAttribute(tc::modeprod_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    if (e != cudaSuccess) return e;
+    // all of the unified L1/shared capacity as shared memory
+    for (int ca = 1; ca <= 2; ca++) {
+      const void *fn = ca == 2 ? (const void *)tc::modeprod_tc_kernel<2, 2> : (const void *)tc::modeprod_tc_kernel<1, 4>;
+      cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
+      if (e != cudaSuccess) return e;
+      e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+      if (e != cudaSuccess) return e;
+    }
     attr = true;
   }
   const int n = args.n, kp = tc_kp(n);
@@ -720,13 +739,17 @@ cudaError_t launch_modeprod_tc(const __nv_bfloat16 *mat, const __nv_bfloat16 *pl
   g.kp = kp;
   g.kblocks = (n + tc::BK - 1) / tc::BK;
   g.bits = bits;
-  const long long r_groups = (((long long)n * n + tc::BN - 1) / tc::BN + tc::CL - 1) / tc::CL;
-  const long long groups = (long long)((n + tc::BM - 1) / tc::BM) * r_groups * count;
+  const int a_tiles = (n + tc::BM - 1) / tc::BM;
+  const int CA = a_tiles % 2 == 0 ? 2 : 1;
+  const int CR = CA == 2 ? 2 : 4;
+  const int CL = CA * CR;
+  const long long r_groups = (((long long)n * n + tc::BN - 1) / tc::BN + CR - 1) / CR;
+  const long long groups = (long long)((a_tiles + CA - 1) / CA) * r_groups * count;
   if (groups > 0x7fffffffLL) return cudaErrorInvalidValue;
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
-  at[0].val.clusterDim.x = tc::CL;
+  at[0].val.clusterDim.x = CL;
   at[0].val.clusterDim.y = 1;
   at[0].val.clusterDim.z = 1;
   cfg.blockDim = dim3(tc::THREADS);
@@ -735,15 +758,18 @@ cudaError_t launch_modeprod_tc(const __nv_bfloat16 *mat, const __nv_bfloat16 *pl
   cfg.attrs = at;
   cfg.numAttrs = 1;
   // persistent: as many clusters as can be resident at once
-  static int max_clusters = 0;
-  if (!max_clusters) {
-    cfg.gridDim = dim3(tc::CL * 256);
-    if ((e = cudaOccupancyMaxActiveClusters(&max_clusters, tc::modeprod_tc_kernel, &cfg)) != cudaSuccess) return e;
-    if (max_clusters < 1) return cudaErrorInvalidConfiguration;
+  static int max_clusters[3] = {0, 0, 0};
+  if (!max_clusters[CA]) {
+    cfg.gridDim = dim3(CL * 128);
+    e = CA == 2 ? cudaOccupancyMaxActiveClusters(&max_clusters[CA], tc::modeprod_tc_kernel<2, 2>, &cfg)
+                : cudaOccupancyMaxActiveClusters(&max_clusters[CA], tc::modeprod_tc_kernel<1, 4>, &cfg);
+    if (e != cudaSuccess) return e;
+    if (max_clusters[CA] < 1) return cudaErrorInvalidConfiguration;
   }
-  const int clusters = (int)(groups < max_clusters ? groups : max_clusters);
-  cfg.gridDim = dim3(tc::CL * clusters);
-  e = cudaLaunchKernelEx(&cfg, tc::modeprod_tc_kernel, ma, mb, g);
+  const int clusters = (int)(groups < max_clusters[CA] ? groups : max_clusters[CA]);
+  cfg.gridDim = dim3(CL * clusters);
+  e = CA == 2 ? cudaLaunchKernelEx(&cfg, tc::modeprod_tc_kernel<2, 2>, ma, mb, g)
+              : cudaLaunchKernelEx(&cfg, tc::modeprod_tc_kernel<1, 4>, ma, mb, g);
   launch_counter()++;
   if (e != cudaSuccess) return e;
   return cudaGetLastError();
