@@ -187,7 +187,6 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(typename Cx<T>::t *data0
   int Ns = 1;
   for (int st = 0; st < rad.count; st++) {
     const int R = rad.r[st];
-    const int nb = N / R;
     const float inb = sd.inv_nb[st], ins = sd.inv_ns[st];
     switch (R) {
       case 4: fft_stage<4, C>(src, dst, tile, N, Ns, inb, ins, tw, sign); break;

@@ -14,6 +14,7 @@
 
 #include <string>
 #include <vector>
+#include <sys/stat.h>
 
 #include "sclet_gb300.h"
 #include "sclet_internal.cuh"
@@ -517,6 +518,72 @@ int sclet_get_field(sclet_ctx *ctx, int kind, int m, double *block) {
   if (f < 0) return fail(ctx, SCLET_ERR_ARG, "no such field");
   return mixed(ctx) ? get_block(ctx, nullptr, fu_of(ctx) + f * ctx->n3, block, f >= ctx->nac ? ctx->ph.cshift : 0.0)
                     : get_block(ctx, u_of(ctx) + f * ctx->n3, nullptr, block);
+}
+
+// the rank's sub-directory "<dir>00/" of the alpha driver's files
+static void make_rank_dir(const char *dir) { mkdir((std::string(dir) + "00").c_str(), 0755); }
+
+int sclet_write_chk(sclet_ctx *ctx, const char *dir, int chk, int irun) {
+  std::vector<double> blk(ctx->n3);
+  char path[4096];
+  make_rank_dir(dir);
+  for (int m = 0; m < ctx->nac; m++) {
+    int rc = sclet_get_field(ctx, SCLET_AC, m, blk.data());
+    if (rc != SCLET_OK) return rc;
+    if (sclet_chk_path(path, sizeof path, dir, m, chk) != SCLET_OK) return fail(ctx, SCLET_ERR_ARG, "path too long");
+    if (sclet_write_chk_file(path, irun, ctx->n, blk.data()) != SCLET_OK)
+      return fail(ctx, SCLET_ERR_IO, std::string("cannot write ") + path);
+  }
+  return SCLET_OK;
+}
+
+int sclet_read_chk(sclet_ctx *ctx, const char *dir, int chk, int *irun) {
+  std::vector<double> blk(ctx->n3);
+  char path[4096];
+  for (int m = 0; m < ctx->nac; m++) {
+    if (sclet_chk_path(path, sizeof path, dir, m, chk) != SCLET_OK) return fail(ctx, SCLET_ERR_ARG, "path too long");
+    if (sclet_read_chk_file(path, ctx->n, irun, blk.data()) != SCLET_OK)
+      return fail(ctx, SCLET_ERR_IO, std::string("cannot read checkpoint ") + path);
+    int rc = sclet_set_field(ctx, SCLET_AC, m, blk.data());
+    if (rc != SCLET_OK) return rc;
+  }
+  return SCLET_OK;
+}
+
+int sclet_field_u16(sclet_ctx *ctx, int kind, int m, unsigned short *out) {
+  int f = field_index(ctx, kind, m);
+  if (f < 0) return fail(ctx, SCLET_ERR_ARG, "no such field");
+  const int k = kind == SCLET_CH ? 1 : 0;
+  // the work block of the context holds the codes (no step is in flight between calls)
+  unsigned short *dev = mixed(ctx) ? reinterpret_cast<unsigned short *>(ctx->fscratch)
+                                   : reinterpret_cast<unsigned short *>(ctx->scratch);
+  if (mixed(ctx))
+    CK(launch_field_u16<float>(fu_of(ctx) + f * ctx->n3, k, f >= ctx->nac ? ctx->ph.cshift : 0.0, ctx->n3, dev,
+                               ctx->stream));
+  else
+    CK(launch_field_u16<double>(u_of(ctx) + f * ctx->n3, k, 0.0, ctx->n3, dev, ctx->stream));
+  CK(cudaMemcpyAsync(out, dev, sizeof(unsigned short) * ctx->n3, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return SCLET_OK;
+}
+
+int sclet_write_field2b(sclet_ctx *ctx, const char *data_dir, int irun, int mode) {
+  if (mode != 0 && mode != 1) return fail(ctx, SCLET_ERR_ARG, "mode must be 0 (order parameters) or 1 (concentrations)");
+  const int kind = mode == 0 ? SCLET_AC : SCLET_CH, count = mode == 0 ? ctx->nac : ctx->nch;
+  std::vector<unsigned short> codes(ctx->n3);
+  char path[4096];
+  make_rank_dir(data_dir);
+  for (int m = 0; m < count; m++) {
+    int rc = sclet_field_u16(ctx, kind, m, codes.data());
+    if (rc != SCLET_OK) return rc;
+    if (sclet_field2b_path(path, sizeof path, data_dir, kind, m, irun) != SCLET_OK)
+      return fail(ctx, SCLET_ERR_ARG, "path too long");
+    FILE *fp = fopen(path, "wb");
+    if (!fp) return fail(ctx, SCLET_ERR_IO, std::string("cannot write ") + path);
+    const bool ok = fwrite(codes.data(), sizeof(unsigned short), codes.size(), fp) == codes.size();
+    if (fclose(fp) != 0 || !ok) return fail(ctx, SCLET_ERR_IO, std::string("cannot write ") + path);
+  }
+  return SCLET_OK;
 }
 
 int sclet_load_restart(sclet_ctx *ctx, int kind, int m, const char *path) {

@@ -137,6 +137,11 @@ cudaError_t mass_target(const float *a, const double *wa, const float *b, const 
 // shifts the owned cells of u so that their sum meets the target partials
 cudaError_t mass_fix(float *u, int n, const double *tpart, double *apart, double *res, cudaStream_t s);
 
+// 16-bit codes of one field block (see k_codec.cu); kind 0 AC, 1 CH; the
+// stored values plus shift are the field's values.
+template <typename T>
+cudaError_t launch_field_u16(const T *u, int kind, double shift, long long cells, unsigned short *out, cudaStream_t s);
+
 // Counts kernel launches issued by this library (per process).
 long long &launch_counter();
 

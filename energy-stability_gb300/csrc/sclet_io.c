@@ -210,3 +210,43 @@ int sclet_read_restart(const char *path, int n, double *block) {
   fclose(f);
   return ok ? SCLET_OK : SCLET_ERR_IO;
 }
+
+/* ---- checkpoint and 16-bit field files (the alpha driver's output) ------ */
+
+/* File names of one block: the rank's z coordinate names a sub-directory and
+ * the three coordinates end the name (vars.c:975 and :1079 of
+ * source_beta_to_alpha/src); a single block is rank (0, 0, 0). */
+int sclet_chk_path(char *out, size_t len, const char *dir, int m, int chk) {
+  int w = snprintf(out, len, "%s%02d/eta%d_chk%d_%02d%02d%02d.dat", dir, 0, m, chk, 0, 0, 0);
+  return (w < 0 || (size_t)w >= len) ? SCLET_ERR_ARG : SCLET_OK;
+}
+
+int sclet_field2b_path(char *out, size_t len, const char *dir, int kind, int m, int irun) {
+  int w = snprintf(out, len, "%s%02d/%s%d_%06d_%02d%02d%02d.dat", dir, 0, kind == SCLET_CH ? "c" : "eta", m, irun, 0,
+                   0, 0);
+  return (w < 0 || (size_t)w >= len) ? SCLET_ERR_ARG : SCLET_OK;
+}
+
+/* write_chk (vars.c:966-989): the step counter as one int, then every cell of
+ * the n^3 block (ghost layers included) as a double, native byte order. */
+int sclet_write_chk_file(const char *path, int irun, int n, const double *block) {
+  FILE *f = fopen(path, "wb");
+  size_t cells = (size_t)n * n * n;
+  int ok;
+  if (!f) return SCLET_ERR_IO;
+  ok = fwrite(&irun, sizeof(int), 1, f) == 1 && fwrite(block, sizeof(double), cells, f) == cells;
+  ok &= fclose(f) == 0;
+  return ok ? SCLET_OK : SCLET_ERR_IO;
+}
+
+/* read_chk (vars.c:1012-1035).  A file shorter than the block is an error
+ * (the reference reads past its end unchecked). */
+int sclet_read_chk_file(const char *path, int n, int *irun, double *block) {
+  FILE *f = fopen(path, "rb");
+  size_t cells = (size_t)n * n * n;
+  int ok;
+  if (!f) return SCLET_ERR_IO;
+  ok = fread(irun, sizeof(int), 1, f) == 1 && fread(block, sizeof(double), cells, f) == cells;
+  fclose(f);
+  return ok ? SCLET_OK : SCLET_ERR_IO;
+}

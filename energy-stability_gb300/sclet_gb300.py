@@ -65,6 +65,15 @@ SIGNATURES = {
                                              ctypes.c_double, ctypes.c_double]),
     "sclet_write_restart": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, _c_dp]),
     "sclet_read_restart": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, _c_dp]),
+    "sclet_write_chk_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, _c_dp]),
+    "sclet_read_chk_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int), _c_dp]),
+    "sclet_chk_path": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_int, ctypes.c_int]),
+    "sclet_field2b_path": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_int,
+                                          ctypes.c_int, ctypes.c_int]),
+    "sclet_write_chk": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int]),
+    "sclet_read_chk": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+    "sclet_field_u16": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
+    "sclet_write_field2b": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int]),
     "sclet_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
     "sclet_destroy": (None, [ctypes.c_void_p]),
     "sclet_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
@@ -250,6 +259,25 @@ class Solver:
         d = (Diag * self.F)()
         self._ck(self.L.sclet_check_soln(self.h, form, d), "check_soln")
         return np.array([[x.max, x.min, x.vol, x.energy] for x in d])
+
+    def write_chk(self, directory: str, chk: int, irun: int):
+        """write_chk of the alpha driver: one checkpoint file per order parameter."""
+        self._ck(self.L.sclet_write_chk(self.h, directory.encode(), chk, irun), "write_chk")
+
+    def read_chk(self, directory: str, chk: int) -> int:
+        irun = ctypes.c_int()
+        self._ck(self.L.sclet_read_chk(self.h, directory.encode(), chk, ctypes.byref(irun)), "read_chk")
+        return irun.value
+
+    def field_u16(self, f: int) -> np.ndarray:
+        """16-bit codes of field f (AC fields first), as Dtype2B_E / Dtype2B_CI."""
+        k, m = self._kind(f)
+        out = np.zeros((self.n, self.n, self.n), dtype=np.uint16)
+        self._ck(self.L.sclet_field_u16(self.h, k, m, out.ctypes.data_as(ctypes.c_void_p)), "field_u16")
+        return out
+
+    def write_field2b(self, data_dir: str, irun: int, mode: int = 0):
+        self._ck(self.L.sclet_write_field2b(self.h, data_dir.encode(), irun, mode), "write_field2b")
 
     def set_step_diagnostics(self, form: int = 1):
         """Queue check_soln_new after every step (form -1: none)."""

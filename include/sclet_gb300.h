@@ -112,6 +112,19 @@ double sclet_seeded_value(unsigned long long seed, int field, long long cell, do
  * field.c:156-174) / reads it (read_field, field.c:137-154). */
 int sclet_write_restart(const char *path, int n, const double *block);
 int sclet_read_restart(const char *path, int n, double *block);
+/* Checkpoint files of the alpha driver (source_beta_to_alpha/src/vars.c):
+ * write_chk (:966-989) writes, per order parameter, the step counter as one
+ * int and then every cell of the n^3 block, ghost layers included, as
+ * doubles in native byte order; read_chk (:1012-1035) reads them back (a
+ * short file is an error here).  File names: sclet_chk_path gives
+ * "<dir>00/eta<m>_chk<chk>_000000.dat" (rank (0, 0, 0) of one block, the
+ * rank's z coordinate naming the sub-directory, vars.c:975), and
+ * sclet_field2b_path gives "<dir>00/eta<m>_<irun:06d>_000000.dat" (or
+ * "c<m>_..." for a concentration) for the 16-bit files (vars.c:1079). */
+int sclet_write_chk_file(const char *path, int irun, int n, const double *block);
+int sclet_read_chk_file(const char *path, int n, int *irun, double *block);
+int sclet_chk_path(char *out, size_t len, const char *dir, int m, int chk);
+int sclet_field2b_path(char *out, size_t len, const char *dir, int kind, int m, int irun);
 
 /* ---- context ----------------------------------------------------------- */
 /* alloc_vars (vars.c:166-300), init_para (vars.c:58-157), read_matrices
@@ -171,6 +184,23 @@ int sclet_last_diagnostics(sclet_ctx *ctx, sclet_diag *out);
  * default is the gradient operator of the dynamics: lambda_file when
  * anisotropic, else diag(kk). */
 int sclet_set_energy_tensors(sclet_ctx *ctx, const double *lam /* nac*9 */);
+
+/* ---- checkpoint and 16-bit output files (the alpha driver's formats) ---- */
+/* write_chk / read_chk (source_beta_to_alpha/src/vars.c:966-1035) for every
+ * order parameter of the context, under dir (the reference's work_dir; the
+ * rank sub-directory "00" is created when missing).  The reference's
+ * concentration checkpoints are compiled out (vars.c:990-1010), so are these. */
+int sclet_write_chk(sclet_ctx *ctx, const char *dir, int chk, int irun);
+int sclet_read_chk(sclet_ctx *ctx, const char *dir, int chk, int *irun);
+/* Dtype2B_E / Dtype2B_CI (anisotropic_hip.c:3920-3944): the 16-bit code of
+ * every cell of one field's n^3 block into out (n^3 host values): order
+ * parameters (eta + 0.1) * 30000, concentrations c * 50000, computed in FP64
+ * and truncated toward zero.  The reference's conversion is undefined outside
+ * [0, 65535]; these codes saturate there. */
+int sclet_field_u16(sclet_ctx *ctx, int kind, int m, unsigned short *out);
+/* write_field2B (vars.c:1066-1116): the codes of every order parameter
+ * (mode 0) or concentration (mode 1) as raw 16-bit files under data_dir. */
+int sclet_write_field2b(sclet_ctx *ctx, const char *data_dir, int irun, int mode);
 
 /* ---- inspection (host buffers) ------------------------------------------ */
 /* fieldE1/fieldE2 of one field, and the elastic force felas.  In the mixed

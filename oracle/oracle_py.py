@@ -211,3 +211,20 @@ class Oracle:
 
     def threads(self) -> int:
         return self.lib.orc_threads()
+
+
+# ---- the alpha driver's output formats (restated; its HIP code cannot run here) ----
+
+def chk_file_bytes(irun: int, block: np.ndarray) -> bytes:
+    """write_chk (source_beta_to_alpha/src/vars.c:966-989): the step counter
+    as a native int, then every cell of the block as native doubles."""
+    return np.array([irun], dtype=np.int32).tobytes() + np.ascontiguousarray(block, dtype=np.float64).tobytes()
+
+
+def field2b_codes(kind: int, block: np.ndarray) -> np.ndarray:
+    """Dtype2B_E / Dtype2B_CI (source_beta_to_alpha/src/anisotropic_hip.c:
+    3920-3944): (eta + 0.1) * 30000 for order parameters (kind 0), c * 50000
+    for concentrations (kind 1), truncated toward zero to unsigned short.
+    Defined by the reference only inside [0, 65535]; callers keep to that."""
+    v = (block + 0.1) * 30000.0 if kind == 0 else block * 50000.0
+    return np.trunc(v).astype(np.uint16)
