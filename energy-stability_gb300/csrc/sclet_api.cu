@@ -586,6 +586,32 @@ int sclet_write_field2b(sclet_ctx *ctx, const char *data_dir, int irun, int mode
   return SCLET_OK;
 }
 
+int sclet_log_soln(sclet_ctx *ctx, const char *work_dir, int iter, int energy_form) {
+  std::vector<sclet_diag> d(ctx->nac + ctx->nch);
+  int rc = sclet_check_soln(ctx, energy_form, d.data());
+  if (rc != SCLET_OK) return rc;
+  double couple = d[0].energy;
+  if (energy_form != 1 && ctx->nac > 0 && ctx->nch > 0) {
+    std::vector<sclet_diag> t(d.size());
+    if ((rc = sclet_check_soln(ctx, 1, t.data())) != SCLET_OK) return rc;
+    couple = t[0].energy;
+  }
+  if (sclet_append_soln_log(work_dir, iter, ctx->nac, ctx->nch, d.data(), &couple) != SCLET_OK)
+    return fail(ctx, SCLET_ERR_IO, std::string("cannot append the diagnostics logs under ") + work_dir);
+  return SCLET_OK;
+}
+
+int sclet_write_vtk(sclet_ctx *ctx, const char *path, int istep) {
+  std::vector<double> blk((size_t)ctx->nac * ctx->n3);
+  for (int m = 0; m < ctx->nac; m++) {
+    int rc = sclet_get_field(ctx, SCLET_AC, m, blk.data() + (size_t)m * ctx->n3);
+    if (rc != SCLET_OK) return rc;
+  }
+  if (sclet_write_vtk_file(path, istep, ctx->n, ctx->nac, blk.data()) != SCLET_OK)
+    return fail(ctx, SCLET_ERR_IO, std::string("cannot write ") + path);
+  return SCLET_OK;
+}
+
 int sclet_load_restart(sclet_ctx *ctx, int kind, int m, const char *path) {
   std::vector<double> blk(ctx->n3, 0.0);
   int f = field_index(ctx, kind, m);

@@ -250,3 +250,68 @@ int sclet_read_chk_file(const char *path, int n, int *irun, double *block) {
   fclose(f);
   return ok ? SCLET_OK : SCLET_ERR_IO;
 }
+
+/* ---- plain-text VTK of the order parameters (post-processing) ---------- */
+/* The layout of visualisation/write_vtk.py:57-101: a legacy ASCII structured grid
+ * of the whole n^3 block, points listed with x fastest and written as
+ * (z, y, x), then one float scalar block "eta<m>" per field, every value in
+ * %14.6e. */
+int sclet_write_vtk_file(const char *path, int istep, int n, int nfields, const double *blocks) {
+  FILE *f = fopen(path, "w");
+  const size_t cells = (size_t)n * n * n;
+  int x, y, z, m, ok = 1;
+  size_t l;
+  if (!f) return SCLET_ERR_IO;
+  ok &= fprintf(f, "# vtk DataFile Version 2.0\ntime_%d.vtk\nASCII\nDATASET STRUCTURED_GRID\n", istep) > 0;
+  ok &= fprintf(f, "DIMENSIONS %5d  %5d  %5d\n", n, n, n) > 0;
+  ok &= fprintf(f, "POINTS %7zu float\n", cells) > 0;
+  for (z = 0; z < n && ok; z++)
+    for (y = 0; y < n; y++)
+      for (x = 0; x < n; x++) ok &= fprintf(f, "%14.6e   %14.6e   %14.6e\n", (double)z, (double)y, (double)x) > 0;
+  ok &= fprintf(f, "POINT_DATA %5zu\n", cells) > 0;
+  for (m = 0; m < nfields && ok; m++) {
+    ok &= fprintf(f, "SCALARS eta%d  float  1\nLOOKUP_TABLE default\n", m) > 0;
+    for (l = 0; l < cells && ok; l++) ok &= fprintf(f, "%14.6e\n", blocks[(size_t)m * cells + l]) > 0;
+  }
+  ok &= fclose(f) == 0;
+  return ok ? SCLET_OK : SCLET_ERR_IO;
+}
+
+/* ---- diagnostics logs of check_soln_new (field.c:419-455, 524, 591, 647) --- */
+/* One row per field "iter,max,min,vol,eng" appended to phi_ac_<m>.csv /
+ * phi_ch_<m>.csv under work_dir, and "iter,eng" to phi_couple.csv when couple
+ * is given; iter 0 starts each file with its header line. */
+static int soln_row(const char *path, int iter, const char *header, const double *v, int nv) {
+  FILE *f;
+  int ok = 1, k;
+  if (iter == 0) {
+    f = fopen(path, "w");
+    if (!f) return SCLET_ERR_IO;
+    ok &= fprintf(f, "%s\n", header) > 0;
+    ok &= fclose(f) == 0;
+    if (!ok) return SCLET_ERR_IO;
+  }
+  f = fopen(path, "a");
+  if (!f) return SCLET_ERR_IO;
+  ok &= fprintf(f, "%d", iter) > 0;
+  for (k = 0; k < nv; k++) ok &= fprintf(f, ",%+1.15f", v[k]) > 0;
+  ok &= fprintf(f, "\n") > 0;
+  ok &= fclose(f) == 0;
+  return ok ? SCLET_OK : SCLET_ERR_IO;
+}
+
+int sclet_append_soln_log(const char *work_dir, int iter, int nac, int nch, const sclet_diag *d, const double *couple) {
+  char path[4096];
+  int m, rc;
+  if (couple && nac > 0 && nch > 0) {
+    snprintf(path, sizeof path, "%sphi_couple.csv", work_dir);
+    if ((rc = soln_row(path, iter, "iter,eng", couple, 1)) != SCLET_OK) return rc;
+  }
+  for (m = 0; m < nac + nch; m++) {
+    const double v[4] = {d[m].max, d[m].min, d[m].vol, d[m].energy};
+    snprintf(path, sizeof path, m < nac ? "%sphi_ac_%d.csv" : "%sphi_ch_%d.csv", work_dir, m < nac ? m : m - nac);
+    rc = soln_row(path, iter, m < nac ? "iter,maxphiE,minphiE,volE,engE" : "iter,maxphiCI,minphiCI,volCI,engCI", v, 4);
+    if (rc != SCLET_OK) return rc;
+  }
+  return SCLET_OK;
+}

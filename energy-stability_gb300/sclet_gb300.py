@@ -70,6 +70,10 @@ SIGNATURES = {
     "sclet_chk_path": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_int, ctypes.c_int]),
     "sclet_field2b_path": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_int,
                                           ctypes.c_int, ctypes.c_int]),
+    "sclet_write_vtk_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _c_dp]),
+    "sclet_write_vtk": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]),
+    "sclet_append_soln_log": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _c_dp, _c_dp]),
+    "sclet_log_soln": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int]),
     "sclet_write_chk": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int]),
     "sclet_read_chk": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     "sclet_field_u16": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
@@ -275,6 +279,12 @@ class Solver:
         out = np.zeros((self.n, self.n, self.n), dtype=np.uint16)
         self._ck(self.L.sclet_field_u16(self.h, k, m, out.ctypes.data_as(ctypes.c_void_p)), "field_u16")
         return out
+
+    def log_soln(self, work_dir: str, iter_: int, energy_form: int = 1):
+        self._ck(self.L.sclet_log_soln(self.h, work_dir.encode(), iter_, energy_form), "log_soln")
+
+    def write_vtk(self, path: str, istep: int):
+        self._ck(self.L.sclet_write_vtk(self.h, path.encode(), istep), "write_vtk")
 
     def write_field2b(self, data_dir: str, irun: int, mode: int = 0):
         self._ck(self.L.sclet_write_field2b(self.h, data_dir.encode(), irun, mode), "write_field2b")

@@ -125,6 +125,10 @@ int sclet_write_chk_file(const char *path, int irun, int n, const double *block)
 int sclet_read_chk_file(const char *path, int n, int *irun, double *block);
 int sclet_chk_path(char *out, size_t len, const char *dir, int m, int chk);
 int sclet_field2b_path(char *out, size_t len, const char *dir, int kind, int m, int irun);
+/* Plain-text VTK of nfields blocks (visualisation/write_vtk.py): a legacy
+ * ASCII structured grid of the whole n^3 block, points with x fastest written
+ * as (z, y, x), one float scalar block "eta<m>" per field, values in %14.6e. */
+int sclet_write_vtk_file(const char *path, int istep, int n, int nfields, const double *blocks);
 
 /* ---- context ----------------------------------------------------------- */
 /* alloc_vars (vars.c:166-300), init_para (vars.c:58-157), read_matrices
@@ -184,6 +188,18 @@ int sclet_last_diagnostics(sclet_ctx *ctx, sclet_diag *out);
  * default is the gradient operator of the dynamics: lambda_file when
  * anisotropic, else diag(kk). */
 int sclet_set_energy_tensors(sclet_ctx *ctx, const double *lam /* nac*9 */);
+/* The log files of check_soln_new (field.c:419-455, 524, 591, 647): under
+ * work_dir, one row "iter,max,min,vol,eng" (%+1.15f) per field appended to
+ * phi_ac_<m>.csv / phi_ch_<m>.csv, and "iter,eng" to phi_couple.csv when
+ * couple is non-NULL and both kinds are present; iter 0 starts each file with
+ * the reference's header line.  d has nac + nch entries, AC fields first. */
+int sclet_append_soln_log(const char *work_dir, int iter, int nac, int nch, const sclet_diag *d, const double *couple);
+/* sclet_check_soln(energy_form) of the context written as those logs; the
+ * coupled energy is the plugin's total free energy (energy_form 1).  The
+ * reference's coupled sum takes the gradients of the first nch AC fields
+ * only (field.c:608-636); here it takes all of them, as the energy the
+ * scheme decreases. */
+int sclet_log_soln(sclet_ctx *ctx, const char *work_dir, int iter, int energy_form);
 
 /* ---- checkpoint and 16-bit output files (the alpha driver's formats) ---- */
 /* write_chk / read_chk (source_beta_to_alpha/src/vars.c:966-1035) for every
@@ -201,6 +217,8 @@ int sclet_field_u16(sclet_ctx *ctx, int kind, int m, unsigned short *out);
 /* write_field2B (vars.c:1066-1116): the codes of every order parameter
  * (mode 0) or concentration (mode 1) as raw 16-bit files under data_dir. */
 int sclet_write_field2b(sclet_ctx *ctx, const char *data_dir, int irun, int mode);
+/* The order parameters of the context as one VTK file (sclet_write_vtk_file). */
+int sclet_write_vtk(sclet_ctx *ctx, const char *path, int istep);
 
 /* ---- inspection (host buffers) ------------------------------------------ */
 /* fieldE1/fieldE2 of one field, and the elastic force felas.  In the mixed

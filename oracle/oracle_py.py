@@ -228,3 +228,44 @@ def field2b_codes(kind: int, block: np.ndarray) -> np.ndarray:
     Defined by the reference only inside [0, 65535]; callers keep to that."""
     v = (block + 0.1) * 30000.0 if kind == 0 else block * 50000.0
     return np.trunc(v).astype(np.uint16)
+
+
+def vtk_text(istep: int, blocks: np.ndarray) -> str:
+    """The VTK layout of visualisation/write_vtk.py:57-101, restated: legacy ASCII
+    structured grid of the whole block, points with x fastest written as
+    (z, y, x) with 14-wide six-digit exponent format, then one float scalar
+    block per field named eta0, eta1, ..."""
+    nf, n = blocks.shape[0], blocks.shape[1]
+    cells = n ** 3
+    out = ["# vtk DataFile Version 2.0", f"time_{istep:d}.vtk", "ASCII", "DATASET STRUCTURED_GRID",
+           f"DIMENSIONS {n:>5d}  {n:>5d}  {n:>5d}", f"POINTS {cells:>7d} float"]
+    z, y, x = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    for a, b, c in zip(z.ravel(), y.ravel(), x.ravel()):
+        out.append(f"{float(a):>14.6e}   {float(b):>14.6e}   {float(c):>14.6e}")
+    out.append(f"POINT_DATA {cells:>5d}")
+    for m in range(nf):
+        out.append(f"SCALARS eta{m}  float  1")
+        out.append("LOOKUP_TABLE default")
+        out.extend(f"{v:>14.6e}" for v in blocks[m].ravel())
+    return "\n".join(out) + "\n"
+
+
+def soln_log_rows(iter_: int, nac: int, nch: int, d: np.ndarray, couple=None) -> Dict[str, str]:
+    """The lines check_soln_new (source_beta_to_omega/src/field.c:419-455, 524,
+    591, 647) adds to its log files for one call, restated: file name -> text.
+    d holds (max, min, vol, eng) per field, AC fields first; iter 0 starts each
+    file with its header line."""
+    out = {}
+
+    def row(name, header, vals):
+        text = (header + "\n") if iter_ == 0 else ""
+        out[name] = text + str(iter_) + "".join(f",{v:+.15f}" for v in vals) + "\n"
+
+    if couple is not None and nac > 0 and nch > 0:
+        row("phi_couple.csv", "iter,eng", [couple])
+    for m in range(nac + nch):
+        if m < nac:
+            row(f"phi_ac_{m}.csv", "iter,maxphiE,minphiE,volE,engE", d[m])
+        else:
+            row(f"phi_ch_{m - nac}.csv", "iter,maxphiCI,minphiCI,volCI,engCI", d[m])
+    return out

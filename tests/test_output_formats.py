@@ -94,3 +94,64 @@ def test_checkpoint_and_field2b_files(sclet_lib, tmp_path):
         assert np.array_equal(got[m], want[m])
     a.close()
     b.close()
+
+
+def test_vtk_file_matches_restated_script(sclet_lib, tmp_path):
+    L = sclet_lib.lib()
+    n, nf = 6, 3
+    blocks = np.random.default_rng(9).uniform(-1.0, 1.0, (nf, n, n, n)) * np.array([1.0, 1e-3, 1e5])[:, None, None, None]
+    path = str(tmp_path / "time_300.vtk").encode()
+    assert L.sclet_write_vtk_file(path, 300, n, nf, _dp(np.ascontiguousarray(blocks))) == 0
+    with open(path) as fp:
+        assert fp.read() == oracle_py.vtk_text(300, blocks)
+
+
+@pytest.mark.gpu
+def test_vtk_of_context_state(sclet_lib, tmp_path):
+    sg = sclet_lib
+    case = bench.workload(24, seed=2)
+    s = sg.Solver(_params(sg, case), sg.MIXED)
+    s.set_fields(bench.block_fields(case))
+    s.step(1)
+    state = s.get_fields()
+    path = str(tmp_path / "time_1.vtk")
+    s.write_vtk(path, 1)
+    with open(path) as fp:
+        assert fp.read() == oracle_py.vtk_text(1, state[:s.nac])
+    s.close()
+
+
+def test_soln_logs_match_restated_check_soln(sclet_lib, tmp_path):
+    L = sclet_lib.lib()
+    nac, nch = 4, 1
+    rng = np.random.default_rng(4)
+    want = {}
+    for it in (0, 1, 2):
+        d = np.ascontiguousarray(rng.normal(0.0, 1e3, (nac + nch, 4)))
+        couple = np.array([-1234.5 * (it + 1)])
+        assert L.sclet_append_soln_log((str(tmp_path) + "/").encode(), it, nac, nch, _dp(d), _dp(couple)) == 0
+        for name, text in oracle_py.soln_log_rows(it, nac, nch, d, couple[0]).items():
+            want[name] = want.get(name, "") + text
+    assert sorted(p.name for p in tmp_path.iterdir()) == sorted(want)
+    for name, text in want.items():
+        assert (tmp_path / name).read_text() == text, name
+
+
+@pytest.mark.gpu
+def test_soln_logs_of_context(sclet_lib, tmp_path):
+    sg = sclet_lib
+    case = bench.workload(24, seed=3)
+    s = sg.Solver(_params(sg, case), sg.FP64)
+    s.set_fields(bench.block_fields(case))
+    work = str(tmp_path) + "/"
+    want = {}
+    for it in range(3):
+        if it:
+            s.step(1)
+        d0, d1 = s.check_soln(0), s.check_soln(1)
+        s.log_soln(work, it, 0)
+        for name, text in oracle_py.soln_log_rows(it, s.nac, s.F - s.nac, d0, d1[0, 3]).items():
+            want[name] = want.get(name, "") + text
+    for name, text in want.items():
+        assert (tmp_path / name).read_text() == text, name
+    s.close()
