@@ -210,6 +210,250 @@ __global__ void __launch_bounds__(256) fft_lines_kernel(typename Cx<T>::t *data0
   }
 }
 
+// ---- FP32 fast path: line FFTs of N = N1 * N2 points in two register passes
+//
+// X[k1 + N1 k2] = sum_t W_N2^(t k2) W_N^(t k1) sum_n1 x[t + N2 n1] W_N1^(n1 k1)
+//
+// Pass A: thread t of a line loads x[t + N2 n1] (n1 < N1), transforms them in
+// registers, applies W_N^(t k1) and writes the N1 results to shared memory.
+// Pass B: thread k1 reads the N2 values of its column, transforms them in
+// registers and stores X[k1 + N1 k2].  Each element crosses shared memory
+// once; the small transforms use constant twiddles (c_wr below).
+namespace fft2 {
+
+// exp(-2 pi i m / R) at index R (R - 1) / 2 + m, for R <= 32
+__constant__ float2 c_wr[528];
+
+template <int R, int SIGN>
+__device__ __forceinline__ float2 wc(int m) {
+  float2 w = c_wr[R * (R - 1) / 2 + m];
+  if (SIGN > 0) w.y = -w.y;
+  return w;
+}
+
+// v * (-i) for the forward sign, v * (+i) for the backward one
+template <int SIGN>
+__device__ __forceinline__ float2 rot(float2 v) {
+  float2 r;
+  if (SIGN < 0) { r.x = v.y; r.y = -v.x; }
+  else { r.x = -v.y; r.y = v.x; }
+  return r;
+}
+
+template <int R>
+struct First {
+  static constexpr int v = (R % 4 == 0 && R > 4) ? 4 : (R % 2 == 0 && R > 2) ? 2 : (R % 3 == 0 && R > 3) ? 3 : R;
+};
+
+// In-register DFT of R points, natural order in and out.  Composite R = A B:
+// A-point transforms over the stride-B subsequences, twiddles W_R^(b ka),
+// B-point transforms across them.
+template <int R, int SIGN>
+struct Dft {
+  static __device__ __forceinline__ void run(float2 (&v)[R]) {
+    constexpr int A = First<R>::v, B = R / A;
+    static_assert(A < R, "unsupported transform length");
+    float2 y[B][A];
+#pragma unroll
+    for (int b = 0; b < B; b++) {
+      float2 u[A];
+#pragma unroll
+      for (int a = 0; a < A; a++) u[a] = v[b + B * a];
+      Dft<A, SIGN>::run(u);
+#pragma unroll
+      for (int ka = 0; ka < A; ka++) y[b][ka] = (b * ka == 0) ? u[ka] : cmul(u[ka], wc<R, SIGN>(b * ka));
+    }
+#pragma unroll
+    for (int ka = 0; ka < A; ka++) {
+      float2 w[B];
+#pragma unroll
+      for (int b = 0; b < B; b++) w[b] = y[b][ka];
+      Dft<B, SIGN>::run(w);
+#pragma unroll
+      for (int kb = 0; kb < B; kb++) v[ka + A * kb] = w[kb];
+    }
+  }
+};
+template <int SIGN>
+struct Dft<1, SIGN> {
+  static __device__ __forceinline__ void run(float2 (&)[1]) {}
+};
+template <int SIGN>
+struct Dft<2, SIGN> {
+  static __device__ __forceinline__ void run(float2 (&v)[2]) {
+    const float2 a = v[0], b = v[1];
+    v[0] = cadd(a, b);
+    v[1] = csub(a, b);
+  }
+};
+template <int SIGN>
+struct Dft<3, SIGN> {
+  static __device__ __forceinline__ void run(float2 (&v)[3]) {
+    const float s3 = 0.86602540378443864676f;  // sin(2 pi / 3)
+    const float2 t1 = cadd(v[1], v[2]);
+    float2 t2, d = csub(v[1], v[2]);
+    t2.x = v[0].x - 0.5f * t1.x;
+    t2.y = v[0].y - 0.5f * t1.y;
+    d.x *= s3;
+    d.y *= s3;
+    const float2 t3 = rot<SIGN>(d);
+    v[0] = cadd(v[0], t1);
+    v[1] = cadd(t2, t3);
+    v[2] = csub(t2, t3);
+  }
+};
+template <int SIGN>
+struct Dft<4, SIGN> {
+  static __device__ __forceinline__ void run(float2 (&v)[4]) {
+    const float2 a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
+    const float2 c = cadd(v[1], v[3]), d = rot<SIGN>(csub(v[1], v[3]));
+    v[0] = cadd(a, c);
+    v[2] = csub(a, c);
+    v[1] = cadd(b, d);
+    v[3] = csub(b, d);
+  }
+};
+template <int SIGN>
+struct Dft<5, SIGN> {
+  static __device__ __forceinline__ void run(float2 (&v)[5]) {
+    float2 o[5];
+#pragma unroll
+    for (int q = 0; q < 5; q++) {
+      float2 acc = v[0];
+#pragma unroll
+      for (int r = 1; r < 5; r++) acc = cadd(acc, cmul(v[r], wc<5, SIGN>((r * q) % 5)));
+      o[q] = acc;
+    }
+#pragma unroll
+    for (int q = 0; q < 5; q++) v[q] = o[q];
+  }
+};
+
+// L lines per CTA.  axis 0: lines along x, lane order over t (pass A) and k1
+// (pass B); axes 1 and 2: L adjacent x-lines, lane order over x.
+template <int N1, int N2, int L, int AXIS, int SIGN>
+__global__ void __launch_bounds__(L *(N1 > N2 ? N1 : N2))
+    lines_kernel(float2 *data0, float2 *data1, const float2 *__restrict__ tw) {
+  constexpr int N = N1 * N2;
+  constexpr int RS = AXIS == 0 ? N2 + 1 : N2;  // row stride of a line's table (padded on axis 0)
+  extern __shared__ float2 tab[];
+  float2 *data = blockIdx.y == 0 ? data0 : data1;
+  const int tid = threadIdx.x;
+  const long long NN = (long long)N * N;
+  long long base;
+  long long ps;  // element stride along the line
+  if (AXIS == 0) {
+    base = (long long)blockIdx.x * L * N;
+    ps = 1;
+  } else {
+    constexpr int ntx = N / L;
+    const int xt = blockIdx.x % ntx, w = blockIdx.x / ntx;  // w = z (axis 1) or y (axis 2)
+    base = (AXIS == 1 ? (long long)w * NN : (long long)w * N) + (long long)xt * L;
+    ps = AXIS == 1 ? N : NN;
+  }
+  auto at = [&](int l, int k1, int t) -> int {
+    return AXIS == 0 ? (l * N1 + k1) * RS + t : (k1 * N2 + t) * L + l;
+  };
+  if (tid < L * N2) {
+    const int l = AXIS == 0 ? tid / N2 : tid % L, t = AXIS == 0 ? tid % N2 : tid / L;
+    const float2 *src = data + base + (AXIS == 0 ? (long long)l * N : (long long)l);
+    float2 v[N1];
+#pragma unroll
+    for (int n1 = 0; n1 < N1; n1++) v[n1] = src[(long long)(t + N2 * n1) * ps];
+    Dft<N1, SIGN>::run(v);
+#pragma unroll
+    for (int k1 = 0; k1 < N1; k1++) {
+      float2 r = v[k1];
+      if (k1 > 0 && t > 0) {
+        float2 w = tw[t * k1];  // t k1 < N
+        if (SIGN > 0) w.y = -w.y;
+        r = cmul(r, w);
+      }
+      tab[at(l, k1, t)] = r;
+    }
+  }
+  __syncthreads();
+  if (tid < L * N1) {
+    const int l = AXIS == 0 ? tid / N1 : tid % L, k1 = AXIS == 0 ? tid % N1 : tid / L;
+    float2 v[N2];
+#pragma unroll
+    for (int t = 0; t < N2; t++) v[t] = tab[at(l, k1, t)];
+    Dft<N2, SIGN>::run(v);
+    float2 *dst = data + base + (AXIS == 0 ? (long long)l * N : (long long)l);
+#pragma unroll
+    for (int k2 = 0; k2 < N2; k2++) dst[(long long)(k1 + N1 * k2) * ps] = v[k2];
+  }
+}
+
+constexpr int L = 16;
+
+template <int N1, int N2>
+constexpr size_t smem_bytes(int axis) {
+  return sizeof(float2) * L * N1 * (axis == 0 ? N2 + 1 : N2);
+}
+
+template <int N1, int N2, int AXIS, int SIGN>
+static cudaError_t launch_one(float2 *z0, float2 *z1, const float2 *tw, cudaStream_t s) {
+  constexpr int N = N1 * N2;
+  constexpr size_t sm = smem_bytes<N1, N2>(AXIS);
+  auto k = lines_kernel<N1, N2, L, AXIS, SIGN>;
+  if (sm > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  const dim3 grid((unsigned)((long long)N * N / L), z1 ? 2u : 1u);
+  k<<<grid, L * (N1 > N2 ? N1 : N2), sm, s>>>(z0, z1 ? z1 : z0, tw);
+  return cudaGetLastError();
+}
+
+template <int N1, int N2, int SIGN>
+static cudaError_t launch_axis(int axis, float2 *z0, float2 *z1, const float2 *tw, cudaStream_t s) {
+  switch (axis) {
+    case 0: return launch_one<N1, N2, 0, SIGN>(z0, z1, tw, s);
+    case 1: return launch_one<N1, N2, 1, SIGN>(z0, z1, tw, s);
+    default: return launch_one<N1, N2, 2, SIGN>(z0, z1, tw, s);
+  }
+}
+
+template <int N1>
+static cudaError_t launch_n1(int axis, int sign, float2 *z0, float2 *z1, const float2 *tw, cudaStream_t s) {
+  return sign < 0 ? launch_axis<N1, 16, -1>(axis, z0, z1, tw, s) : launch_axis<N1, 16, 1>(axis, z0, z1, tw, s);
+}
+
+// N = 16 N1 with N1 in {2, 3, 4, 5, 6, 8, 10, 12, 16}; 0 if N has no fast path
+static int pass_n1(int N) {
+  static const int ok[] = {2, 3, 4, 5, 6, 8, 10, 12, 16};
+  if (N % 16) return 0;
+  for (int n1 : ok)
+    if (n1 * 16 == N) return n1;
+  return 0;
+}
+
+static cudaError_t launch(int N, int axis, int sign, float2 *z0, float2 *z1, const float2 *tw, cudaStream_t s) {
+  switch (pass_n1(N)) {
+    case 2: return launch_n1<2>(axis, sign, z0, z1, tw, s);
+    case 3: return launch_n1<3>(axis, sign, z0, z1, tw, s);
+    case 4: return launch_n1<4>(axis, sign, z0, z1, tw, s);
+    case 5: return launch_n1<5>(axis, sign, z0, z1, tw, s);
+    case 6: return launch_n1<6>(axis, sign, z0, z1, tw, s);
+    case 8: return launch_n1<8>(axis, sign, z0, z1, tw, s);
+    case 10: return launch_n1<10>(axis, sign, z0, z1, tw, s);
+    case 12: return launch_n1<12>(axis, sign, z0, z1, tw, s);
+    default: return launch_n1<16>(axis, sign, z0, z1, tw, s);
+  }
+}
+
+// fills c_wr on the current device
+static cudaError_t upload_constants(cudaStream_t s) {
+  std::vector<float2> h(528);
+  for (int R = 1; R <= 32; R++)
+    for (int m = 0; m < R; m++) {
+      const double a = -2.0 * 3.14159265358979323846 * (double)m / (double)R;
+      h[R * (R - 1) / 2 + m] = make_float2((float)cos(a), (float)sin(a));
+    }
+  cudaError_t e = cudaMemcpyToSymbolAsync(c_wr, h.data(), sizeof(float2) * 528, 0, cudaMemcpyHostToDevice, s);
+  return e == cudaSuccess ? cudaStreamSynchronize(s) : e;
+}
+
+}  // namespace fft2
+
 // eta pairs -> complex grids (owned cells of the n^3 blocks, n = N + 4).
 template <typename T>
 __global__ void pack_kernel(const T *__restrict__ u, typename Cx<T>::t *__restrict__ z01,
@@ -372,6 +616,7 @@ struct ElasticPlan {
   void *z01, *z23;
   double *bn;     // 10 * N^3
   int tile, ltile;
+  int fast;       // FP32 plan with a two-pass register path for N
   StageDiv sd;
   size_t smem;
   bool first;     // no previous elastic call: scratch ghosts are zero
@@ -414,6 +659,8 @@ cudaError_t elastic_plan_create(ElasticPlan **out, int N, int nac, const double 
       for (int j = 0; j < 2 * N; j++) twf[j] = (float)twd[j];
       e = cudaMemcpyAsync(p->tw, twf.data(), sizeof(float) * 2 * N, cudaMemcpyHostToDevice, s);
       if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      p->fast = fft2::pass_n1(N) != 0 && getenv("SCLET_FFT_GENERIC") == nullptr;
+      if (e == cudaSuccess && p->fast) e = fft2::upload_constants(s);
     } else {
       e = cudaMemcpyAsync(p->tw, twd.data(), sizeof(double) * 2 * N, cudaMemcpyHostToDevice, s);
       if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -497,6 +744,14 @@ static cudaError_t fft3d(ElasticPlan *p, typename Cx<T>::t *z0, typename Cx<T>::
   const typename Cx<T>::t *tw = (const typename Cx<T>::t *)p->tw;
   int order[3] = {0, 1, 2};
   if (sign > 0) { order[0] = 2; order[2] = 0; }
+  if (sizeof(T) == 4 && p->fast) {
+    for (int k = 0; k < 3; k++) {
+      cudaError_t e = fft2::launch(N, order[k], sign, (float2 *)z0, (float2 *)z1, (const float2 *)tw, s);
+      launch_counter()++;
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  }
   for (int k = 0; k < 3; k++) {
     fft_lines_kernel<T><<<grid, 256, p->smem, s>>>(z0, z1, N, order[k], p->ltile, tw, sign, p->rad, p->sd);
     launch_counter()++;

@@ -91,3 +91,26 @@ def test_step_diagnostics_match_check_soln(precision_name, sclet_lib):
     s.set_step_diagnostics(-1)
     np.testing.assert_array_equal(queued, s.check_soln(1))
     s.close()
+
+
+@pytest.mark.parametrize("big_n", [24, 32, 48, 80, 96, 160])
+def test_fp32_elastic_force_matches_fp64(big_n, sclet_lib):
+    """FP32 elastic force (pack, three line-FFT passes each way, contraction)
+    against the FP64 form on the same state.  N = 16 N1 takes the two-pass
+    register transforms; 24 the generic Stockham stages."""
+    sg = sclet_lib
+    case = bench.workload(big_n, seed=13)
+    p = params_for(sg, case)
+    u0 = bench.block_fields(case)
+    u0[:case.nac] *= 50.0  # order parameters of order 0.5
+    out = {}
+    for prec in (sg.FP64, sg.MIXED):
+        s = sg.Solver(p, prec)
+        s.set_fields(u0)
+        s.transfer()
+        s.elastic()
+        out[prec] = s.get_felas()
+        s.close()
+    for m in range(case.nac):
+        err = rel(out[sg.MIXED][m], out[sg.FP64][m])
+        assert err <= 2e-6, (big_n, m, err)
