@@ -329,11 +329,24 @@ struct Dft<5, SIGN> {
   }
 };
 
+// Grids and blocks of one elastic call.  io 1 (first forward x-pass): lines
+// are read from the order parameters (grid y = q holds eta_2q + i eta_2q+1 of
+// the owned cells) instead of data; io 2 (last inverse x-pass): the real and
+// imaginary parts, scaled by 1 / N^3, go to felas_2q and felas_2q+1.
+struct LineIO {
+  const float *u;  // order parameters, nac blocks of n^3
+  float *felas;    // elastic force, nac blocks of n^3
+  int n, nac;
+  long long n3;
+  float scale;     // 1 / N^3
+};
+
 // L lines per CTA.  axis 0: lines along x, lane order over t (pass A) and k1
 // (pass B); axes 1 and 2: L adjacent x-lines, lane order over x.
-template <int N1, int N2, int L, int AXIS, int SIGN>
+template <int N1, int N2, int L, int AXIS, int SIGN, int IO>
 __global__ void __launch_bounds__(L *(N1 > N2 ? N1 : N2))
-    lines_kernel(float2 *data0, float2 *data1, const float2 *__restrict__ tw) {
+    lines_kernel(float2 *data0, float2 *data1, const float2 *__restrict__ tw, LineIO io) {
+  static_assert(IO == 0 || AXIS == 0, "fused packing on x-passes only");
   constexpr int N = N1 * N2;
   constexpr int RS = AXIS == 0 ? N2 + 1 : N2;  // row stride of a line's table (padded on axis 0)
   extern __shared__ float2 tab[];
@@ -354,12 +367,25 @@ __global__ void __launch_bounds__(L *(N1 > N2 ? N1 : N2))
   auto at = [&](int l, int k1, int t) -> int {
     return AXIS == 0 ? (l * N1 + k1) * RS + t : (k1 * N2 + t) * L + l;
   };
+  // owned-cell offset of this CTA's line l in an n^3 block (io != 0)
+  auto cell0 = [&](int l) -> long long {
+    const int gl = blockIdx.x * L + l, z = gl / N, y = gl - z * N;
+    return ((long long)(z + 2) * io.n + (y + 2)) * io.n + 2;
+  };
+  const int f0 = 2 * blockIdx.y;
   if (tid < L * N2) {
     const int l = AXIS == 0 ? tid / N2 : tid % L, t = AXIS == 0 ? tid % N2 : tid / L;
-    const float2 *src = data + base + (AXIS == 0 ? (long long)l * N : (long long)l);
     float2 v[N1];
+    if (IO == 1) {
+      const float *re = io.u + f0 * io.n3 + cell0(l);
+      const float *im = f0 + 1 < io.nac ? re + io.n3 : nullptr;
 #pragma unroll
-    for (int n1 = 0; n1 < N1; n1++) v[n1] = src[(long long)(t + N2 * n1) * ps];
+      for (int n1 = 0; n1 < N1; n1++) v[n1] = make_float2(re[t + N2 * n1], im ? im[t + N2 * n1] : 0.0f);
+    } else {
+      const float2 *src = data + base + (AXIS == 0 ? (long long)l * N : (long long)l);
+#pragma unroll
+      for (int n1 = 0; n1 < N1; n1++) v[n1] = src[(long long)(t + N2 * n1) * ps];
+    }
     Dft<N1, SIGN>::run(v);
 #pragma unroll
     for (int k1 = 0; k1 < N1; k1++) {
@@ -379,9 +405,19 @@ __global__ void __launch_bounds__(L *(N1 > N2 ? N1 : N2))
 #pragma unroll
     for (int t = 0; t < N2; t++) v[t] = tab[at(l, k1, t)];
     Dft<N2, SIGN>::run(v);
-    float2 *dst = data + base + (AXIS == 0 ? (long long)l * N : (long long)l);
+    if (IO == 2) {
+      float *re = io.felas + f0 * io.n3 + cell0(l);
+      float *im = f0 + 1 < io.nac ? re + io.n3 : nullptr;
 #pragma unroll
-    for (int k2 = 0; k2 < N2; k2++) dst[(long long)(k1 + N1 * k2) * ps] = v[k2];
+      for (int k2 = 0; k2 < N2; k2++) {
+        re[k1 + N1 * k2] = v[k2].x * io.scale;
+        if (im) im[k1 + N1 * k2] = v[k2].y * io.scale;
+      }
+    } else {
+      float2 *dst = data + base + (AXIS == 0 ? (long long)l * N : (long long)l);
+#pragma unroll
+      for (int k2 = 0; k2 < N2; k2++) dst[(long long)(k1 + N1 * k2) * ps] = v[k2];
+    }
   }
 }
 
@@ -392,29 +428,33 @@ constexpr size_t smem_bytes(int axis) {
   return sizeof(float2) * L * N1 * (axis == 0 ? N2 + 1 : N2);
 }
 
-template <int N1, int N2, int AXIS, int SIGN>
-static cudaError_t launch_one(float2 *z0, float2 *z1, const float2 *tw, cudaStream_t s) {
+template <int N1, int N2, int AXIS, int SIGN, int IO>
+static cudaError_t launch_one(float2 *z0, float2 *z1, const float2 *tw, const LineIO &io, cudaStream_t s) {
   constexpr int N = N1 * N2;
   constexpr size_t sm = smem_bytes<N1, N2>(AXIS);
-  auto k = lines_kernel<N1, N2, L, AXIS, SIGN>;
+  auto k = lines_kernel<N1, N2, L, AXIS, SIGN, IO>;
   if (sm > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   const dim3 grid((unsigned)((long long)N * N / L), z1 ? 2u : 1u);
-  k<<<grid, L * (N1 > N2 ? N1 : N2), sm, s>>>(z0, z1 ? z1 : z0, tw);
+  k<<<grid, L * (N1 > N2 ? N1 : N2), sm, s>>>(z0, z1 ? z1 : z0, tw, io);
   return cudaGetLastError();
 }
 
-template <int N1, int N2, int SIGN>
-static cudaError_t launch_axis(int axis, float2 *z0, float2 *z1, const float2 *tw, cudaStream_t s) {
-  switch (axis) {
-    case 0: return launch_one<N1, N2, 0, SIGN>(z0, z1, tw, s);
-    case 1: return launch_one<N1, N2, 1, SIGN>(z0, z1, tw, s);
-    default: return launch_one<N1, N2, 2, SIGN>(z0, z1, tw, s);
+// forward: x (reading the order parameters), y, z; inverse: z, y, x (writing felas)
+template <int N1, int N2>
+static cudaError_t launch_pass(int sign, int k, float2 *z0, float2 *z1, const float2 *tw, const LineIO &io,
+                               cudaStream_t s) {
+  if (sign < 0) {
+    switch (k) {
+      case 0: return launch_one<N1, N2, 0, -1, 1>(z0, z1, tw, io, s);
+      case 1: return launch_one<N1, N2, 1, -1, 0>(z0, z1, tw, io, s);
+      default: return launch_one<N1, N2, 2, -1, 0>(z0, z1, tw, io, s);
+    }
   }
-}
-
-template <int N1>
-static cudaError_t launch_n1(int axis, int sign, float2 *z0, float2 *z1, const float2 *tw, cudaStream_t s) {
-  return sign < 0 ? launch_axis<N1, 16, -1>(axis, z0, z1, tw, s) : launch_axis<N1, 16, 1>(axis, z0, z1, tw, s);
+  switch (k) {
+    case 0: return launch_one<N1, N2, 2, 1, 0>(z0, z1, tw, io, s);
+    case 1: return launch_one<N1, N2, 1, 1, 0>(z0, z1, tw, io, s);
+    default: return launch_one<N1, N2, 0, 1, 2>(z0, z1, tw, io, s);
+  }
 }
 
 // N = 16 N1 with N1 in {2, 3, 4, 5, 6, 8, 10, 12, 16}; 0 if N has no fast path
@@ -426,17 +466,19 @@ static int pass_n1(int N) {
   return 0;
 }
 
-static cudaError_t launch(int N, int axis, int sign, float2 *z0, float2 *z1, const float2 *tw, cudaStream_t s) {
+// pass k (0..2) of the forward (sign -1) or inverse (+1) 3-D transform
+static cudaError_t launch(int N, int sign, int k, float2 *z0, float2 *z1, const float2 *tw, const LineIO &io,
+                          cudaStream_t s) {
   switch (pass_n1(N)) {
-    case 2: return launch_n1<2>(axis, sign, z0, z1, tw, s);
-    case 3: return launch_n1<3>(axis, sign, z0, z1, tw, s);
-    case 4: return launch_n1<4>(axis, sign, z0, z1, tw, s);
-    case 5: return launch_n1<5>(axis, sign, z0, z1, tw, s);
-    case 6: return launch_n1<6>(axis, sign, z0, z1, tw, s);
-    case 8: return launch_n1<8>(axis, sign, z0, z1, tw, s);
-    case 10: return launch_n1<10>(axis, sign, z0, z1, tw, s);
-    case 12: return launch_n1<12>(axis, sign, z0, z1, tw, s);
-    default: return launch_n1<16>(axis, sign, z0, z1, tw, s);
+    case 2: return launch_pass<2, 16>(sign, k, z0, z1, tw, io, s);
+    case 3: return launch_pass<3, 16>(sign, k, z0, z1, tw, io, s);
+    case 4: return launch_pass<4, 16>(sign, k, z0, z1, tw, io, s);
+    case 5: return launch_pass<5, 16>(sign, k, z0, z1, tw, io, s);
+    case 6: return launch_pass<6, 16>(sign, k, z0, z1, tw, io, s);
+    case 8: return launch_pass<8, 16>(sign, k, z0, z1, tw, io, s);
+    case 10: return launch_pass<10, 16>(sign, k, z0, z1, tw, io, s);
+    case 12: return launch_pass<12, 16>(sign, k, z0, z1, tw, io, s);
+    default: return launch_pass<16, 16>(sign, k, z0, z1, tw, io, s);
   }
 }
 
@@ -455,13 +497,17 @@ static cudaError_t upload_constants(cudaStream_t s) {
 }  // namespace fft2
 
 // eta pairs -> complex grids (owned cells of the n^3 blocks, n = N + 4).
+// The element-wise kernels below run over rows (y, z) of the grid, one CTA
+// per row at a time and threads along x: no per-element index division.
 template <typename T>
 __global__ void pack_kernel(const T *__restrict__ u, typename Cx<T>::t *__restrict__ z01,
                             typename Cx<T>::t *__restrict__ z23, int N, int nac) {
   const int n = N + 4;
-  const long long n3 = (long long)n * n * n, N3 = (long long)N * N * N;
-  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < N3; g += (long long)gridDim.x * blockDim.x) {
-    int x = (int)(g % N), y = (int)((g / N) % N), z = (int)(g / ((long long)N * N));
+  const long long n3 = (long long)n * n * n;
+  for (int row = blockIdx.x; row < N * N; row += gridDim.x)
+  for (int x = threadIdx.x; x < N; x += blockDim.x) {
+    const int z = row / N, y = row - z * N;
+    const long long g = (long long)row * N + x;
     long long l = ((long long)(z + 2) * n + (y + 2)) * n + (x + 2);
     T v[4];
     for (int q = 0; q < 4; q++) v[q] = q < nac ? u[q * n3 + l] : (T)0;
@@ -486,7 +532,8 @@ struct BnConst {
   double t0[10];
 };
 
-__global__ void bn_kernel(double *__restrict__ bn, int N, BnConst bc) {
+template <typename B>
+__global__ void bn_kernel(B *__restrict__ bn, int N, BnConst bc) {
   const long long N3 = (long long)N * N * N;
   for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < N3; g += (long long)gridDim.x * blockDim.x) {
     int x = (int)(g % N), y = (int)((g / N) % N), z = (int)(g / ((long long)N * N));
@@ -529,21 +576,26 @@ __global__ void bn_kernel(double *__restrict__ bn, int N, BnConst bc) {
         double t1 = 0.0;
         for (int j = 0; j < 3; j++)
           for (int k = 0; k < 3; k++) t1 += v[p][j] * om[j * 3 + k] * v[q][k];
-        bn[(long long)pq_slot(p, q) * N3 + g] = bc.t0[pq_slot(p, q)] - t1;
+        bn[(long long)pq_slot(p, q) * N3 + g] = (B)(bc.t0[pq_slot(p, q)] - t1);
       }
   }
 }
 
-// Contraction on pairs {k, -k}; see the file comment.
-template <typename T>
-__global__ void contract_kernel(typename Cx<T>::t *z01, typename Cx<T>::t *z23, const double *__restrict__ bn, int N,
+// Contraction on pairs {k, -k}; see the file comment.  A row (y, z) is done
+// together with its mirror row (-y, -z), by the lower of the two.
+template <typename T, typename B>
+__global__ void contract_kernel(typename Cx<T>::t *z01, typename Cx<T>::t *z23, const B *__restrict__ bn, int N,
                                 int nac) {
   typedef typename Cx<T>::t C;
   const long long N3 = (long long)N * N * N;
-  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < N3; g += (long long)gridDim.x * blockDim.x) {
-    int x = (int)(g % N), y = (int)((g / N) % N), z = (int)(g / ((long long)N * N));
-    int xm = (N - x) % N, ym = (N - y) % N, zm = (N - z) % N;
-    long long gm = ((long long)zm * N + ym) * N + xm;
+  for (int row = blockIdx.x; row < N * N; row += gridDim.x) {
+  const int z = row / N, y = row - z * N;
+  const int ym = y == 0 ? 0 : N - y, zm = z == 0 ? 0 : N - z;
+  const int rowm = zm * N + ym;
+  if (rowm < row) continue;
+  for (int x = threadIdx.x; x < N; x += blockDim.x) {
+    const int xm = x == 0 ? 0 : N - x;
+    const long long g = (long long)row * N + x, gm = (long long)rowm * N + xm;
     if (gm < g) continue;  // the pair is handled by its lower index
     C H[4], Hm[4];
     C a = z01[g], am = z01[gm];
@@ -586,6 +638,7 @@ __global__ void contract_kernel(typename Cx<T>::t *z01, typename Cx<T>::t *z23, 
       if (gm != g) z23[gm] = w23m;
     }
   }
+  }
 }
 
 // Interior of felas_p from the inverse transforms, scaled by 1/N^3.
@@ -595,8 +648,10 @@ __global__ void unpack_kernel(const typename Cx<T>::t *__restrict__ w01, const t
   const int n = N + 4;
   const long long n3 = (long long)n * n * n, N3 = (long long)N * N * N;
   const double s = 1.0 / (double)N3;
-  for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < N3; g += (long long)gridDim.x * blockDim.x) {
-    int x = (int)(g % N), y = (int)((g / N) % N), z = (int)(g / ((long long)N * N));
+  for (int row = blockIdx.x; row < N * N; row += gridDim.x)
+  for (int x = threadIdx.x; x < N; x += blockDim.x) {
+    const int z = row / N, y = row - z * N;
+    const long long g = (long long)row * N + x;
     long long l = ((long long)(z + 2) * n + (y + 2)) * n + (x + 2);
     typename Cx<T>::t a = w01[g];
     felas[l] = (T)(a.x * s);
@@ -614,7 +669,7 @@ struct ElasticPlan {
   Radices rad;
   void *tw;       // twiddles, complex of the working precision
   void *z01, *z23;
-  double *bn;     // 10 * N^3
+  void *bn;       // 10 * N^3 Green-tensor slots, double (FP64 plan) or float
   int tile, ltile;
   int fast;       // FP32 plan with a two-pass register path for N
   StageDiv sd;
@@ -646,7 +701,7 @@ cudaError_t elastic_plan_create(ElasticPlan **out, int N, int nac, const double 
   if ((e = cudaMalloc(&p->tw, csz * N)) != cudaSuccess) goto fail;
   if ((e = cudaMalloc(&p->z01, csz * N3)) != cudaSuccess) goto fail;
   if (nac > 2 && (e = cudaMalloc(&p->z23, csz * N3)) != cudaSuccess) goto fail;
-  if ((e = cudaMalloc(&p->bn, sizeof(double) * 10 * N3)) != cudaSuccess) goto fail;
+  if ((e = cudaMalloc(&p->bn, (fp32 ? sizeof(float) : sizeof(double)) * 10 * N3)) != cudaSuccess) goto fail;
   {
     std::vector<double> twd(2 * N);
     for (int j = 0; j < N; j++) {
@@ -693,7 +748,8 @@ cudaError_t elastic_plan_create(ElasticPlan **out, int N, int nac, const double 
                 t0 += bc.C[((i * 3 + j) * 3 + k) * 3 + l] * eps[a * 9 + i * 3 + j] * eps[b * 9 + k * 3 + l];
         bc.t0[pq_slot(a, b)] = t0;
       }
-    bn_kernel<<<grid1(N3), 256, 0, s>>>(p->bn, N, bc);
+    if (fp32) bn_kernel<float><<<grid1(N3), 256, 0, s>>>((float *)p->bn, N, bc);
+    else bn_kernel<double><<<grid1(N3), 256, 0, s>>>((double *)p->bn, N, bc);
     launch_counter()++;
     if ((e = cudaGetLastError()) != cudaSuccess) goto fail;
   }
@@ -729,8 +785,8 @@ void elastic_plan_destroy(ElasticPlan *p) {
   delete p;
 }
 
-// 3-D transform of one or two complex grids (z1 may be null): one launch per
-// axis, x, y, z forward and z, y, x backward.
+// 3-D transform of one or two complex grids (z1 may be null) by the generic
+// Stockham stages: one launch per axis, x, y, z forward and z, y, x backward.
 template <typename T>
 static cudaError_t fft3d(ElasticPlan *p, typename Cx<T>::t *z0, typename Cx<T>::t *z1, int sign, cudaStream_t s) {
   const int N = p->N;
@@ -744,14 +800,6 @@ static cudaError_t fft3d(ElasticPlan *p, typename Cx<T>::t *z0, typename Cx<T>::
   const typename Cx<T>::t *tw = (const typename Cx<T>::t *)p->tw;
   int order[3] = {0, 1, 2};
   if (sign > 0) { order[0] = 2; order[2] = 0; }
-  if (sizeof(T) == 4 && p->fast) {
-    for (int k = 0; k < 3; k++) {
-      cudaError_t e = fft2::launch(N, order[k], sign, (float2 *)z0, (float2 *)z1, (const float2 *)tw, s);
-      launch_counter()++;
-      if (e != cudaSuccess) return e;
-    }
-    return cudaSuccess;
-  }
   for (int k = 0; k < 3; k++) {
     fft_lines_kernel<T><<<grid, 256, p->smem, s>>>(z0, z1, N, order[k], p->ltile, tw, sign, p->rad, p->sd);
     launch_counter()++;
@@ -759,20 +807,51 @@ static cudaError_t fft3d(ElasticPlan *p, typename Cx<T>::t *z0, typename Cx<T>::
   return cudaGetLastError();
 }
 
+// launch shape of the row kernels: rows (y, z) over CTAs, x over threads
+static dim3 rows_grid(int N) { return dim3((unsigned)(N * N < 152 * 16 ? N * N : 152 * 16)); }
+static dim3 rows_block(int N) { return dim3((unsigned)(N >= 256 ? 256 : (N + 31) / 32 * 32)); }
+
 template <typename T>
 cudaError_t elastic_compute(ElasticPlan *p, const T *u, T *felas, int n, T *shell, cudaStream_t s) {
   typedef typename Cx<T>::t C;
   const int N = p->N;
-  const long long N3 = (long long)N * N * N, n3 = (long long)n * n * n;
+  const long long n3 = (long long)n * n * n;
   C *z01 = (C *)p->z01, *z23 = (C *)p->z23;
-  pack_kernel<T><<<grid1(N3), 256, 0, s>>>(u, z01, z23, N, p->nac);
-  launch_counter()++;
-  fft3d<T>(p, z01, z23, -1, s);
-  contract_kernel<T><<<grid1(N3), 256, 0, s>>>(z01, z23, p->bn, N, p->nac);
-  launch_counter()++;
-  fft3d<T>(p, z01, z23, +1, s);
-  unpack_kernel<T><<<grid1(N3), 256, 0, s>>>(z01, z23, felas, N, p->nac);
-  launch_counter()++;
+  if (sizeof(T) == 4 && p->fast) {
+    // packing and unpacking fused into the first and last x-passes
+    fft2::LineIO io;
+    io.u = (const float *)u;
+    io.felas = (float *)felas;
+    io.n = n;
+    io.nac = p->nac;
+    io.n3 = n3;
+    io.scale = (float)(1.0 / ((double)N * N * N));
+    const float2 *tw = (const float2 *)p->tw;
+    for (int k = 0; k < 3; k++) {
+      cudaError_t e = fft2::launch(N, -1, k, (float2 *)z01, (float2 *)z23, tw, io, s);
+      launch_counter()++;
+      if (e != cudaSuccess) return e;
+    }
+    contract_kernel<T, float><<<rows_grid(N), rows_block(N), 0, s>>>(z01, z23, (const float *)p->bn, N, p->nac);
+    launch_counter()++;
+    for (int k = 0; k < 3; k++) {
+      cudaError_t e = fft2::launch(N, +1, k, (float2 *)z01, (float2 *)z23, tw, io, s);
+      launch_counter()++;
+      if (e != cudaSuccess) return e;
+    }
+  } else {
+    pack_kernel<T><<<rows_grid(N), rows_block(N), 0, s>>>(u, z01, z23, N, p->nac);
+    launch_counter()++;
+    fft3d<T>(p, z01, z23, -1, s);
+    if (p->fp32)
+      contract_kernel<T, float><<<rows_grid(N), rows_block(N), 0, s>>>(z01, z23, (const float *)p->bn, N, p->nac);
+    else
+      contract_kernel<T, double><<<rows_grid(N), rows_block(N), 0, s>>>(z01, z23, (const double *)p->bn, N, p->nac);
+    launch_counter()++;
+    fft3d<T>(p, z01, z23, +1, s);
+    unpack_kernel<T><<<rows_grid(N), rows_block(N), 0, s>>>(z01, z23, felas, N, p->nac);
+    launch_counter()++;
+  }
   // ghost cells: the shared-scratch semantics, field by field in order
   for (int q = 0; q < p->nac; q++) {
     const T *prev = felas + (long long)((q + p->nac - 1) % p->nac) * n3;

@@ -60,6 +60,13 @@ struct sclet_ctx {
   float4 *coef[2] = {nullptr, nullptr};   // ETD1 coefficient pairs per field kind
   float2 *coef2[2] = {nullptr, nullptr};  // ETD2 phi2 pairs per field kind
   double *stage64 = nullptr;  // n^3 FP64 staging block for host transfers
+  // pipelined transfers of all fields (sclet_set_fields_async /
+  // sclet_get_fields_async): an FP64 staging area per direction, filled and
+  // drained by the copy engines on one stream per direction, while the
+  // context's stream only converts between staging and state
+  cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  double *in_stage = nullptr, *out_stage = nullptr;
+  cudaEvent_t in_ready = nullptr, in_free = nullptr, out_ready = nullptr, out_free = nullptr;
   // conserved-field mass of the mixed form: FP64 weights wE, wP (, w2) of n^3
   // each, target / after partial sums, last (target, before, shift)
   double *massW = nullptr, *massPart = nullptr, *massRes = nullptr;
@@ -127,6 +134,25 @@ __global__ void f64_to_f32(const double *__restrict__ a, float *__restrict__ b, 
 __global__ void f32_to_f64(const float *__restrict__ a, double *__restrict__ b, long long count, double shift) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x)
     b[i] = (double)a[i] + shift;
+}
+
+// all F fields between the FP64 host layout and the state: FP32 states hold
+// the conserved fields (f >= nac) relative to shift; grid y = field
+__global__ void fields_to_state(const double *__restrict__ a, float *__restrict__ b, long long n3, int nac,
+                                double shift) {
+  const double sh = (int)blockIdx.y >= nac ? shift : 0.0;
+  const double *s = a + blockIdx.y * n3;
+  float *d = b + blockIdx.y * n3;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3; i += (long long)gridDim.x * blockDim.x)
+    d[i] = (float)(s[i] - sh);
+}
+__global__ void fields_from_state(const float *__restrict__ a, double *__restrict__ b, long long n3, int nac,
+                                  double shift) {
+  const double sh = (int)blockIdx.y >= nac ? shift : 0.0;
+  const float *s = a + blockIdx.y * n3;
+  double *d = b + blockIdx.y * n3;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3; i += (long long)gridDim.x * blockDim.x)
+    d[i] = (double)s[i] + sh;
 }
 
 int grid_of(long long total) {
@@ -282,9 +308,80 @@ int get_block(sclet_ctx *ctx, const double *src64, const float *src32, double *h
   return SCLET_OK;
 }
 
+// staging areas, copy streams and events of the pipelined transfers, on first use
+int ensure_io(sclet_ctx *ctx) {
+  if (ctx->copy_in) return SCLET_OK;
+  const size_t bytes = sizeof(double) * ctx->F * ctx->n3;
+  if (!ctx->in_stage) CK(cudaMalloc(&ctx->in_stage, bytes));
+  if (!ctx->out_stage) CK(cudaMalloc(&ctx->out_stage, bytes));
+  cudaEvent_t *evs[] = {&ctx->in_ready, &ctx->in_free, &ctx->out_ready, &ctx->out_free};
+  for (cudaEvent_t *e : evs)
+    if (!*e) CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  // the "free" events start out complete
+  CK(cudaEventRecord(ctx->in_free, ctx->stream));
+  CK(cudaEventRecord(ctx->out_free, ctx->stream));
+  if (!ctx->copy_out) CK(cudaStreamCreateWithFlags(&ctx->copy_out, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&ctx->copy_in, cudaStreamNonBlocking));
+  return SCLET_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+int sclet_set_fields_async(sclet_ctx *ctx, const double *host) {
+  int rc = ensure_io(ctx);
+  if (rc != SCLET_OK) return rc;
+  const size_t bytes = sizeof(double) * ctx->F * ctx->n3;
+  CK(cudaStreamWaitEvent(ctx->copy_in, ctx->in_free, 0));
+  CK(cudaMemcpyAsync(ctx->in_stage, host, bytes, cudaMemcpyHostToDevice, ctx->copy_in));
+  CK(cudaEventRecord(ctx->in_ready, ctx->copy_in));
+  CK(cudaStreamWaitEvent(ctx->stream, ctx->in_ready, 0));
+  if (mixed(ctx)) {
+    fields_to_state<<<dim3(grid_of(ctx->n3), ctx->F), 256, 0, ctx->stream>>>(ctx->in_stage, fu_of(ctx), ctx->n3,
+                                                                            ctx->nac, ctx->ph.cshift);
+    launch_counter()++;
+    CK(cudaGetLastError());
+  } else {
+    CK(cudaMemcpyAsync(u_of(ctx), ctx->in_stage, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  CK(cudaEventRecord(ctx->in_free, ctx->stream));
+  return SCLET_OK;
+}
+
+int sclet_get_fields_async(sclet_ctx *ctx, double *host) {
+  int rc = ensure_io(ctx);
+  if (rc != SCLET_OK) return rc;
+  const size_t bytes = sizeof(double) * ctx->F * ctx->n3;
+  CK(cudaStreamWaitEvent(ctx->stream, ctx->out_free, 0));
+  if (mixed(ctx)) {
+    fields_from_state<<<dim3(grid_of(ctx->n3), ctx->F), 256, 0, ctx->stream>>>(fu_of(ctx), ctx->out_stage, ctx->n3,
+                                                                              ctx->nac, ctx->ph.cshift);
+    launch_counter()++;
+    CK(cudaGetLastError());
+  } else {
+    CK(cudaMemcpyAsync(ctx->out_stage, u_of(ctx), bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  CK(cudaEventRecord(ctx->out_ready, ctx->stream));
+  CK(cudaStreamWaitEvent(ctx->copy_out, ctx->out_ready, 0));
+  CK(cudaMemcpyAsync(host, ctx->out_stage, bytes, cudaMemcpyDeviceToHost, ctx->copy_out));
+  CK(cudaEventRecord(ctx->out_free, ctx->copy_out));
+  return SCLET_OK;
+}
+
+int sclet_set_fields(sclet_ctx *ctx, const double *host) {
+  int rc = sclet_set_fields_async(ctx, host);
+  if (rc != SCLET_OK) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return SCLET_OK;
+}
+
+int sclet_get_fields(sclet_ctx *ctx, double *host) {
+  int rc = sclet_get_fields_async(ctx, host);
+  if (rc != SCLET_OK) return rc;
+  CK(cudaStreamSynchronize(ctx->copy_out));
+  return SCLET_OK;
+}
 
 const char *sclet_last_error(const sclet_ctx *ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
 
@@ -297,12 +394,14 @@ void sclet_destroy(sclet_ctx *ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->copy_in) cudaStreamSynchronize(ctx->copy_in);
+  if (ctx->copy_out) cudaStreamSynchronize(ctx->copy_out);
   void *bufs[] = {ctx->state2, ctx->rhs2, ctx->A, ctx->B, ctx->felas, ctx->scratch, ctx->shell, ctx->elam,
                   ctx->partials, ctx->diag, ctx->phi1[0], ctx->phi1[1], ctx->phi2[0], ctx->phi2[1], ctx->dev_err,
                   ctx->fstate2, ctx->frhs2, ctx->ffelas, ctx->fscratch, ctx->fshell, ctx->W1, ctx->W2, ctx->P,
                   ctx->scaleP, ctx->rsV, ctx->rsVi, ctx->matV, ctx->matVi, ctx->stage64,
                   ctx->coef[0], ctx->coef[1], ctx->coef2[0], ctx->coef2[1], ctx->massW, ctx->massPart,
-                  ctx->massRes};
+                  ctx->massRes, ctx->in_stage, ctx->out_stage};
   for (void *b : bufs) cudaFree(b);
   for (int a = 0; a < 3; a++) {
     cudaFree(ctx->V[a]);
@@ -314,6 +413,11 @@ void sclet_destroy(sclet_ctx *ctx) {
     cudaEventDestroy(e.b);
   }
   elastic_plan_destroy(ctx->elastic);
+  cudaEvent_t ioev[] = {ctx->in_ready, ctx->in_free, ctx->out_ready, ctx->out_free};
+  for (cudaEvent_t e : ioev)
+    if (e) cudaEventDestroy(e);
+  if (ctx->copy_in) cudaStreamDestroy(ctx->copy_in);
+  if (ctx->copy_out) cudaStreamDestroy(ctx->copy_out);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -923,6 +1027,8 @@ int sclet_mode_product(sclet_ctx *ctx, int inverse, const double *in, double *ou
 
 int sclet_sync(sclet_ctx *ctx) {
   CK(cudaStreamSynchronize(ctx->stream));
+  if (ctx->copy_in) CK(cudaStreamSynchronize(ctx->copy_in));
+  if (ctx->copy_out) CK(cudaStreamSynchronize(ctx->copy_out));
   int e = 0;
   CK(cudaMemcpyAsync(&e, ctx->dev_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));

@@ -70,6 +70,10 @@ SIGNATURES = {
     "sclet_chk_path": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_int, ctypes.c_int]),
     "sclet_field2b_path": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_int,
                                           ctypes.c_int, ctypes.c_int]),
+    "sclet_set_fields": (ctypes.c_int, [ctypes.c_void_p, _c_dp]),
+    "sclet_get_fields": (ctypes.c_int, [ctypes.c_void_p, _c_dp]),
+    "sclet_set_fields_async": (ctypes.c_int, [ctypes.c_void_p, _c_dp]),
+    "sclet_get_fields_async": (ctypes.c_int, [ctypes.c_void_p, _c_dp]),
     "sclet_write_vtk_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _c_dp]),
     "sclet_write_vtk": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]),
     "sclet_append_soln_log": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, _c_dp, _c_dp]),
@@ -206,18 +210,28 @@ class Solver:
     def _kind(self, f: int):
         return (AC, f) if f < self.nac else (CH, f - self.nac)
 
+    def _fields_arg(self, u: np.ndarray) -> np.ndarray:
+        if u.shape != (self.F, self.n, self.n, self.n) or u.dtype != np.float64 or not u.flags.c_contiguous:
+            raise ValueError(f"expected a C-contiguous float64 array of shape {(self.F, self.n, self.n, self.n)}")
+        return u
+
     def set_fields(self, u: np.ndarray):
-        for f in range(self.F):
-            k, m = self._kind(f)
-            self._ck(self.L.sclet_set_field(self.h, k, m, _dp(np.ascontiguousarray(u[f], dtype=np.float64))),
-                     "set_field")
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        self._ck(self.L.sclet_set_fields(self.h, _dp(self._fields_arg(u))), "set_fields")
 
     def get_fields(self) -> np.ndarray:
         out = np.zeros((self.F, self.n, self.n, self.n))
-        for f in range(self.F):
-            k, m = self._kind(f)
-            self._ck(self.L.sclet_get_field(self.h, k, m, _dp(out[f])), "get_field")
+        self._ck(self.L.sclet_get_fields(self.h, _dp(out)), "get_fields")
         return out
+
+    def set_fields_async(self, u: np.ndarray):
+        """Queues the state's replacement by u (kept alive and unchanged by the
+        caller until sync); page-locked u (PinnedArray) overlaps the steps."""
+        self._ck(self.L.sclet_set_fields_async(self.h, _dp(self._fields_arg(u))), "set_fields_async")
+
+    def get_fields_async(self, out: np.ndarray):
+        """Queues the copy of the state into out, complete after sync."""
+        self._ck(self.L.sclet_get_fields_async(self.h, _dp(self._fields_arg(out))), "get_fields_async")
 
     def load_restart_dir(self, case_dir: str, restart_iter: int = 0):
         """init_field with restart = 1: ./input/field_iter{it}_{ac|ch}{m}_000.txt"""

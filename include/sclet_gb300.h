@@ -152,6 +152,22 @@ void *sclet_stream(const sclet_ctx *ctx);
 /* ---- state transfer (host <-> device) ---------------------------------- */
 int sclet_set_field(sclet_ctx *ctx, int kind, int m, const double *block);
 int sclet_get_field(sclet_ctx *ctx, int kind, int m, double *block);
+/* No counterpart in the reference, whose fields live in host memory.  All
+ * fields at once: host holds field-count blocks of n^3 doubles, AC fields
+ * first.  sclet_set_fields returns when the state holds them;
+ * sclet_get_fields when host holds the state. */
+int sclet_set_fields(sclet_ctx *ctx, const double *host);
+int sclet_get_fields(sclet_ctx *ctx, double *host);
+/* Pipelined forms: the copies run on copy engines on one stream per direction
+ * (overlapping the steps when host is page-locked, sclet_host_alloc) through
+ * an FP64 staging area per direction, allocated on first use.  In the
+ * context's stream order, set_fields_async replaces the state and
+ * get_fields_async reads it, so a caller may queue
+ *   set(step k+1 inputs) while step k runs, and get(step k results) before it;
+ * host must stay valid and unchanged (set) or unread (get) until sclet_sync
+ * returns, which waits for both copy streams too. */
+int sclet_set_fields_async(sclet_ctx *ctx, const double *host);
+int sclet_get_fields_async(sclet_ctx *ctx, double *host);
 /* init_field with restart = 1 (field.c:743-755): interior from text. */
 int sclet_load_restart(sclet_ctx *ctx, int kind, int m, const char *path);
 

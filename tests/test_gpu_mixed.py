@@ -114,3 +114,46 @@ def test_fp32_elastic_force_matches_fp64(big_n, sclet_lib):
     for m in range(case.nac):
         err = rel(out[sg.MIXED][m], out[sg.FP64][m])
         assert err <= 2e-6, (big_n, m, err)
+
+
+@pytest.mark.parametrize("precision_name", ["FP64", "MIXED"])
+def test_pipelined_field_transfers(precision_name, sclet_lib):
+    """set/get_fields(_async) of all fields against the per-field accessors,
+    and a pipelined loop (inputs of step k+1 queued while step k runs)
+    against the same calls made synchronously on a second context with the
+    same history (the elastic ghost shell carries state between calls)."""
+    sg = sclet_lib
+    prec = getattr(sg, precision_name)
+    case = bench.workload(24, seed=21)
+    p = params_for(sg, case)
+    u0 = bench.block_fields(case)
+    s = sg.Solver(p, prec)
+    s.set_fields(u0)
+    per_field = np.zeros_like(u0)
+    for f in range(s.F):
+        k, m = s._kind(f)
+        assert s.L.sclet_get_field(s.h, k, m, sg._dp(per_field[f])) == 0
+    np.testing.assert_array_equal(s.get_fields(), per_field)
+    want = []
+    for k in range(3):
+        s.set_fields(u0)
+        s.step(k + 1)
+        want.append(s.get_fields())
+    s.close()
+    s = sg.Solver(p, prec)
+    s.set_fields(u0)
+    pin_in = sg.PinnedArray(u0.shape)
+    pin_in.array[...] = u0
+    outs = [sg.PinnedArray(u0.shape) for _ in range(3)]
+    s.set_fields_async(pin_in.array)
+    for k in range(3):
+        s.step(k + 1)
+        s.get_fields_async(outs[k].array)
+        if k < 2:
+            s.set_fields_async(pin_in.array)
+    s.sync()
+    for k in range(3):
+        np.testing.assert_array_equal(outs[k].array, want[k])
+    for a in outs + [pin_in]:
+        a.free()
+    s.close()
