@@ -65,6 +65,82 @@ constexpr int MAXF = 5;
 // eng_ac.s, eng_ac.c, eng_ch.s, eng_ch.c
 __host__ __device__ inline int rec_len(int F) { return 4 * F + 4; }
 
+// Reduction of the record (per field max, min, vol; two energies): warp
+// butterflies, then the block's warps in lane order; fixed shape, so the
+// result is deterministic.  TwoSum is exact and symmetric, so every lane of
+// a butterfly holds the same pair.
+__device__ __forceinline__ void block_record(double (&mxd)[MAXF], double (&mnd)[MAXF], KS (&vol)[MAXF], KS eac, KS ech,
+                                             int F, double *__restrict__ part) {
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const int lane = tid & 31, wid = tid >> 5;
+  constexpr int NW = EB / 32;
+  __shared__ double wrec[NW][4 * MAXF + 4];
+  auto shfl_ks = [](KS v, int off) {
+    KS o;
+    o.s = __shfl_xor_sync(0xffffffffu, v.s, off);
+    o.c = __shfl_xor_sync(0xffffffffu, v.c, off);
+    return ks_merge(v, o);
+  };
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+    for (int f = 0; f < MAXF; f++) {
+      mxd[f] = fmax(mxd[f], __shfl_xor_sync(0xffffffffu, mxd[f], off));
+      mnd[f] = fmin(mnd[f], __shfl_xor_sync(0xffffffffu, mnd[f], off));
+      vol[f] = shfl_ks(vol[f], off);
+    }
+    eac = shfl_ks(eac, off);
+    ech = shfl_ks(ech, off);
+  }
+  if (lane == 0) {
+    for (int f = 0; f < F; f++) {
+      wrec[wid][4 * f] = mxd[f];
+      wrec[wid][4 * f + 1] = mnd[f];
+      wrec[wid][4 * f + 2] = vol[f].s;
+      wrec[wid][4 * f + 3] = vol[f].c;
+    }
+    wrec[wid][4 * F] = eac.s;
+    wrec[wid][4 * F + 1] = eac.c;
+    wrec[wid][4 * F + 2] = ech.s;
+    wrec[wid][4 * F + 3] = ech.c;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    const int src = lane < NW ? lane : 0;  // lanes beyond the warp count repeat warp 0 (idempotent for max/min)
+    double *dst = part + (long long)blockIdx.x * rec_len(F);
+    for (int f = 0; f < F; f++) {
+      double a = wrec[src][4 * f], b = wrec[src][4 * f + 1];
+      KS v = {lane < NW ? wrec[src][4 * f + 2] : 0.0, lane < NW ? wrec[src][4 * f + 3] : 0.0};
+#pragma unroll
+      for (int off = NW / 2; off > 0; off >>= 1) {
+        a = fmax(a, __shfl_xor_sync(0xffffffffu, a, off));
+        b = fmin(b, __shfl_xor_sync(0xffffffffu, b, off));
+        v = shfl_ks(v, off);
+      }
+      if (lane == 0) {
+        dst[4 * f] = a;
+        dst[4 * f + 1] = b;
+        dst[4 * f + 2] = v.s;
+        dst[4 * f + 3] = v.c;
+      }
+    }
+    KS ea = {lane < NW ? wrec[src][4 * F] : 0.0, lane < NW ? wrec[src][4 * F + 1] : 0.0};
+    KS eb = {lane < NW ? wrec[src][4 * F + 2] : 0.0, lane < NW ? wrec[src][4 * F + 3] : 0.0};
+#pragma unroll
+    for (int off = NW / 2; off > 0; off >>= 1) {
+      ea = shfl_ks(ea, off);
+      eb = shfl_ks(eb, off);
+    }
+    if (lane == 0) {
+      dst[4 * F] = ea.s;
+      dst[4 * F + 1] = ea.c;
+      dst[4 * F + 2] = eb.s;
+      dst[4 * F + 3] = eb.c;
+    }
+  }
+}
+
+
 template <typename T>
 __global__ void __launch_bounds__(EB) energy_partial_kernel(Phys ph, const T *__restrict__ u, const double *__restrict__ elam,
                                                             int form, double *__restrict__ part) {
@@ -187,76 +263,199 @@ __global__ void __launch_bounds__(EB) energy_partial_kernel(Phys ph, const T *__
     vol[f].c = 0.0;
     ks_add(vol[f], (double)cnt * (sh + 1.0));
   }
-  // Reduction of the record (per field max, min, vol; two energies): warp
-  // butterflies, then the block's warps in lane order; fixed shape, so the
-  // result is deterministic.  TwoSum is exact and symmetric, so every lane of
-  // a butterfly holds the same pair.
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  constexpr int NW = EB / 32;
-  __shared__ double wrec[NW][4 * MAXF + 4];
-  auto shfl_ks = [](KS v, int off) {
-    KS o;
-    o.s = __shfl_xor_sync(0xffffffffu, v.s, off);
-    o.c = __shfl_xor_sync(0xffffffffu, v.c, off);
-    return ks_merge(v, o);
-  };
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-#pragma unroll
-    for (int f = 0; f < MAXF; f++) {
-      mxd[f] = fmax(mxd[f], __shfl_xor_sync(0xffffffffu, mxd[f], off));
-      mnd[f] = fmin(mnd[f], __shfl_xor_sync(0xffffffffu, mnd[f], off));
-      vol[f] = shfl_ks(vol[f], off);
-    }
-    eac = shfl_ks(eac, off);
-    ech = shfl_ks(ech, off);
-  }
-  if (lane == 0) {
-    for (int f = 0; f < F; f++) {
-      wrec[wid][4 * f] = mxd[f];
-      wrec[wid][4 * f + 1] = mnd[f];
-      wrec[wid][4 * f + 2] = vol[f].s;
-      wrec[wid][4 * f + 3] = vol[f].c;
-    }
-    wrec[wid][4 * F] = eac.s;
-    wrec[wid][4 * F + 1] = eac.c;
-    wrec[wid][4 * F + 2] = ech.s;
-    wrec[wid][4 * F + 3] = ech.c;
+  block_record(mxd, mnd, vol, eac, ech, F, part);
+}
+
+// ---- FP32 states: z-marching form of the same reduction --------------------
+//
+// A CTA of 32 x 8 threads owns 32 x 8 owned (x, y) columns of one unit and
+// walks its ZCH planes in z.  Each thread keeps the (x, y), (x, y + 1) values
+// of plane z and z + 1 of every field in registers and takes the x + 1
+// neighbours from the next lane, so a cell costs two loads per field instead
+// of eight.  The conserved field's corner average is an exact FP32 pair sum
+// finished in pair arithmetic (no FP64 instructions per cell).  Blocks loop
+// over units; one partial record per block, the same layout as above.
+constexpr int EZ = 8;  // planes per unit
+
+__host__ __device__ inline int energy_units(int N) { return ((N + 31) / 32) * ((N + 7) / 8) * ((N + EZ - 1) / EZ); }
+
+struct Pair {
+  float s, e;
+};
+// exact running sum of floats (TwoSum, Knuth)
+__device__ __forceinline__ void pair_add(Pair &p, float v) {
+  const float t = p.s + v, bp = t - p.s;
+  p.e += (p.s - (t - bp)) + (v - bp);
+  p.s = t;
+}
+// (a.s + a.e) + (b.s + b.e) rounded to float
+__device__ __forceinline__ float pair_sum(Pair a, Pair b) {
+  const float t = a.s + b.s, bp = t - a.s;
+  const float err = (a.s - (t - bp)) + (b.s - bp);
+  return t + (err + a.e + b.e);
+}
+
+template <int NAC, int NCH>
+__global__ void __launch_bounds__(256, 2) energy_partial_f32(Phys ph, const float *__restrict__ u,
+                                                             const double *__restrict__ elam, int form,
+                                                             double *__restrict__ part) {
+  constexpr int F = NAC + NCH;
+  const int n = ph.n, N = n - 4;
+  const long long n3 = (long long)n * n * n;
+  __shared__ float q6[4][6];  // half epn2 times the symmetrised gradient tensors: xx yy zz xy xz yz
+  if (threadIdx.x < 4 * 6 && threadIdx.y == 0) {
+    const int m = threadIdx.x / 6, c = threadIdx.x % 6;
+    const double *L = elam + 9 * m;
+    const double v = c == 0 ? L[0] : c == 1 ? L[4] : c == 2 ? L[8] : c == 3 ? L[1] + L[3] : c == 4 ? L[2] + L[6] : L[5] + L[7];
+    q6[m][c] = (float)(0.5 * ph.epn2 * v);
   }
   __syncthreads();
-  if (wid == 0) {
-    const int src = lane < NW ? lane : 0;  // lanes beyond the warp count repeat warp 0 (idempotent for max/min)
-    double *dst = part + (long long)blockIdx.x * rec_len(F);
+  const float i4hx = (float)(0.25 / ph.h[0]), i4hy = (float)(0.25 / ph.h[1]), i4hz = (float)(0.25 / ph.h[2]);
+  const float half_epn2 = (float)(0.5 * ph.epn2);
+  const float a2h = (float)(ph.a2 / 2.0), a4q = (float)(ph.a4 / 4.0), a6s = (float)(ph.a6 / 6.0), g = (float)ph.g;
+  const float th = (float)ph.th, Ah = (float)(ph.A / 2.0);
+  const float p2 = (float)(2376.0 / 2372.0 / 2.0), p3 = (float)((7128.0 + 12.0 * 2372.0) / 2372.0 / 3.0),
+              p4 = (float)((4752.0 + 12.0 * 2372.0) / 2372.0 / 4.0);
+  // cshift - c0 and cshift as float pairs
+  const double kd = ph.cshift - ph.c0;
+  const Pair kdp = {(float)kd, (float)(kd - (double)(float)kd)};
+  const Pair kcp = {(float)ph.cshift, (float)(ph.cshift - (double)(float)ph.cshift)};
+  float mx[F], mn[F];
+  Acc<float> vsum[F], eac_p, ech_p;
+  int cnt = 0;
+#pragma unroll
+  for (int f = 0; f < F; f++) {
+    mx[f] = -1.0e30f;
+    mn[f] = 1.0e30f;
+  }
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int nti = (N + 31) / 32, ntj = (N + 7) / 8, units = energy_units(N);
+  for (int unit = blockIdx.x; unit < units; unit += gridDim.x) {
+    const int ti = unit % nti, tj = (unit / nti) % ntj, zc = unit / (nti * ntj);
+    const int i = 2 + ti * 32 + tx, j = 2 + tj * 8 + ty;
+    const bool own = i <= n - 3 && j <= n - 3, inner = i <= n - 4 && j <= n - 4;
+    const int ic = i < n - 2 ? i : n - 2, jc = j < n - 2 ? j : n - 2;  // clamped: loads stay inside the block
+    const int k0 = 2 + zc * EZ, k1 = k0 + EZ < n - 2 ? k0 + EZ : n - 2;
+    float a0[F], a1[F], a2[F], a3[F];  // plane k: (i, j) (i+1, j) (i, j+1) (i+1, j+1)
+    const long long row0 = ((long long)k0 * n + jc) * n + ic;
+#pragma unroll
     for (int f = 0; f < F; f++) {
-      double a = wrec[src][4 * f], b = wrec[src][4 * f + 1];
-      KS v = {lane < NW ? wrec[src][4 * f + 2] : 0.0, lane < NW ? wrec[src][4 * f + 3] : 0.0};
-#pragma unroll
-      for (int off = NW / 2; off > 0; off >>= 1) {
-        a = fmax(a, __shfl_xor_sync(0xffffffffu, a, off));
-        b = fmin(b, __shfl_xor_sync(0xffffffffu, b, off));
-        v = shfl_ks(v, off);
-      }
-      if (lane == 0) {
-        dst[4 * f] = a;
-        dst[4 * f + 1] = b;
-        dst[4 * f + 2] = v.s;
-        dst[4 * f + 3] = v.c;
+      const float *q = u + f * n3 + row0;
+      a0[f] = q[0];
+      a2[f] = q[n];
+      a1[f] = __shfl_down_sync(0xffffffffu, a0[f], 1);
+      a3[f] = __shfl_down_sync(0xffffffffu, a2[f], 1);
+      if (tx == 31) {
+        a1[f] = q[1];
+        a3[f] = q[n + 1];
       }
     }
-    KS ea = {lane < NW ? wrec[src][4 * F] : 0.0, lane < NW ? wrec[src][4 * F + 1] : 0.0};
-    KS eb = {lane < NW ? wrec[src][4 * F + 2] : 0.0, lane < NW ? wrec[src][4 * F + 3] : 0.0};
+    for (int k = k0; k < k1; k++) {
+      float b0[F], b1[F], b2[F], b3[F];  // plane k + 1
+      const long long row = ((long long)(k + 1) * n + jc) * n + ic;
 #pragma unroll
-    for (int off = NW / 2; off > 0; off >>= 1) {
-      ea = shfl_ks(ea, off);
-      eb = shfl_ks(eb, off);
-    }
-    if (lane == 0) {
-      dst[4 * F] = ea.s;
-      dst[4 * F + 1] = ea.c;
-      dst[4 * F + 2] = eb.s;
-      dst[4 * F + 3] = eb.c;
+      for (int f = 0; f < F; f++) {
+        const float *q = u + f * n3 + row;
+        b0[f] = q[0];
+        b2[f] = q[n];
+        b1[f] = __shfl_down_sync(0xffffffffu, b0[f], 1);
+        b3[f] = __shfl_down_sync(0xffffffffu, b2[f], 1);
+        if (tx == 31) {
+          b1[f] = q[1];
+          b3[f] = q[n + 1];
+        }
+      }
+      if (own) {
+        cnt++;
+#pragma unroll
+        for (int f = 0; f < F; f++) {
+          mx[f] = fmaxf(mx[f], a0[f]);
+          mn[f] = fminf(mn[f], a0[f]);
+          vsum[f].add(a0[f]);
+        }
+      }
+      if (inner && k <= n - 4) {
+        float avg[F > 0 ? F : 1];
+        float e_ac = 0.0f, e_ch = 0.0f, cd = 0.0f, cval = 0.0f;
+#pragma unroll
+        for (int f = 0; f < F; f++) {
+          const float v0 = a0[f], v1 = a1[f], v2 = a2[f], v3 = a3[f], v4 = b0[f], v5 = b1[f], v6 = b2[f], v7 = b3[f];
+          avg[f] = (((v0 + v1) + (v2 + v3)) + ((v4 + v5) + (v6 + v7))) * 0.125f;
+          const float ux = ((v1 - v0) + (v3 - v2) + (v5 - v4) + (v7 - v6)) * i4hx;
+          const float uy = ((v2 - v0) + (v3 - v1) + (v6 - v4) + (v7 - v5)) * i4hy;
+          const float uz = ((v4 - v0) + (v5 - v1) + (v6 - v2) + (v7 - v3)) * i4hz;
+          if (f < NAC) {
+            const float *qm = q6[f];
+            e_ac += qm[0] * ux * ux + qm[1] * uy * uy + qm[2] * uz * uz + qm[3] * ux * uy + qm[4] * ux * uz +
+                    qm[5] * uy * uz;
+          } else {
+            const float gr = half_epn2 * (ux * ux + uy * uy + uz * uz);
+            if (form == 0) e_ch += gr;
+            else e_ac += gr;
+            // exact corner sum, then (sum / 8 + cshift - c0) and (sum / 8 + cshift)
+            Pair cs = {v0, 0.0f};
+            pair_add(cs, v1);
+            pair_add(cs, v2);
+            pair_add(cs, v3);
+            pair_add(cs, v4);
+            pair_add(cs, v5);
+            pair_add(cs, v6);
+            pair_add(cs, v7);
+            cs.s *= 0.125f;
+            cs.e *= 0.125f;
+            cd = pair_sum(cs, kdp);
+            cval = pair_sum(cs, kcp);
+          }
+        }
+        if (form == 0) {
+          if (NAC > 0) {
+            float s2 = 0.0f, s3 = 0.0f;
+#pragma unroll
+            for (int f = 0; f < (NAC < 4 ? NAC : 4); f++) {
+              s2 += avg[f] * avg[f];
+              s3 += avg[f] * avg[f] * avg[f];
+            }
+            e_ac += p2 * s2 - p3 * s3 + p4 * s2 * s2;
+          }
+          if (NCH > 0) e_ch += (cval * cval - 1.0f) * (cval * cval - 1.0f) * 0.25f;
+        } else {
+          float fl = 0.0f, s2 = 0.0f;
+#pragma unroll
+          for (int m = 0; m < (NAC < 4 ? NAC : 4); m++) {
+            const float u2 = avg[m] * avg[m];
+            s2 += u2;
+            fl += a2h * u2 + a4q * u2 * u2 + a6s * u2 * u2 * u2;
+#pragma unroll
+            for (int q = m + 1; q < (NAC < 4 ? NAC : 4); q++) fl += g * u2 * avg[q] * avg[q];
+          }
+          if (NCH > 0) fl += Ah * cd * cd - th * cd * s2;
+          e_ac += fl;
+        }
+        eac_p.add(e_ac);
+        ech_p.add(e_ch);
+      }
+#pragma unroll
+      for (int f = 0; f < F; f++) {
+        a0[f] = b0[f];
+        a1[f] = b1[f];
+        a2[f] = b2[f];
+        a3[f] = b3[f];
+      }
     }
   }
+  // the record of this block, reduced as in energy_partial_kernel
+  double mxd[MAXF], mnd[MAXF];
+  KS vol[MAXF], eac = {eac_p.value(), 0.0}, ech = {ech_p.value(), 0.0};
+#pragma unroll
+  for (int f = 0; f < MAXF; f++) {
+    const double sh = f >= NAC ? ph.cshift : 0.0;
+    mxd[f] = f < F ? (double)mx[f < F ? f : 0] + sh : -1.0e30;
+    mnd[f] = f < F ? (double)mn[f < F ? f : 0] + sh : 1.0e30;
+    vol[f].s = f < F ? vsum[f < F ? f : 0].value() : 0.0;
+    vol[f].c = 0.0;
+    ks_add(vol[f], (double)cnt * (sh + 1.0));
+  }
+  block_record(mxd, mnd, vol, eac, ech, F, part);
 }
 
 // Final reduction over the block records: one block; each thread folds a
@@ -310,17 +509,38 @@ __global__ void __launch_bounds__(EB) energy_final_kernel(Phys ph, int form, con
   }
 }
 
+// partial records (blocks) of one reduction: four CTAs per SM at most
 int check_soln_partials(int n) {
-  long long N3 = (long long)(n - 4) * (n - 4) * (n - 4);
-  long long b = (N3 + EB - 1) / EB;
-  return (int)(b > 152 * 2 ? 152 * 2 : b);
+  const int u = energy_units(n - 4);
+  return u > 152 * 4 ? 152 * 4 : (u < 1 ? 1 : u);
+}
+
+template <int NAC, int NCH>
+static void launch_f32(const Phys &ph, const float *u, const double *elam, int form, double *partials, int npart,
+                       cudaStream_t s) {
+  energy_partial_f32<NAC, NCH><<<npart, dim3(32, 8), 0, s>>>(ph, u, elam, form, partials);
 }
 
 template <typename T>
 cudaError_t launch_check_soln(const Phys &ph, const T *u, const double *elam, int form, double *partials, int npart,
                               double *out, cudaStream_t s) {
-  if (ph.F > MAXF) return cudaErrorInvalidValue;
-  energy_partial_kernel<T><<<npart, EB, 0, s>>>(ph, u, elam, form, partials);
+  if (ph.F < 1 || ph.F > MAXF || ph.nac > 4 || ph.nch > 1) return cudaErrorInvalidValue;
+  if constexpr (sizeof(T) == 4) {
+    const float *uf = u;
+    switch (ph.nac * 2 + ph.nch) {
+      case 1: launch_f32<0, 1>(ph, uf, elam, form, partials, npart, s); break;
+      case 2: launch_f32<1, 0>(ph, uf, elam, form, partials, npart, s); break;
+      case 3: launch_f32<1, 1>(ph, uf, elam, form, partials, npart, s); break;
+      case 4: launch_f32<2, 0>(ph, uf, elam, form, partials, npart, s); break;
+      case 5: launch_f32<2, 1>(ph, uf, elam, form, partials, npart, s); break;
+      case 6: launch_f32<3, 0>(ph, uf, elam, form, partials, npart, s); break;
+      case 7: launch_f32<3, 1>(ph, uf, elam, form, partials, npart, s); break;
+      case 8: launch_f32<4, 0>(ph, uf, elam, form, partials, npart, s); break;
+      default: launch_f32<4, 1>(ph, uf, elam, form, partials, npart, s); break;
+    }
+  } else {
+    energy_partial_kernel<T><<<npart, EB, 0, s>>>(ph, u, elam, form, partials);
+  }
   energy_final_kernel<<<1, EB, 0, s>>>(ph, form, partials, npart, out);
   launch_counter() += 2;
   return cudaGetLastError();
