@@ -58,6 +58,15 @@ struct Acc<float> {
     s = t;
   }
   __device__ double value() const { return (double)s + (double)e; }
+  // pair sum with the partner lane at xor distance off; both lanes end with
+  // the same pair (TwoSum is exact and the merge symmetric)
+  __device__ void merge_lane(int off) {
+    const float os = __shfl_xor_sync(0xffffffffu, s, off), oe = __shfl_xor_sync(0xffffffffu, e, off);
+    const float t = s + os, bp = t - s;
+    const float err = (s - (t - bp)) + (os - bp);
+    e = (e + oe) + err;
+    s = t;
+  }
 };
 constexpr int MAXF = 5;
 
@@ -69,29 +78,21 @@ __host__ __device__ inline int rec_len(int F) { return 4 * F + 4; }
 // butterflies, then the block's warps in lane order; fixed shape, so the
 // result is deterministic.  TwoSum is exact and symmetric, so every lane of
 // a butterfly holds the same pair.
-__device__ __forceinline__ void block_record(double (&mxd)[MAXF], double (&mnd)[MAXF], KS (&vol)[MAXF], KS eac, KS ech,
-                                             int F, double *__restrict__ part) {
+__device__ __forceinline__ KS shfl_ks(KS v, int off) {
+  KS o;
+  o.s = __shfl_xor_sync(0xffffffffu, v.s, off);
+  o.c = __shfl_xor_sync(0xffffffffu, v.c, off);
+  return ks_merge(v, o);
+}
+
+// Lane 0 of every warp holds its warp's values: the block's record.
+__device__ __forceinline__ void block_record_from_warps(const double (&mxd)[MAXF], const double (&mnd)[MAXF],
+                                                        const KS (&vol)[MAXF], KS eac, KS ech, int F,
+                                                        double *__restrict__ part) {
   const int tid = threadIdx.y * blockDim.x + threadIdx.x;
   const int lane = tid & 31, wid = tid >> 5;
   constexpr int NW = EB / 32;
   __shared__ double wrec[NW][4 * MAXF + 4];
-  auto shfl_ks = [](KS v, int off) {
-    KS o;
-    o.s = __shfl_xor_sync(0xffffffffu, v.s, off);
-    o.c = __shfl_xor_sync(0xffffffffu, v.c, off);
-    return ks_merge(v, o);
-  };
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-#pragma unroll
-    for (int f = 0; f < MAXF; f++) {
-      mxd[f] = fmax(mxd[f], __shfl_xor_sync(0xffffffffu, mxd[f], off));
-      mnd[f] = fmin(mnd[f], __shfl_xor_sync(0xffffffffu, mnd[f], off));
-      vol[f] = shfl_ks(vol[f], off);
-    }
-    eac = shfl_ks(eac, off);
-    ech = shfl_ks(ech, off);
-  }
   if (lane == 0) {
     for (int f = 0; f < F; f++) {
       wrec[wid][4 * f] = mxd[f];
@@ -138,6 +139,22 @@ __device__ __forceinline__ void block_record(double (&mxd)[MAXF], double (&mnd)[
       dst[4 * F + 3] = eb.c;
     }
   }
+}
+
+__device__ __forceinline__ void block_record(double (&mxd)[MAXF], double (&mnd)[MAXF], KS (&vol)[MAXF], KS eac, KS ech,
+                                             int F, double *__restrict__ part) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+    for (int f = 0; f < MAXF; f++) {
+      mxd[f] = fmax(mxd[f], __shfl_xor_sync(0xffffffffu, mxd[f], off));
+      mnd[f] = fmin(mnd[f], __shfl_xor_sync(0xffffffffu, mnd[f], off));
+      vol[f] = shfl_ks(vol[f], off);
+    }
+    eac = shfl_ks(eac, off);
+    ech = shfl_ks(ech, off);
+  }
+  block_record_from_warps(mxd, mnd, vol, eac, ech, F, part);
 }
 
 
@@ -443,36 +460,52 @@ __global__ void __launch_bounds__(256, 2) energy_partial_f32(Phys ph, const floa
       }
     }
   }
-  // the record of this block, reduced as in energy_partial_kernel
-  double mxd[MAXF], mnd[MAXF];
-  KS vol[MAXF], eac = {eac_p.value(), 0.0}, ech = {ech_p.value(), 0.0};
+  // warp butterflies in FP32 (max, min) and exact-pair arithmetic (sums),
+  // then the warps' values in FP64 as in energy_partial_kernel
 #pragma unroll
-  for (int f = 0; f < MAXF; f++) {
-    const double sh = f >= NAC ? ph.cshift : 0.0;
-    mxd[f] = f < F ? (double)mx[f < F ? f : 0] + sh : -1.0e30;
-    mnd[f] = f < F ? (double)mn[f < F ? f : 0] + sh : 1.0e30;
-    vol[f].s = f < F ? vsum[f < F ? f : 0].value() : 0.0;
-    vol[f].c = 0.0;
-    ks_add(vol[f], (double)cnt * (sh + 1.0));
+  for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+    for (int f = 0; f < F; f++) {
+      mx[f] = fmaxf(mx[f], __shfl_xor_sync(0xffffffffu, mx[f], off));
+      mn[f] = fminf(mn[f], __shfl_xor_sync(0xffffffffu, mn[f], off));
+      vsum[f].merge_lane(off);
+    }
+    eac_p.merge_lane(off);
+    ech_p.merge_lane(off);
+    cnt += __shfl_xor_sync(0xffffffffu, cnt, off);
   }
-  block_record(mxd, mnd, vol, eac, ech, F, part);
+  double mxd[MAXF], mnd[MAXF];
+  KS vol[MAXF], eac = {0.0, 0.0}, ech = {0.0, 0.0};
+  if ((threadIdx.x & 31) == 0) {
+    eac = KS{(double)eac_p.s, (double)eac_p.e};
+    ech = KS{(double)ech_p.s, (double)ech_p.e};
+#pragma unroll
+    for (int f = 0; f < MAXF; f++) {
+      const double sh = f >= NAC ? ph.cshift : 0.0;
+      mxd[f] = f < F ? (double)mx[f < F ? f : 0] + sh : -1.0e30;
+      mnd[f] = f < F ? (double)mn[f < F ? f : 0] + sh : 1.0e30;
+      vol[f] = f < F ? KS{(double)vsum[f < F ? f : 0].s, (double)vsum[f < F ? f : 0].e} : KS{0.0, 0.0};
+      ks_add(vol[f], (double)cnt * (sh + 1.0));
+    }
+  }
+  block_record_from_warps(mxd, mnd, vol, eac, ech, F, part);
 }
 
-// Final reduction over the block records: one block; each thread folds a
-// fixed strided subset of the records, then a fixed-shape tree (deterministic).
-__global__ void __launch_bounds__(EB) energy_final_kernel(Phys ph, int form, const double *__restrict__ part, int npart,
-                                                          double *__restrict__ out) {
+// Final reduction over the block records: one warp per quantity (per field
+// max, min, vol; the two energies); each lane folds a fixed strided subset of
+// the records, then a butterfly (deterministic).
+__global__ void energy_final_kernel(Phys ph, int form, const double *__restrict__ part, int npart,
+                                    double *__restrict__ out) {
   const int F = ph.F, L = rec_len(F);
   const double h3 = ph.h[0] * ph.h[1] * ph.h[2];
-  __shared__ double sa[EB], sb[EB];
   __shared__ double res[4 * MAXF + 4];
-  // quantities: per field max (0), min (1), vol (2); then eng_ac, eng_ch
+  const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nq = 3 * F + 2;
-  for (int q = 0; q < nq; q++) {
+  if (q < nq) {
     const int f = q < 3 * F ? q / 3 : -1, kind = q < 3 * F ? q % 3 : 3 + (q - 3 * F);
     double m = kind == 0 ? -1.0e30 : (kind == 1 ? 1.0e30 : 0.0);
     KS k = {0, 0};
-    for (int b = threadIdx.x; b < npart; b += EB) {
+    for (int b = lane; b < npart; b += 32) {
       const double *r = part + (long long)b * L;
       if (kind == 0) m = fmax(m, r[4 * f]);
       else if (kind == 1) m = fmin(m, r[4 * f + 1]);
@@ -480,24 +513,15 @@ __global__ void __launch_bounds__(EB) energy_final_kernel(Phys ph, int form, con
       else if (kind == 3) k = ks_merge(k, KS{r[4 * F], r[4 * F + 1]});
       else k = ks_merge(k, KS{r[4 * F + 2], r[4 * F + 3]});
     }
-    sa[threadIdx.x] = kind < 2 ? m : k.s;
-    sb[threadIdx.x] = k.c;
-    __syncthreads();
-    for (int w = EB / 2; w > 0; w >>= 1) {
-      if (threadIdx.x < w) {
-        if (kind == 0) sa[threadIdx.x] = fmax(sa[threadIdx.x], sa[threadIdx.x + w]);
-        else if (kind == 1) sa[threadIdx.x] = fmin(sa[threadIdx.x], sa[threadIdx.x + w]);
-        else {
-          KS x = ks_merge(KS{sa[threadIdx.x], sb[threadIdx.x]}, KS{sa[threadIdx.x + w], sb[threadIdx.x + w]});
-          sa[threadIdx.x] = x.s;
-          sb[threadIdx.x] = x.c;
-        }
-      }
-      __syncthreads();
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      if (kind == 0) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, off));
+      else if (kind == 1) m = fmin(m, __shfl_xor_sync(0xffffffffu, m, off));
+      else k = shfl_ks(k, off);
     }
-    if (threadIdx.x == 0) res[q] = kind < 2 ? sa[0] : sa[0] + sb[0];
-    __syncthreads();
+    if (lane == 0) res[q] = kind < 2 ? m : k.s + k.c;
   }
+  __syncthreads();
   if (threadIdx.x == 0) {
     for (int f = 0; f < F; f++) {
       out[4 * f] = res[3 * f];
@@ -541,7 +565,7 @@ cudaError_t launch_check_soln(const Phys &ph, const T *u, const double *elam, in
   } else {
     energy_partial_kernel<T><<<npart, EB, 0, s>>>(ph, u, elam, form, partials);
   }
-  energy_final_kernel<<<1, EB, 0, s>>>(ph, form, partials, npart, out);
+  energy_final_kernel<<<1, 32 * (3 * MAXF + 2), 0, s>>>(ph, form, partials, npart, out);
   launch_counter() += 2;
   return cudaGetLastError();
 }
