@@ -515,53 +515,80 @@ __device__ __forceinline__ float pow2_scale(float m) {
 // reduced by its nearest integer).
 constexpr int SLICE_MAXC = 17;  // column pairs per lane: rows of up to 32 * 2 * 17 = 1088 values
 
-// C = column-pair chunks per lane held in registers (C >= ceil(n / 64)).
+// C = column-pair chunks per lane held in registers (C >= ceil(n / 64)).  A
+// warp takes two adjacent rows at a time (both rows' loads in flight before
+// either is reduced); pairs of columns load as float2 when n is even.
 template <int C>
-__global__ void slice_fields_kernel(const float *__restrict__ x, const float *__restrict__ sub, float *__restrict__ scale,
-                                    __nv_bfloat16 *__restrict__ out, int n, int kp, int count, int bits) {
+__global__ void __launch_bounds__(256) slice_fields_kernel(const float *__restrict__ x, const float *__restrict__ sub,
+                                                           float *__restrict__ scale, __nv_bfloat16 *__restrict__ out,
+                                                           int n, int kp, int count, int bits) {
   const float step = ldexpf(1.0f, bits);
   const long long rows = (long long)n * n, total_rows = rows * count;
   const int lane = threadIdx.x & 31;
   const int chunks = (n + 63) / 64;
+  const bool pairs = (n & 1) == 0;  // every row starts on an 8-byte boundary
   const long long warp0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-  for (long long wr = warp0; wr < total_rows; wr += nwarps) {
-    const int t = (int)(wr / rows);
-    const long long row = wr - (long long)t * rows;
-    const long long in0 = wr * n;  // rows are contiguous lines of n
-    // the whole line in registers (one read), two columns per lane and chunk
-    float v0[C], v1[C];
-    float m = 0.0f;
+  for (long long w0 = 2 * warp0; w0 < total_rows; w0 += 2 * nwarps) {
+    // the two lines in registers (one read each), two columns per lane and chunk
+    float v0[2][C], v1[2][C];
+    float m[2] = {0.0f, 0.0f};
 #pragma unroll
-    for (int c = 0; c < C; c++) {
-      v0[c] = 0.0f;
-      v1[c] = 0.0f;
-      if (c < chunks) {
+    for (int h = 0; h < 2; h++) {
+      const long long wr = w0 + h;
+      const long long in0 = wr * n;  // rows are contiguous lines of n
+#pragma unroll
+      for (int c = 0; c < C; c++) {
+        v0[h][c] = 0.0f;
+        v1[h][c] = 0.0f;
         const int k = 2 * lane + 64 * c;
-        if (k < n) v0[c] = sub ? x[in0 + k] - sub[in0 + k] : x[in0 + k];
-        if (k + 1 < n) v1[c] = sub ? x[in0 + k + 1] - sub[in0 + k + 1] : x[in0 + k + 1];
-        m = fmaxf(m, fmaxf(fabsf(v0[c]), fabsf(v1[c])));
+        if (wr < total_rows && c < chunks && k < n) {
+          if (pairs) {
+            float2 a = *reinterpret_cast<const float2 *>(x + in0 + k);
+            if (sub) {
+              const float2 b = *reinterpret_cast<const float2 *>(sub + in0 + k);
+              a.x -= b.x;
+              a.y -= b.y;
+            }
+            v0[h][c] = a.x;
+            v1[h][c] = a.y;
+          } else {
+            v0[h][c] = sub ? x[in0 + k] - sub[in0 + k] : x[in0 + k];
+            if (k + 1 < n) v1[h][c] = sub ? x[in0 + k + 1] - sub[in0 + k + 1] : x[in0 + k + 1];
+          }
+        }
+        m[h] = fmaxf(m[h], fmaxf(fabsf(v0[h][c]), fabsf(v1[h][c])));
       }
     }
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
-    const float S = pow2_scale(m), inv = 1.0f / S;
-    if (lane == 0) scale[wr] = S;
-    const long long o0 = ((long long)t * TC_PLANES * rows + row) * kp;
-    // stored as bf16 pairs (kp is even; a pad column beyond n receives zero
-    // slices)
+    for (int off = 16; off > 0; off >>= 1) {
+      m[0] = fmaxf(m[0], __shfl_xor_sync(0xffffffffu, m[0], off));
+      m[1] = fmaxf(m[1], __shfl_xor_sync(0xffffffffu, m[1], off));
+    }
 #pragma unroll
-    for (int c = 0; c < C; c++) {
-      const int k = 2 * lane + 64 * c;
-      if (c < chunks && k < n) {
-        float r0 = v0[c] * inv, r1 = v1[c] * inv;
+    for (int h = 0; h < 2; h++) {
+      const long long wr = w0 + h;
+      if (wr >= total_rows) break;
+      const int t = (int)(wr / rows);
+      const long long row = wr - (long long)t * rows;
+      const float S = pow2_scale(m[h]), inv = 1.0f / S;
+      if (lane == 0) scale[wr] = S;
+      const long long o0 = ((long long)t * TC_PLANES * rows + row) * kp;
+      // stored as bf16 pairs (kp is even; a pad column beyond n receives zero
+      // slices)
 #pragma unroll
-        for (int p = 0; p < TC_PLANES; p++) {
-          const float y0 = r0 * step, y1 = r1 * step;
-          const float d0 = rintf(y0), d1 = rintf(y1);
-          r0 = y0 - d0;
-          r1 = y1 - d1;
-          *reinterpret_cast<__nv_bfloat162 *>(out + o0 + (long long)p * rows * kp + k) = __floats2bfloat162_rn(d0, d1);
+      for (int c = 0; c < C; c++) {
+        const int k = 2 * lane + 64 * c;
+        if (c < chunks && k < n) {
+          float r0 = v0[h][c] * inv, r1 = v1[h][c] * inv;
+#pragma unroll
+          for (int p = 0; p < TC_PLANES; p++) {
+            const float y0 = r0 * step, y1 = r1 * step;
+            const float d0 = rintf(y0), d1 = rintf(y1);
+            r0 = y0 - d0;
+            r1 = y1 - d1;
+            *reinterpret_cast<__nv_bfloat162 *>(out + o0 + (long long)p * rows * kp + k) = __floats2bfloat162_rn(d0, d1);
+          }
         }
       }
     }
@@ -1123,7 +1150,7 @@ cudaError_t tc_slice_matrix(const double *m, __nv_bfloat16 *planes, float *row_s
 cudaError_t tc_slice_fields(const float *x, const float *sub, float *scale, __nv_bfloat16 *planes, int n, int count,
                             cudaStream_t s) {
   if (n > 64 * tc::SLICE_MAXC) return cudaErrorInvalidValue;
-  long long warps = (long long)n * n * count;
+  long long warps = ((long long)n * n * count + 1) / 2;  // two rows per warp
   long long blocks = (warps * 32 + 255) / 256;
   int g = (int)(blocks > 152 * 32 ? 152 * 32 : blocks);
   const int chunks = (n + 63) / 64, kp = tc_kp(n), bits = tc_slice_bits(n);
