@@ -42,7 +42,11 @@ struct sclet_ctx {
   std::string err;
   // shared
   double *dd[3] = {nullptr, nullptr, nullptr};  // eigenvalues / h^2 (FP64)
-  double *elam = nullptr, *partials = nullptr, *diag = nullptr;
+  double *elam = nullptr, *partials = nullptr;
+  // the diagnostics record: page-locked host memory mapped into the device,
+  // written by the reduction kernel, so reading it needs no copy (a copy would
+  // queue behind large transfers on the copy engines)
+  double *diag_host = nullptr, *diag = nullptr;
   int npart = 0;
   ElasticPlan *elastic = nullptr;
   int *dev_err = nullptr;  // bounded-wait failures of device kernels
@@ -401,12 +405,13 @@ void sclet_destroy(sclet_ctx *ctx) {
   if (ctx->copy_in) cudaStreamSynchronize(ctx->copy_in);
   if (ctx->copy_out) cudaStreamSynchronize(ctx->copy_out);
   void *bufs[] = {ctx->state2, ctx->rhs2, ctx->A, ctx->B, ctx->felas, ctx->scratch, ctx->shell, ctx->elam,
-                  ctx->partials, ctx->diag, ctx->phi1[0], ctx->phi1[1], ctx->phi2[0], ctx->phi2[1], ctx->dev_err,
+                  ctx->partials, ctx->phi1[0], ctx->phi1[1], ctx->phi2[0], ctx->phi2[1], ctx->dev_err,
                   ctx->fstate2, ctx->frhs2, ctx->ffelas, ctx->fscratch, ctx->fshell, ctx->W1, ctx->W2, ctx->P,
                   ctx->scaleP, ctx->rsV, ctx->rsVi, ctx->matV, ctx->matVi, ctx->stage64,
                   ctx->coef[0], ctx->coef[1], ctx->coef2[0], ctx->coef2[1], ctx->massW, ctx->massPart,
                   ctx->massRes, ctx->in_stage, ctx->out_stage, ctx->lmax[0], ctx->lmax[1]};
   for (void *b : bufs) cudaFree(b);
+  if (ctx->diag_host) cudaFreeHost(ctx->diag_host);
   for (int a = 0; a < 3; a++) {
     cudaFree(ctx->V[a]);
     cudaFree(ctx->Vi[a]);
@@ -518,7 +523,8 @@ int sclet_create(const sclet_params *p, int precision, int device, sclet_ctx **o
   CC(cudaMalloc(&ctx->elam, sizeof(double) * 36));
   ctx->npart = check_soln_partials(n);
   CC(cudaMalloc(&ctx->partials, sizeof(double) * ctx->npart * (4 * F + 4)));
-  CC(cudaMalloc(&ctx->diag, sizeof(double) * 4 * F));
+  CC(cudaHostAlloc(&ctx->diag_host, sizeof(double) * 4 * F, cudaHostAllocMapped | cudaHostAllocPortable));
+  CC(cudaHostGetDevicePointer(&ctx->diag, ctx->diag_host, 0));
   CC(cudaMalloc(&ctx->dev_err, sizeof(int)));
   CC(cudaMemsetAsync(ctx->dev_err, 0, sizeof(int), s));
   const int nfel = ctx->nac > 0 ? ctx->nac : 1;
@@ -1057,9 +1063,8 @@ int queue_diagnostics(sclet_ctx *ctx, int energy_form) {
 
 // waits for the stream and copies the last diagnostics record out
 int read_diagnostics(sclet_ctx *ctx, sclet_diag *out) {
-  std::vector<double> h(4 * ctx->F);
-  CK(cudaMemcpyAsync(h.data(), ctx->diag, sizeof(double) * 4 * ctx->F, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  const double *h = ctx->diag_host;
   int nonfinite = 0;
   for (int f = 0; f < ctx->F; f++) {
     out[f].max = h[4 * f];
