@@ -52,9 +52,9 @@ import cases  # noqa: E402
 METRIC = "cell-updates/s on 1 GB300: mixed/learned vs plain FP64 at ≤1e-5 rel L2"
 UNIT = "cell-updates/s"
 # DRAM bytes (read + write) of one tensor-core product launch over its
-# algorithmic bytes, from an ncu capture at 160^3: (363.0 + 156.2) MB over
-# (361.4 + 176.4) MB.
-TC_TRAFFIC_RATIO = 0.965
+# algorithmic bytes, from an ncu capture of a five-tensor launch at 192^3:
+# (308.8 + 115.5) MB over 5 x 196^3 x (8 x 200 / 196 + 4) B = 458.0 MB.
+TC_TRAFFIC_RATIO = 0.926
 FP64_PEAK_TFLOPS = 1.25  # nominal GB300 FP64 rate (the measured peaks cover HBM and bf16 only)
 
 
@@ -266,8 +266,8 @@ def tc_roofline(case, stage_ms, stage_launches, steps):
         "bound": "hbm", "kernel": "modeprod_tc_kernel (split-BF16 tcgen05 eigenbasis products)",
         "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
         "traffic": per_launch * TC_TRAFFIC_RATIO,
-        "traffic_source": f"ncu DRAM read+write / algorithmic bytes = {TC_TRAFFIC_RATIO} on a 160^3 capture "
-                          "(profiles/modeprod_tc_160cubed.md), scaled to this launch size",
+        "traffic_source": f"ncu DRAM read+write / algorithmic bytes = {TC_TRAFFIC_RATIO} on one 192^3 launch of five "
+                          "tensors (--set full capture), scaled to this launch size",
         "peak_source": src, "avg_launch_ms": stage_ms["tc_kernel"] / launches,
         "algorithmic_bytes_per_launch": per_launch, "bytes_per_step": bytes_step,
         "tensor": {"algorithmic_tflops": flops_step * steps / t / 1e12,

@@ -312,8 +312,38 @@ __device__ __forceinline__ float pair_sum(Pair a, Pair b) {
   return t + (err + a.e + b.e);
 }
 
+// FP32 constants of energy_partial_f32, rounded once on the host (kernel
+// parameters: read from the constant bank, never recomputed in the loop)
+struct EConst {
+  float i4hx, i4hy, i4hz, half_epn2;
+  float a2h, a4q, a6s, g, th, Ah;
+  float p2, p3, p4;  // the 2-3-4 polynomial of energy form 0
+  Pair kdp, kcp;     // cshift - c0 and cshift as float pairs
+};
+
+static EConst econst(const Phys &ph) {
+  EConst c;
+  c.i4hx = (float)(0.25 / ph.h[0]);
+  c.i4hy = (float)(0.25 / ph.h[1]);
+  c.i4hz = (float)(0.25 / ph.h[2]);
+  c.half_epn2 = (float)(0.5 * ph.epn2);
+  c.a2h = (float)(ph.a2 / 2.0);
+  c.a4q = (float)(ph.a4 / 4.0);
+  c.a6s = (float)(ph.a6 / 6.0);
+  c.g = (float)ph.g;
+  c.th = (float)ph.th;
+  c.Ah = (float)(ph.A / 2.0);
+  c.p2 = (float)(2376.0 / 2372.0 / 2.0);
+  c.p3 = (float)((7128.0 + 12.0 * 2372.0) / 2372.0 / 3.0);
+  c.p4 = (float)((4752.0 + 12.0 * 2372.0) / 2372.0 / 4.0);
+  const double kd = ph.cshift - ph.c0;
+  c.kdp = Pair{(float)kd, (float)(kd - (double)(float)kd)};
+  c.kcp = Pair{(float)ph.cshift, (float)(ph.cshift - (double)(float)ph.cshift)};
+  return c;
+}
+
 template <int NAC, int NCH>
-__global__ void __launch_bounds__(256, 2) energy_partial_f32(Phys ph, const float *__restrict__ u,
+__global__ void __launch_bounds__(256, 2) energy_partial_f32(Phys ph, EConst ec, const float *__restrict__ u,
                                                              const double *__restrict__ elam, int form,
                                                              double *__restrict__ part) {
   constexpr int F = NAC + NCH;
@@ -327,16 +357,10 @@ __global__ void __launch_bounds__(256, 2) energy_partial_f32(Phys ph, const floa
     q6[m][c] = (float)(0.5 * ph.epn2 * v);
   }
   __syncthreads();
-  const float i4hx = (float)(0.25 / ph.h[0]), i4hy = (float)(0.25 / ph.h[1]), i4hz = (float)(0.25 / ph.h[2]);
-  const float half_epn2 = (float)(0.5 * ph.epn2);
-  const float a2h = (float)(ph.a2 / 2.0), a4q = (float)(ph.a4 / 4.0), a6s = (float)(ph.a6 / 6.0), g = (float)ph.g;
-  const float th = (float)ph.th, Ah = (float)(ph.A / 2.0);
-  const float p2 = (float)(2376.0 / 2372.0 / 2.0), p3 = (float)((7128.0 + 12.0 * 2372.0) / 2372.0 / 3.0),
-              p4 = (float)((4752.0 + 12.0 * 2372.0) / 2372.0 / 4.0);
-  // cshift - c0 and cshift as float pairs
-  const double kd = ph.cshift - ph.c0;
-  const Pair kdp = {(float)kd, (float)(kd - (double)(float)kd)};
-  const Pair kcp = {(float)ph.cshift, (float)(ph.cshift - (double)(float)ph.cshift)};
+  const float i4hx = ec.i4hx, i4hy = ec.i4hy, i4hz = ec.i4hz, half_epn2 = ec.half_epn2;
+  const float a2h = ec.a2h, a4q = ec.a4q, a6s = ec.a6s, g = ec.g, th = ec.th, Ah = ec.Ah;
+  const float p2 = ec.p2, p3 = ec.p3, p4 = ec.p4;
+  const Pair kdp = ec.kdp, kcp = ec.kcp;
   float mx[F], mn[F];
   Acc<float> vsum[F], eac_p, ech_p;
   int cnt = 0;
@@ -542,7 +566,7 @@ int check_soln_partials(int n) {
 template <int NAC, int NCH>
 static void launch_f32(const Phys &ph, const float *u, const double *elam, int form, double *partials, int npart,
                        cudaStream_t s) {
-  energy_partial_f32<NAC, NCH><<<npart, dim3(32, 8), 0, s>>>(ph, u, elam, form, partials);
+  energy_partial_f32<NAC, NCH><<<npart, dim3(32, 8), 0, s>>>(ph, econst(ph), u, elam, form, partials);
 }
 
 template <typename T>
