@@ -27,7 +27,9 @@ struct P {
   T ih2x, ih2y, ih2z;   // 1 / h^2 per axis
   T i2hx, i2hy, i2hz;   // 1 / (2 h) per axis
   T a2, a4, a6, g, th, c0, A;
-  T lam[4][9];
+  // anisotropic term folded: kan[m][3 r + c] = epn2 LE (1/2h_r) lam_m[r][c] (1/2h_c),
+  // the flux row r differenced along axis r
+  T kan[4][9];
 };
 
 template <typename T>
@@ -40,8 +42,11 @@ static P<T> to_p(const Phys &ph) {
   p.i2hx = (T)(0.5 / ph.h[0]); p.i2hy = (T)(0.5 / ph.h[1]); p.i2hz = (T)(0.5 / ph.h[2]);
   p.LE = (T)ph.LE; p.KE = (T)ph.KE; p.LCI = (T)ph.LCI; p.KCI = (T)ph.KCI; p.es = (T)ph.elastic_scale;
   p.a2 = (T)ph.a2; p.a4 = (T)ph.a4; p.a6 = (T)ph.a6; p.g = (T)ph.g; p.th = (T)ph.th; p.c0 = (T)(ph.c0 - ph.cshift); p.A = (T)ph.A;
+  const double i2h[3] = {0.5 / ph.h[0], 0.5 / ph.h[1], 0.5 / ph.h[2]};
   for (int m = 0; m < 4; m++)
-    for (int k = 0; k < 9; k++) p.lam[m][k] = (T)ph.lam[m][k];
+    for (int k = 0; k < 9; k++) {
+      p.kan[m][k] = (T)(ph.epn2 * ph.LE * i2h[k / 3] * ph.lam[m][k] * i2h[k % 3]);
+    }
   return p;
 }
 
@@ -94,19 +99,22 @@ __global__ void __launch_bounds__(RX * RY) rhs_ac_kernel(P<T> p, const T *__rest
   // this thread's share of one haloed plane of every order parameter:
   // PLANE / 256 rounded up values per field
   constexpr int PER = (PLANE + RX * RY - 1) / (RX * RY);
+  // this thread's cells of a haloed plane: in-plane offset, or -1 outside the block
+  int poff[PER];
+#pragma unroll
+  for (int q = 0; q < PER; q++) {
+    const int i = tid + q * RX * RY;
+    const int ly = i / HX, lx = i - ly * HX;
+    const int gx = x0 + lx - 2, gy = y0 + ly - 2;
+    poff[q] = i < PLANE && gx >= 0 && gx < n && gy >= 0 && gy < n ? gy * n + gx : -1;
+  }
   auto fetch = [&](int z, T *reg) {
+    const bool zin = z >= 0 && z < n;
 #pragma unroll
     for (int m = 0; m < NAC; m++) {
-      const T *um = u + m * n3;
+      const T *um = u + m * n3 + (size_t)z * n * n;
 #pragma unroll
-      for (int q = 0; q < PER; q++) {
-        const int i = tid + q * RX * RY;
-        const int ly = i / HX, lx = i - ly * HX;
-        const int gx = x0 + lx - 2, gy = y0 + ly - 2;
-        T v = (T)0;
-        if (i < PLANE && z >= 0 && z < n && gx >= 0 && gx < n && gy >= 0 && gy < n) v = um[((size_t)z * n + gy) * n + gx];
-        reg[m * PER + q] = v;
-      }
+      for (int q = 0; q < PER; q++) reg[m * PER + q] = zin && poff[q] >= 0 ? um[poff[q]] : (T)0;
     }
   };
   auto store = [&](int z, const T *reg) {
@@ -135,8 +143,9 @@ __global__ void __launch_bounds__(RX * RY) rhs_ac_kernel(P<T> p, const T *__rest
       const size_t l = ((size_t)z * n + y) * n + x;
       // ring slots of planes z-2 .. z+2, with this thread's (ly, lx) applied
       int so[5];
+      const int s0 = (z - 2 + 5 * 1024) % 5;
 #pragma unroll
-      for (int d = 0; d < 5; d++) so[d] = ((z + d - 2 + 5 * 1024) % 5) * PLANE + ly * HX + lx;
+      for (int d = 0; d < 5; d++) so[d] = (s0 + d < 5 ? s0 + d : s0 + d - 5) * PLANE + ly * HX + lx;
       T e[NAC];
 #pragma unroll
       for (int m = 0; m < NAC; m++) e[m] = ring[(size_t)m * 5 * PLANE + so[2]];
@@ -164,37 +173,21 @@ __global__ void __launch_bounds__(RX * RY) rhs_ac_kernel(P<T> p, const T *__rest
           // zero when q is outside the block; y and z differences are
           // (previous - next), as the reference writes them
           auto U = [&](int dz, int dy, int dx) { return rg[so[dz + 2] + dy * HX + dx]; };
-          const T *lam = p.lam[m];
           const T c0 = U(0, 0, 0);
           const T xp2 = U(0, 0, 2), xm2 = U(0, 0, -2), yp2 = U(0, 2, 0), ym2 = U(0, -2, 0), zp2 = U(2, 0, 0),
                   zm2 = U(-2, 0, 0);
           const T xpym = U(0, -1, 1), xpyp = U(0, 1, 1), xmym = U(0, -1, -1), xmyp = U(0, 1, -1);
           const T xpzm = U(-1, 0, 1), xpzp = U(1, 0, 1), xmzm = U(-1, 0, -1), xmzp = U(1, 0, -1);
           const T ymzm = U(-1, -1, 0), ymzp = U(1, -1, 0), ypzm = U(-1, 1, 0), ypzp = U(1, 1, 0);
-          const T *l0 = lam, *l1 = lam + 3, *l2 = lam + 6;
-          const T ar = x < n - 1 ? l0[0] * ((xp2 - c0) * p.i2hx) + l0[1] * ((xpym - xpyp) * p.i2hy) +
-                                       l0[2] * ((xpzm - xpzp) * p.i2hz)
-                                 : (T)0;
-          const T al = x > 0 ? l0[0] * ((c0 - xm2) * p.i2hx) + l0[1] * ((xmym - xmyp) * p.i2hy) +
-                                   l0[2] * ((xmzm - xmzp) * p.i2hz)
-                             : (T)0;
-          const T at = y > 0 ? l1[0] * ((xpym - xmym) * p.i2hx) + l1[1] * ((ym2 - c0) * p.i2hy) +
-                                   l1[2] * ((ymzm - ymzp) * p.i2hz)
-                             : (T)0;
-          const T ab = y < n - 1 ? l1[0] * ((xpyp - xmyp) * p.i2hx) + l1[1] * ((c0 - yp2) * p.i2hy) +
-                                       l1[2] * ((ypzm - ypzp) * p.i2hz)
-                                 : (T)0;
-          const T af = z > 0 ? l2[0] * ((xpzm - xmzm) * p.i2hx) + l2[1] * ((ymzm - ypzm) * p.i2hy) +
-                                   l2[2] * ((zm2 - c0) * p.i2hz)
-                             : (T)0;
-          const T ak = z < n - 1 ? l2[0] * ((xpzp - xmzp) * p.i2hx) + l2[1] * ((ymzp - ypzp) * p.i2hy) +
-                                       l2[2] * ((c0 - zp2) * p.i2hz)
-                                 : (T)0;
-          T t = (T)0;
-          t += (ar - al) * p.i2hx;
-          t += (at - ab) * p.i2hy;
-          t += (af - ak) * p.i2hz;
-          v -= p.epn2 * p.LE * t;
+          // folded constants: k[3 r + c] = epn2 LE lam[r][c] / (2 h_r 2 h_c)
+          const T *k = p.kan[m];
+          const T ar = x < n - 1 ? k[0] * (xp2 - c0) + k[1] * (xpym - xpyp) + k[2] * (xpzm - xpzp) : (T)0;
+          const T al = x > 0 ? k[0] * (c0 - xm2) + k[1] * (xmym - xmyp) + k[2] * (xmzm - xmzp) : (T)0;
+          const T at = y > 0 ? k[3] * (xpym - xmym) + k[4] * (ym2 - c0) + k[5] * (ymzm - ymzp) : (T)0;
+          const T ab = y < n - 1 ? k[3] * (xpyp - xmyp) + k[4] * (c0 - yp2) + k[5] * (ypzm - ypzp) : (T)0;
+          const T af = z > 0 ? k[6] * (xpzm - xmzm) + k[7] * (ymzm - ypzm) + k[8] * (zm2 - c0) : (T)0;
+          const T ak = z < n - 1 ? k[6] * (xpzp - xmzp) + k[7] * (ymzp - ypzp) + k[8] * (c0 - zp2) : (T)0;
+          v -= ((ar - al) + (at - ab)) + (af - ak);
         }
         if (p.elastic == 1) v -= p.LE * p.es * felas[m * n3 + l];
         out[m * n3 + l] = v;
