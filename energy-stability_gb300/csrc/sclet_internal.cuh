@@ -125,13 +125,14 @@ cudaError_t launch_check_soln(const Phys &ph, const T *u, const double *elam, in
 int check_soln_partials(int n);
 
 // Conserved-field mass of the mixed form (see k_mass.cu).  Weight `which`
-// (0 E, 1 phi1, 2 phi2) into w (n^3, FP64) using tmp (n^3); g (n) and viT
+// (0 E, 1 phi1, 2 phi2) into w (n^3 slots of 8 bytes: computed in FP64, then
+// stored as FP32 (hi, lo) pairs) using tmp (n^3 doubles); g (n) and viT
 // (n x n row-major) on the device.
 cudaError_t mass_weight(double *w, double *tmp, const double *g, const double *viT, int n, int which,
                         const EtdCoef &ec, cudaStream_t s);
 int mass_partials();
 // part (2 * mass_partials()) = partial sums of wa.a (owned sum of a if wa is
-// null) + wb.(b - bsub)
+// null) + wb.(b - bsub); wa, wb hold the weight pairs of mass_weight
 cudaError_t mass_target(const float *a, const double *wa, const float *b, const float *bsub, const double *wb, int n,
                         double *part, cudaStream_t s);
 // shifts the owned cells of u so that their sum meets the target partials
