@@ -185,3 +185,20 @@ def test_fp32_input_products_match_slice_planes(big_n, etd2, sclet_lib, monkeypa
         out.append(s.get_fields())
         s.close()
     np.testing.assert_array_equal(out[0], out[1])
+
+
+def test_mixed_conserves_ch_mass_like_fp64(sclet_lib):
+    """The conserved field's mass (volume integral of check_soln_new) of the
+    mixed form tracks the FP64 form's through the FP64 mass correction."""
+    sg = sclet_lib
+    case = bench.workload(32, seed=17)
+    p = params_for(sg, case)
+    u0 = bench.block_fields(case)
+    vols = {}
+    for prec in (sg.FP64, sg.MIXED):
+        s = sg.Solver(p, prec)
+        s.set_fields(u0)
+        s.step(40)
+        vols[prec] = s.check_soln(1)[case.nac, 2]
+        s.close()
+    assert abs(vols[sg.MIXED] - vols[sg.FP64]) <= 1e-11 * abs(vols[sg.FP64]), vols
