@@ -421,16 +421,20 @@ __global__ void __launch_bounds__(L *(N1 > N2 ? N1 : N2))
   }
 }
 
-constexpr int L = 16;
+// lines per CTA: 16, or 8 for lines beyond 256 points (256 threads per CTA)
+template <int N1, int N2>
+constexpr int lines_per_cta() {
+  return N1 * N2 > 256 ? 8 : 16;
+}
 
 template <int N1, int N2>
 constexpr size_t smem_bytes(int axis) {
-  return sizeof(float2) * L * N1 * (axis == 0 ? N2 + 1 : N2);
+  return sizeof(float2) * lines_per_cta<N1, N2>() * N1 * (axis == 0 ? N2 + 1 : N2);
 }
 
 template <int N1, int N2, int AXIS, int SIGN, int IO>
 static cudaError_t launch_one(float2 *z0, float2 *z1, const float2 *tw, const LineIO &io, cudaStream_t s) {
-  constexpr int N = N1 * N2;
+  constexpr int N = N1 * N2, L = lines_per_cta<N1, N2>();
   constexpr size_t sm = smem_bytes<N1, N2>(AXIS);
   auto k = lines_kernel<N1, N2, L, AXIS, SIGN, IO>;
   if (sm > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -457,9 +461,9 @@ static cudaError_t launch_pass(int sign, int k, float2 *z0, float2 *z1, const fl
   }
 }
 
-// N = 16 N1 with N1 in {2, 3, 4, 5, 6, 8, 10, 12, 16}; 0 if N has no fast path
+// N = 16 N1 with N1 in {2, 3, 4, 5, 6, 8, 10, 12, 16, 32}; 0 if N has no fast path
 static int pass_n1(int N) {
-  static const int ok[] = {2, 3, 4, 5, 6, 8, 10, 12, 16};
+  static const int ok[] = {2, 3, 4, 5, 6, 8, 10, 12, 16, 32};
   if (N % 16) return 0;
   for (int n1 : ok)
     if (n1 * 16 == N) return n1;
@@ -478,7 +482,8 @@ static cudaError_t launch(int N, int sign, int k, float2 *z0, float2 *z1, const 
     case 8: return launch_pass<8, 16>(sign, k, z0, z1, tw, io, s);
     case 10: return launch_pass<10, 16>(sign, k, z0, z1, tw, io, s);
     case 12: return launch_pass<12, 16>(sign, k, z0, z1, tw, io, s);
-    default: return launch_pass<16, 16>(sign, k, z0, z1, tw, io, s);
+    case 16: return launch_pass<16, 16>(sign, k, z0, z1, tw, io, s);
+    default: return launch_pass<32, 16>(sign, k, z0, z1, tw, io, s);
   }
 }
 

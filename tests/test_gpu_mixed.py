@@ -96,11 +96,12 @@ def test_step_diagnostics_match_check_soln(precision_name, sclet_lib):
     s.close()
 
 
-@pytest.mark.parametrize("big_n", [24, 32, 48, 80, 96, 160])
+@pytest.mark.parametrize("big_n", [24, 32, 48, 80, 96, 160, 512])
 def test_fp32_elastic_force_matches_fp64(big_n, sclet_lib):
     """FP32 elastic force (pack, three line-FFT passes each way, contraction)
     against the FP64 form on the same state.  N = 16 N1 takes the two-pass
-    register transforms; 24 the generic Stockham stages."""
+    register transforms (N1 = 32 at 512, eight lines per CTA); 24 the generic
+    Stockham stages."""
     sg = sclet_lib
     case = bench.workload(big_n, seed=13)
     p = params_for(sg, case)
@@ -189,7 +190,10 @@ def test_fp32_input_products_match_slice_planes(big_n, etd2, sclet_lib, monkeypa
 
 def test_mixed_conserves_ch_mass_like_fp64(sclet_lib):
     """The conserved field's mass (volume integral of check_soln_new) of the
-    mixed form tracks the FP64 form's through the FP64 mass correction."""
+    mixed form tracks the FP64 form's through the FP64 mass correction.  What
+    remains is the FP32 rounding of the stored state (c - c0 of about 0.02:
+    ulp 2e-9 per cell, a random sum over 32^3 cells of about 2e-11 of the
+    mass), so the bar is 1e-10."""
     sg = sclet_lib
     case = bench.workload(32, seed=17)
     p = params_for(sg, case)
@@ -201,4 +205,4 @@ def test_mixed_conserves_ch_mass_like_fp64(sclet_lib):
         s.step(40)
         vols[prec] = s.check_soln(1)[case.nac, 2]
         s.close()
-    assert abs(vols[sg.MIXED] - vols[sg.FP64]) <= 1e-11 * abs(vols[sg.FP64]), vols
+    assert abs(vols[sg.MIXED] - vols[sg.FP64]) <= 1e-10 * abs(vols[sg.FP64]), vols
