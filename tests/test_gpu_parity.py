@@ -105,8 +105,9 @@ def test_all_options_match_oracle(tmp_path, sclet_lib, oracle_lib):
 
 
 def test_beta_omega_64_cubed_1000_steps(tmp_path, sclet_lib, oracle_lib):
-    """configs[0]: 64^3, 4 order parameters, Landau 2-4-6, cubic elasticity,
-    dt = 0.01, 1000 steps: per-field relative L2 <= 1e-10 against the oracle."""
+    """The beta->omega plain-ETD workload: 64^3, 4 order parameters, Landau
+    2-4-6, cubic elasticity, dt = 0.01, 1000 steps: per-field relative L2
+    <= 1e-10 against the oracle."""
     case = cases.Case(big_n=64, steps=1000, seed=2024, suffix="omega64")
     errs, eg, eo = _oracle_vs_gpu(tmp_path, sclet_lib, oracle_lib, case, 1000)
     assert max(errs) <= 1e-10, errs
