@@ -1,7 +1,7 @@
 """ctypes front end of the C oracle (oracle/liboracle_sclet.so).
 
 TEST INFRASTRUCTURE: used by tests/, __graft_entry__.smoke() and the bench's
-CPU-baseline leg as the checker; never by the product path.
+CPU-baseline leg as the oracle; never by the product path.
 
 ``load_case(dir, suffix)`` parses a run directory in the reference's formats
 (see oracle/cases.py) with numpy, independently of the product's C parser, and

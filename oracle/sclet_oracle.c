@@ -1,7 +1,7 @@
 /*
  * CPU restatement of the reference's ScLETD ETD step on one periodic rank.
- * TEST INFRASTRUCTURE ONLY (the checker for tests, smoke() and the CPU
- * baseline); see sclet_oracle.h.  Citations are relative to the reference's
+ * TEST INFRASTRUCTURE ONLY (the reference results for tests, smoke() and the
+ * CPU baseline); see sclet_oracle.h.  Citations are relative to the reference's
  * source_beta_to_omega/src/.
  */
 #include "sclet_oracle.h"

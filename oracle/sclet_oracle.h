@@ -1,7 +1,7 @@
 /*
  * CPU restatement of the reference's ScLETD ETD step (single periodic rank),
  * TEST INFRASTRUCTURE ONLY: tests, __graft_entry__.smoke() and the bench's
- * CPU baseline use it as the checker; the product never links it.
+ * CPU baseline use it as the oracle; the product never links it.
  *
  * Every routine cites the reference function it restates
  * (paths relative to the reference project, source_beta_to_omega/src/...).
