@@ -4,8 +4,8 @@
                     [--impl reference] [--size N3EDGE] [--accuracy-steps S]
 
 Workload: the beta->alpha coupled case -- one conserved concentration
-c = 0.5 + U(-0.02, 0.02) and four order parameters U(-0.01, 0.01) on a 192^3
-periodic grid (block edge 196), Landau 2-4-6 with cross term 1.5 and c-eta
+c = 0.5 + U(-0.02, 0.02) and four order parameters U(-0.01, 0.01) on a 512^3
+periodic grid (block edge 516; --size 192 gives the 192^3 case), Landau 2-4-6 with cross term 1.5 and c-eta
 coupling 0.8, anisotropic gradient tensors diag(0.5, 0.5, 0.3) with
 stabiliser kk = 0.5, cubic elasticity C11/C12/C44 = 1.0/0.6/0.4 with four
 <111> eigenstrains, dt = 0.005, first-order ETD.  Synthetic seeded data.
@@ -22,7 +22,9 @@ from the same state.
 
 --impl reference times the reference's CPU path (the C restatement of
 oracle/, the reference's own build cannot run on this host) on all host
-cores, on the same workload.
+cores, on the same workload.  A 512^3 step takes minutes on the host, so the
+CPU sample is bounded by time: it reports the steps it actually timed and
+the per-step rate is extrapolated from them.
 
 Several GPUs (torchrun): independent replicas with their own seeds (the path
 has no data exchange between replicas); value = all ranks' cell updates /
@@ -68,6 +70,11 @@ def workload(big_n: int, seed: int) -> cases.Case:
 def workload_name(big_n: int) -> str:
     return (f"beta-alpha coupled CH + 4 AC, {big_n}^3 periodic (block {big_n + 4}^3), Landau 2-4-6, "
             f"anisotropic, cubic elasticity, ETD1, dt 0.005")
+
+
+def config_of(big_n: int, world: int) -> dict:
+    return {"workload": workload_name(big_n), "cells_per_step": big_n ** 3,
+            "l2": "inputs larger than L2 (state of a step > 129 MB)", "parallelism": f"replicas x{world}"}
 
 
 def block_fields(case: cases.Case) -> np.ndarray:
@@ -182,20 +189,32 @@ def cpu_oracle_rate(case: cases.Case, steps: int, warmup: int, budget_s: float =
     return case.big_n ** 3 * done / dt, o.threads(), dt, done
 
 
+def cpu_budget(size: int) -> tuple[int, float]:
+    """Warm-up steps and time budget of a CPU sample: a 512^3 step takes a
+    few minutes on 16 host threads, so large grids time one step, no warm-up."""
+    return (0, 1.0) if size >= 384 else (1, 120.0)
+
+
+def sample_text(done: int, asked: int, warm: int, cores: int, secs: float) -> str:
+    cut = f", {done} of {asked} asked, per-step rate extrapolated from them" if done < asked else ""
+    return (f"{done} full step(s) of the workload with diagnostics{cut}, after {warm} warm-up step(s) "
+            f"(C restatement of the reference's step, OpenMP on {cores} threads, {secs:.1f} s)")
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
     case = workload(args.size, seed=1000)
-    rate, cores, secs, done = cpu_oracle_rate(case, args.steps, args.warmup)
+    warm, budget = cpu_budget(args.size)
+    warm = min(warm, args.warmup)
+    rate, cores, secs, done = cpu_oracle_rate(case, args.steps, warm, budget)
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * secs / done,
+        "steps": done, "warmup": warm, "ms_per_step": 1000.0 * secs / done,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workload_name(args.size), "cells_per_step": args.size ** 3},
+        "config": config_of(args.size, world),
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{done} full steps of the workload with diagnostics, after "
-                                   f"{min(args.warmup, 1)} warm-up step (C restatement of the reference's step, "
-                                   f"OpenMP on {cores} threads, {secs:.1f} s)"},
+                         "sample": sample_text(done, args.steps, warm, cores, secs)},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -274,6 +293,28 @@ def tc_roofline(case, stage_ms, stage_launches, steps):
                    "mma_tflops": mma_step * steps / t / 1e12, "peak_bf16_tflops": bf16,
                    "mma_frac": mma_step * steps / t / 1e12 / bf16},
     }
+
+
+def fp64_stage_roofline(case, stage_ms_per_step):
+    """HBM fraction of the plain FP64 step's stencil, FFT and diagnostics
+    stages on their algorithmic bytes per cell-update (owned cell, all
+    fields): right-hand sides 8 F (read the fields) + 8 nac (elastic force) +
+    8 F (write) B; elastic force 112 B per order parameter (forward R2C and
+    inverse C2R, three axis passes reading and writing half a complex value
+    each, plus the real field in and out); diagnostics 8 F B."""
+    hbm, _, src = peaks()
+    F, nac = case.nac + case.nch, case.nac
+    cells = case.big_n ** 3
+    per_cell = {"rhs": 16.0 * F + 8.0 * nac, "elastic": 112.0 * nac, "diagnostics": 8.0 * F}
+    out = {}
+    for k, b in per_cell.items():
+        ms = stage_ms_per_step.get(k, 0.0)
+        if ms > 0:
+            gbs = b * cells / (ms / 1000.0) / 1e9
+            out[k] = {"bytes_per_cell": b, "ms": ms, "gbs": gbs, "frac": gbs / hbm}
+    out["peak"] = hbm
+    out["peak_source"] = src
+    return out
 
 
 def accuracy_check(sg, params, u0, steps, every, local):
@@ -360,6 +401,18 @@ def run_gpu(args, world, rank, local):
     pin_out.free()
     stage_ms, stage_launches = profiled_stages(s, 2)
     s.close()
+    # the CPU baseline runs on the host cores while the GPU times the plain
+    # FP64 step (whose kernels last tens to thousands of milliseconds, so the
+    # launching thread sharing the cores costs it nothing)
+    cpu_box = {}
+    cpu_thread = None
+    if not args.no_cpu_baseline and world == 1:
+        def cpu_leg():
+            small = workload(args.size, seed=1000)
+            warm, budget = cpu_budget(args.size)
+            cpu_box["r"] = cpu_oracle_rate(small, args.cpu_steps, warm, budget)
+        cpu_thread = threading.Thread(target=cpu_leg, daemon=True)
+        cpu_thread.start()
     # the plain FP64 step beside it (same workload, same timing)
     fp64 = None
     if precision == sg.MIXED and not args.no_fp64:
@@ -372,10 +425,20 @@ def run_gpu(args, world, rank, local):
         s64.close()
         ms64 = dist_max(ms64, world)
         fp64 = {"value": cells / (ms64 / 1000.0), "ms_per_step": ms64 / args.steps,
-                "speedup_of_mixed": ms64 / ms_max, "stage_ms_per_step": st64}
+                "speedup_of_mixed": ms64 / ms_max, "stage_ms_per_step": st64,
+                "stage_hbm": fp64_stage_roofline(case, st64)}
     accuracy = None
     if precision == sg.MIXED and rank == 0:
-        accuracy = accuracy_check(sg, params, u0, args.accuracy_steps, args.accuracy_every, local)
+        acc_steps = args.accuracy_steps if args.accuracy_steps is not None else (10 if args.size >= 384 else 100)
+        accuracy = accuracy_check(sg, params, u0, acc_steps, args.accuracy_every, local)
+    cpu = None
+    if cpu_thread is not None:
+        cpu_thread.join()
+        rate, cores, secs, done = cpu_box["r"]
+        warm = cpu_budget(args.size)[0]
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": sample_text(done, args.cpu_steps, warm, cores, secs)
+               + "; run on the host while the GPU timed the FP64 step"}
     if rank != 0:
         return
     if precision == sg.MIXED:
@@ -389,21 +452,12 @@ def run_gpu(args, world, rank, local):
                     "avg_launch_ms": stage_ms["products"] / max(stage_launches["products"], 1)}
     roofline["stage_ms_per_step"] = {k: v / 2 for k, v in stage_ms.items()}
     roofline["stage_launches_per_step"] = {k: v // 2 for k, v in stage_launches.items()}
-    cpu = None
-    if not args.no_cpu_baseline and world == 1:
-        small = workload(args.size, seed=1000)
-        rate, cores, secs, done = cpu_oracle_rate(small, args.cpu_steps, 0)
-        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"{done} full steps of the same workload with diagnostics, C restatement of the "
-                         f"reference's step on {cores} host threads ({secs:.1f} s)"}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if precision == sg.FP64 else "bf16-slices/f32 (f64 eigenbasis, diagnostics, mass)",
         "data": "synthetic",
-        "config": {"workload": workload_name(args.size), "cells_per_step": args.size ** 3,
-                   "precision": args.precision, "l2": "inputs larger than L2 (state of a step > 129 MB)",
-                   "parallelism": f"replicas x{world}"},
+        "config": config_of(args.size, world), "precision": args.precision,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": bytes_step, "d2h_bytes_per_step": bytes_step},
         "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
         "fp64": fp64, "accuracy_vs_fp64": accuracy,
@@ -418,15 +472,24 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
-    ap.add_argument("--size", type=int, default=192, help="physical grid edge N")
+    ap.add_argument("--size", type=int, default=512, help="physical grid edge N")
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip timing the plain FP64 step beside the mixed one")
-    ap.add_argument("--accuracy-steps", type=int, default=100,
-                    help="steps of the mixed-vs-FP64 check from the same state (0: skip)")
+    ap.add_argument("--accuracy-steps", type=int, default=None,
+                    help="steps of the mixed-vs-FP64 check from the same state (0: skip; default 10 at 512^3, "
+                         "100 below)")
     ap.add_argument("--accuracy-every", type=int, default=0, help="checkpoint interval of that check (0: end only)")
     args = ap.parse_args()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # one process per GPU: start the replicas under torchrun
+        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+               "--master-addr=127.0.0.1", f"--master-port={29500 + os.getpid() % 1000}",
+               os.path.abspath(__file__), *sys.argv[1:]]
+        sys.exit(subprocess.call(cmd))
     world, rank, local = dist_setup()
+    if world != args.gpus:
+        raise SystemExit(f"--gpus {args.gpus} but the launcher started {world} ranks")
     if args.impl == "reference":
         run_reference(args, world, rank)
     else:

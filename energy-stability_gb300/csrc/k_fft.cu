@@ -17,6 +17,7 @@
 // transform is exactly that real part, before packing G_0 + i G_1.
 // Each 1D pass keeps tiles of lines in shared memory (Stockham autosort,
 // radices 4, 2, 3, 5); lines along y and z are loaded as runs of adjacent x.
+#include <mutex>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -437,7 +438,10 @@ static cudaError_t launch_one(float2 *z0, float2 *z1, const float2 *tw, const Li
   constexpr int N = N1 * N2, L = lines_per_cta<N1, N2>();
   constexpr size_t sm = smem_bytes<N1, N2>(AXIS);
   auto k = lines_kernel<N1, N2, L, AXIS, SIGN, IO>;
-  if (sm > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (sm > 48 * 1024) {
+    const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+  }
   const dim3 grid((unsigned)((long long)N * N / L), z1 ? 2u : 1u);
   k<<<grid, L * (N1 > N2 ? N1 : N2), sm, s>>>(z0, z1 ? z1 : z0, tw, io);
   return cudaGetLastError();
@@ -795,11 +799,22 @@ void elastic_plan_destroy(ElasticPlan *p) {
 template <typename T>
 static cudaError_t fft3d(ElasticPlan *p, typename Cx<T>::t *z0, typename Cx<T>::t *z1, int sign, cudaStream_t s) {
   const int N = p->N;
-  static bool attr_set[2] = {false, false};
-  int which = sizeof(T) == 4 ? 1 : 0;
-  if (!attr_set[which]) {
-    cudaFuncSetAttribute(fft_lines_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr_set[which] = true;
+  // the shared-memory attribute is per device
+  constexpr int MAXDEV = 64;
+  static std::mutex mu;
+  static bool attr_set[MAXDEV][2] = {};
+  const int which = sizeof(T) == 4 ? 1 : 0;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= MAXDEV) return cudaErrorInvalidDevice;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (!attr_set[dev][which]) {
+      e = cudaFuncSetAttribute(fft_lines_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+      if (e != cudaSuccess) return e;
+      attr_set[dev][which] = true;
+    }
   }
   const dim3 grid((unsigned)((long long)N * N / p->tile), z1 ? 2u : 1u);
   const typename Cx<T>::t *tw = (const typename Cx<T>::t *)p->tw;

@@ -30,17 +30,15 @@
 // out[t][a' * n*n + r] for input row r = c * n + b, i.e. contracted index
 // slowest: three products return to x-fastest order.
 //
-// Kernel: persistent clusters of CA x 4 CTAs (one CTA per SM) looping over
-// groups of output tiles D[128 a' x 128 r]: a cluster takes four consecutive
-// input tiles of CA consecutive a'-tiles (CA = 2 for an even a'-tile count,
-// else 1).  Each CTA loads a share of the matrix slice planes for the CTAs of
-// its a'-tile and a share of the input slice planes for the CTAs of its input
-// tile, by TMA multicast: the L2 reads of the matrix operand drop by 4 and of
-// the input operand by CA, and the input slices come from HBM once.
+// Kernel: persistent CTAs (one per SM) looping over output tiles D[128 a' x
+// 128 r], a'-tiles fastest so that the CTAs working on the a'-tiles of one
+// input tile run side by side and the input slices come from HBM once (the
+// second read hits L2); the matrix slices stay in L2.  Every CTA loads its
+// own operand tiles (no cluster).
 // A = matrix slices (128 a' rows x 32 k, 64-byte swizzle), B = input
 // slices (128 r rows x 32 k), both K-major, in a three-stage mbarrier pipeline
-// that runs ahead across tiles; a stage is refilled once every CTA of the
-// cluster has consumed it (MMA completion is signalled to all of them).
+// that runs ahead across tiles; a stage is refilled once the MMAs that read
+// it have completed.
 // Warp 0 issues TMA, warp 1 issues MMAs (one elected thread each) and owns the
 // tensor memory (4 classes x 128 columns).  Warps 2-5 run the epilogue (TMEM
 // lane quadrant warp % 4): the four classes of the tile are combined into
@@ -48,13 +46,15 @@
 // fused ETD update (ac_updateU_new / ch_updateU_new, calc.c:489-535) or phi2
 // scaling (prepare_U2_new, calc.c:553-567) and the FP32 stores overlap the
 // next tile's MMAs.  Every mbarrier wait is bounded: on timeout the CTA
-// records an error, drains its copies and MMAs (bounded), waits for its
-// cluster, frees TMEM and returns.
+// records an error, drains its copies and MMAs (bounded), frees TMEM and
+// returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 #include <stdint.h>
 #include <string.h>
+
+#include <mutex>
 
 #include "sclet_internal.cuh"
 #include "sclet_tc.cuh"
@@ -65,11 +65,8 @@ namespace sclet {
 
 namespace tc {
 
-template <int CA, int CR>
 __global__ void __launch_bounds__(THREADS, 1)
     modeprod_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcArgs g) {
-  constexpr int CL = CA * CR;
-  constexpr uint16_t ALL = (uint16_t)((1u << CL) - 1);
   extern __shared__ uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t full_bar[STAGES];
   __shared__ __align__(8) uint64_t empty_bar[STAGES];
@@ -84,21 +81,13 @@ __global__ void __launch_bounds__(THREADS, 1)
   const long long rows = (long long)g.n * g.n;
   const int a_tiles = (g.n + BM - 1) / BM;
   const int r_tiles = (int)((rows + BN - 1) / BN);
-  const int r_groups = (r_tiles + CR - 1) / CR;
-  const int a_groups = (a_tiles + CA - 1) / CA;
-  const int total = a_groups * r_groups * g.count;  // tile groups, one per cluster pass
+  const int total = a_tiles * r_tiles * g.count;
   const int nkb = g.kblocks;
-  const int rank = (int)cluster_rank(), cid = (int)cluster_index(), ncl = (int)cluster_count();
-  const int ra = rank % CA, rr = rank / CA;
-  // partners sharing this CTA's a'-tile (matrix planes) and input tile (input planes)
-  uint16_t mask_a = 0, mask_b = 0;
-  for (int k = 0; k < CR; k++) mask_a |= (uint16_t)(1u << (ra + CA * k));
-  for (int k = 0; k < CA; k++) mask_b |= (uint16_t)(1u << (k + CA * rr));
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; s++) {
       mbar_init(&full_bar[s], 1);
-      mbar_init(&empty_bar[s], CL);  // consumed by the MMAs of every CTA in the cluster
+      mbar_init(&empty_bar[s], 1);
     }
     for (int b = 0; b < NBUF; b++) {
       mbar_init(&tfull_bar[b], 1);
@@ -119,19 +108,14 @@ __global__ void __launch_bounds__(THREADS, 1)
   __syncthreads();
   fence_after();
   const uint32_t tmem = tmem_slot;
-  // every barrier of the cluster is initialised before any copy or arrival crosses CTAs
-  cluster_sync_all();
 
   if (warp == 0) {
     if (lane == 0) {
       // producer: five A slices and four B slices per stage, k-blocks of all
       // this CTA's tiles in one stream
-      // A stage is refilled once every CTA of the cluster has consumed it (its
-      // empty barrier counts CL arrivals): the planes this CTA sends land in
-      // its partners.
       int it = 0;
-      for (int gam = cid; gam < total; gam += ncl) {
-        const TileIdx ti = tile_of<CA, CR>(gam, ra, rr, a_groups, r_groups);
+      for (int gam = blockIdx.x; gam < total; gam += gridDim.x) {
+        const TileIdx ti = tile_of(gam, a_tiles, r_tiles);
         for (int kb = 0; kb < nkb; kb++, it++) {
           const int s = it % STAGES;
           if (it >= STAGES && !mbar_wait(&empty_bar[s], ((it / STAGES) & 1) ^ 1)) {
@@ -140,29 +124,17 @@ __global__ void __launch_bounds__(THREADS, 1)
           }
           if (*(volatile int *)&failed) break;
           uint8_t *st = base + s * STAGE_BYTES;
-          // this CTA's planes + the matrix planes every CTA sends to it
           mbar_expect_tx(&full_bar[s], STAGE_BYTES);
-          for (int p = rr; p < NPM; p += CR)
-            tma_load_3d_mc(st + p * PLANE_A, &tmA, kb * BK, ti.a_tile * BM, p, &full_bar[s], mask_a);
-          for (int p = ra; p < NP; p += CA) {
-            if (CA == 1)
-              tma_load_3d(st + NPM * PLANE_A + p * PLANE_B, &tmB, kb * BK, ti.r_tile * BN, ti.t * NP + p, &full_bar[s]);
-            else
-              tma_load_3d_mc(st + NPM * PLANE_A + p * PLANE_B, &tmB, kb * BK, ti.r_tile * BN, ti.t * NP + p,
-                             &full_bar[s], mask_b);
-          }
+          for (int p = 0; p < NPM; p++)
+            tma_load_3d(st + p * PLANE_A, &tmA, kb * BK, ti.a_tile * BM, p, &full_bar[s]);
+          for (int p = 0; p < NP; p++)
+            tma_load_3d(st + NPM * PLANE_A + p * PLANE_B, &tmB, kb * BK, ti.r_tile * BN, ti.t * NP + p, &full_bar[s]);
         }
         if (*(volatile int *)&failed) break;
       }
       if (*(volatile int *)&failed) {
         // drain: wait (bounded) for copies still in flight into this CTA
         for (int i = it - STAGES < 0 ? 0 : it - STAGES; i < it; i++) mbar_wait(&full_bar[i % STAGES], (i / STAGES) & 1);
-      }
-      // tail: the last consumption of every stage, by every CTA of the
-      // cluster, has arrived here, so no peer signals this CTA after it exits
-      for (int s = 0; s < STAGES && s < it; s++) {
-        const int last = it - 1 - ((it - 1 - s) % STAGES);
-        if (!mbar_wait(&empty_bar[s], (last / STAGES) & 1)) failed = 1;
       }
     }
   } else if (warp == 1) {
@@ -175,7 +147,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       const int pairB[11] = {0, 3, 2, 1, 0, 2, 1, 0, 1, 0, 0};
       const int cls[11] = {3, 3, 3, 3, 3, 2, 2, 2, 1, 1, 0};
       int it = 0, j = 0;
-      for (int gam = cid; gam < total && !*(volatile int *)&failed; gam += ncl, j++) {
+      for (int gam = blockIdx.x; gam < total && !*(volatile int *)&failed; gam += gridDim.x, j++) {
         const int b = j % NBUF;
         // accumulator set b was last used by tile j - NBUF
         if (j >= NBUF && !mbar_wait(&tempty_bar[b], ((j / NBUF) & 1) ^ 1)) {
@@ -207,7 +179,7 @@ __global__ void __launch_bounds__(THREADS, 1)
               mma_bf16(acc + (uint32_t)(w * BN), da, db, idesc, start ? 0u : 1u);
             }
           }
-          mma_commit_mc(&empty_bar[s], ALL);
+          mma_commit(&empty_bar[s]);
         }
         if (!ok) {
           failed = 1;
@@ -232,7 +204,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                             ldexpf(1.0f, -5 * g.bits)};
     const bool vec = (rows & 3) == 0;
     int j = 0;
-    for (int gam = cid; gam < total; gam += ncl, j++) {
+    for (int gam = blockIdx.x; gam < total; gam += gridDim.x, j++) {
       const int b = j % NBUF;
       // one lane waits, the warp follows its verdict (tcgen05.ld below needs
       // the whole warp converged)
@@ -262,7 +234,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&tempty_bar[b]);
-      const TileIdx ti = tile_of<CA, CR>(gam, ra, rr, a_groups, r_groups);
+      const TileIdx ti = tile_of(gam, a_tiles, r_tiles);
       const int a = ti.a_tile * BM + row;
       const int kind = (ti.t % g.F) >= g.nac ? 1 : 0;
       const long long tb = (long long)ti.t * g.n * rows;
@@ -337,8 +309,6 @@ __global__ void __launch_bounds__(THREADS, 1)
   }
   __syncthreads();
   if (threadIdx.x == 0 && failed) atomicExch(g.err, 1);
-  // no CTA leaves while a peer may still send to it
-  cluster_sync_all();
   if (warp == 1) {
     fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
@@ -553,64 +523,56 @@ cudaError_t tc_make_coefs(float4 *coef, float2 *coef2, int n, int kind, const do
   return cudaGetLastError();
 }
 
+// Per-device launch set-up: the dynamic shared-memory attributes (set per
+// device) and the number of CTAs that can be resident at once.
+static int tc_setup(int *ctas) {
+  constexpr int MAXDEV = 64;
+  static std::mutex mu;
+  static int resident[MAXDEV] = {0};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= MAXDEV) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!resident[dev]) {
+    // all of the unified L1/shared capacity as shared memory
+    e = cudaFuncSetAttribute(tc::modeprod_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(tc::modeprod_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0, sms = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc::modeprod_tc_kernel, tc::THREADS, tc::SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    resident[dev] = per_sm * sms;
+  }
+  *ctas = resident[dev];
+  return cudaSuccess;
+}
+
 cudaError_t launch_modeprod_tc(const __nv_bfloat16 *mat, const __nv_bfloat16 *planes, int count, const TcArgs &args,
                                cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
-    // all of the unified L1/shared capacity as shared memory
-    for (int ca = 1; ca <= 2; ca++) {
-      const void *fn = ca == 2 ? (const void *)tc::modeprod_tc_kernel<2, 2> : (const void *)tc::modeprod_tc_kernel<1, 4>;
-      cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
-      if (e != cudaSuccess) return e;
-      e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-      if (e != cudaSuccess) return e;
-    }
-    attr = true;
-  }
+  int ctas = 0;
+  cudaError_t e = (cudaError_t)tc_setup(&ctas);
+  if (e != cudaSuccess) return e;
   const int n = args.n, kp = tc_kp(n);
   const int bits = tc_slice_bits(n);
   if ((long long)tc::BK * ((n + tc::BK - 1) / tc::BK) > (1LL << (24 - 2 * bits))) return cudaErrorInvalidValue;
   CUtensorMap ma, mb;
-  cudaError_t e;
   if ((e = make_map(&ma, mat, kp, n, TC_PLANES_M, tc::BM)) != cudaSuccess) return e;
   if ((e = make_map(&mb, planes, kp, (long long)n * n, TC_PLANES * count, tc::BN)) != cudaSuccess) return e;
   TcArgs g = args;
   g.kp = kp;
   g.kblocks = (n + tc::BK - 1) / tc::BK;
   g.bits = bits;
-  const int a_tiles = (n + tc::BM - 1) / tc::BM;
-  const int CA = a_tiles % 2 == 0 ? 2 : 1;
-  const int CR = CA == 2 ? 2 : 4;
-  const int CL = CA * CR;
-  const long long r_groups = (((long long)n * n + tc::BN - 1) / tc::BN + CR - 1) / CR;
-  const long long groups = (long long)((a_tiles + CA - 1) / CA) * r_groups * count;
-  if (groups > 0x7fffffffLL) return cudaErrorInvalidValue;
-  cudaLaunchConfig_t cfg = {};
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeClusterDimension;
-  at[0].val.clusterDim.x = CL;
-  at[0].val.clusterDim.y = 1;
-  at[0].val.clusterDim.z = 1;
-  cfg.blockDim = dim3(tc::THREADS);
-  cfg.dynamicSmemBytes = tc::SMEM_BYTES;
-  cfg.stream = s;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  // persistent: as many clusters as can be resident at once
-  static int max_clusters[3] = {0, 0, 0};
-  if (!max_clusters[CA]) {
-    cfg.gridDim = dim3(CL * 128);
-    e = CA == 2 ? cudaOccupancyMaxActiveClusters(&max_clusters[CA], tc::modeprod_tc_kernel<2, 2>, &cfg)
-                : cudaOccupancyMaxActiveClusters(&max_clusters[CA], tc::modeprod_tc_kernel<1, 4>, &cfg);
-    if (e != cudaSuccess) return e;
-    if (max_clusters[CA] < 1) return cudaErrorInvalidConfiguration;
-  }
-  const int clusters = (int)(groups < max_clusters[CA] ? groups : max_clusters[CA]);
-  cfg.gridDim = dim3(CL * clusters);
-  e = CA == 2 ? cudaLaunchKernelEx(&cfg, tc::modeprod_tc_kernel<2, 2>, ma, mb, g)
-              : cudaLaunchKernelEx(&cfg, tc::modeprod_tc_kernel<1, 4>, ma, mb, g);
+  const long long tiles = (long long)((n + tc::BM - 1) / tc::BM) * (((long long)n * n + tc::BN - 1) / tc::BN) * count;
+  if (tiles > 0x7fffffffLL) return cudaErrorInvalidValue;
+  // persistent: as many CTAs as can be resident at once
+  const int grid = (int)(tiles < ctas ? tiles : ctas);
+  tc::modeprod_tc_kernel<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(ma, mb, g);
   launch_counter()++;
-  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 

@@ -61,10 +61,6 @@ struct sclet_ctx {
   float *fstate2 = nullptr, *frhs2 = nullptr, *ffelas = nullptr, *fscratch = nullptr, *fshell = nullptr;
   float *W1 = nullptr, *W2 = nullptr, *scaleP = nullptr, *rsV = nullptr, *rsVi = nullptr;
   __nv_bfloat16 *P = nullptr, *matV = nullptr, *matVi = nullptr;
-  // FP32-input products (tcf): the slices are cut inside the product kernel;
-  // lmax holds two ping-pong sets of line maxima (2F blocks of n*n rows)
-  bool tcf = false;
-  unsigned *lmax[2] = {nullptr, nullptr};
   float4 *coef[2] = {nullptr, nullptr};   // ETD1 coefficient pairs per field kind
   float2 *coef2[2] = {nullptr, nullptr};  // ETD2 phi2 pairs per field kind
   double *stage64 = nullptr;  // n^3 FP64 staging block for host transfers
@@ -409,7 +405,7 @@ void sclet_destroy(sclet_ctx *ctx) {
                   ctx->fstate2, ctx->frhs2, ctx->ffelas, ctx->fscratch, ctx->fshell, ctx->W1, ctx->W2, ctx->P,
                   ctx->scaleP, ctx->rsV, ctx->rsVi, ctx->matV, ctx->matVi, ctx->stage64,
                   ctx->coef[0], ctx->coef[1], ctx->coef2[0], ctx->coef2[1], ctx->massW, ctx->massPart,
-                  ctx->massRes, ctx->in_stage, ctx->out_stage, ctx->lmax[0], ctx->lmax[1]};
+                  ctx->massRes, ctx->in_stage, ctx->out_stage};
   for (void *b : bufs) cudaFree(b);
   if (ctx->diag_host) cudaFreeHost(ctx->diag_host);
   for (int a = 0; a < 3; a++) {
@@ -558,13 +554,7 @@ int sclet_create(const sclet_params *p, int precision, int device, sclet_ctx **o
     CC(cudaMalloc(&ctx->fshell, sizeof(float) * F * shell_count(n)));
     CC(cudaMalloc(&ctx->W1, 2 * F * blk));
     CC(cudaMalloc(&ctx->W2, 2 * F * blk));
-    // Slice planes in global memory by default; SCLET_TC_FP32_INPUT selects
-    // the products that cut the slices in shared memory from FP32 rows (same
-    // results bit for bit, slower at present), where the rows are 16-byte aligned.
-    ctx->tcf = tc_fp32_input_ok(n) && getenv("SCLET_TC_FP32_INPUT") != nullptr;
-    if (ctx->tcf) {
-      for (int k = 0; k < 2; k++) CC(cudaMalloc(&ctx->lmax[k], sizeof(unsigned) * 2 * F * n * n));
-    } else {
+    {
       const size_t pbytes = sizeof(__nv_bfloat16) * plane_stride(ctx) * 2 * F;
       // pad columns of the slice planes are never written and must stay zero
       CC(cudaMalloc(&ctx->P, pbytes));
@@ -833,34 +823,6 @@ static cudaError_t tc_prod(sclet_ctx *ctx, bool inverse, const __nv_bfloat16 *pl
   return e;
 }
 
-// The same product from FP32 blocks `in` with line maxima `lin`; the line
-// maxima of out's rows (along the next contraction) go to lout when given.
-static cudaError_t tc_prodf(sclet_ctx *ctx, bool inverse, const float *in, const unsigned *lin, int count, float *out,
-                            int epi, const float *aux, int outmode, unsigned *lout) {
-  StageEv ev;
-  long long l0 = launch_counter();
-  stage_begin(ctx, 5, ev);
-  cudaError_t e = cudaSuccess;
-  if (lout) e = cudaMemsetAsync(lout, 0, sizeof(unsigned) * count * ctx->n * ctx->n, ctx->stream);
-  TcArgs g = tc_args(ctx, inverse, count, out, epi, aux, outmode);
-  g.lmax_in = lin;
-  g.lmax_out = lout;
-  if (e == cudaSuccess) e = launch_modeprod_tcf(inverse ? ctx->matV : ctx->matVi, in, count, g, ctx->stream);
-  stage_end(ctx, ev, l0);
-  return e;
-}
-
-// line maxima of count FP32 blocks (x - sub, stored to diff, when sub is given)
-static cudaError_t tc_scales(sclet_ctx *ctx, const float *x, const float *sub, float *diff, unsigned *lmax,
-                             int count) {
-  StageEv ev;
-  long long l0 = launch_counter();
-  stage_begin(ctx, 6, ev);
-  cudaError_t e = tc_line_max(x, sub, diff, lmax, ctx->n, count, ctx->stream);
-  stage_end(ctx, ev, l0);
-  return e;
-}
-
 // x (count FP32 blocks, minus sub) -> slice planes P and row scales
 static cudaError_t tc_slice(sclet_ctx *ctx, const float *x, const float *sub, int count) {
   StageEv ev;
@@ -880,22 +842,6 @@ static int etd_update_mixed(sclet_ctx *ctx) {
   if (ctx->nch > 0)  // target mass of the conserved field from (u, N1)
     CK(mass_target(fu_of(ctx) + ctx->nac * n3, ctx->massW, frhs1_of(ctx) + ctx->nac * n3, nullptr, ctx->massW + n3,
                    ctx->n, ctx->massPart, ctx->stream));
-  if (ctx->tcf) {
-    unsigned *L0 = ctx->lmax[0], *L1 = ctx->lmax[1];
-    float *W1 = ctx->W1, *W2 = ctx->W2;
-    CK(tc_scales(ctx, ctx->fstate2, nullptr, nullptr, L0, 2 * F));
-    CK(tc_prodf(ctx, false, ctx->fstate2, L0, 2 * F, W1, 0, nullptr, 1, L1));
-    CK(tc_prodf(ctx, false, W1, L1, 2 * F, W2, 0, nullptr, 1, L0));
-    CK(tc_prodf(ctx, false, W2, L0, F, W1, 0, nullptr, 1, nullptr));
-    CK(tc_prodf(ctx, false, W2 + F * n3, L0 + F * rows, F, W1, 1, W1, 1, L1));
-    CK(tc_prodf(ctx, true, W1, L1, F, W2, 0, nullptr, 1, L0));
-    CK(tc_prodf(ctx, true, W2, L0, F, W1, 0, nullptr, 1, L1));
-    CK(tc_prodf(ctx, true, W1, L1, F, fu_of(ctx), 0, nullptr, 1, nullptr));
-    if (ctx->nch > 0)
-      CK(mass_fix(fu_of(ctx) + ctx->nac * n3, ctx->n, ctx->massPart, ctx->massPart + 2 * mass_partials(),
-                  ctx->massRes, ctx->stream));
-    return SCLET_OK;
-  }
   CK(tc_slice(ctx, ctx->fstate2, nullptr, 2 * F));
   CK(tc_prod(ctx, false, ctx->P, ctx->scaleP, 2 * F, ctx->W1, 0, nullptr, 1));
   CK(tc_slice(ctx, ctx->W1, nullptr, 2 * F));
@@ -922,21 +868,6 @@ static int etd2_correct_mixed(sclet_ctx *ctx) {
   if (ctx->nch > 0)  // target: current mass plus <w2, N2 - N1>
     CK(mass_target(fu_of(ctx) + off, nullptr, ctx->frhs2 + off, frhs1_of(ctx) + off, ctx->massW + 2 * n3, ctx->n,
                    ctx->massPart, ctx->stream));
-  if (ctx->tcf) {
-    unsigned *L0 = ctx->lmax[0], *L1 = ctx->lmax[1];
-    float *W1 = ctx->W1, *W2 = ctx->W2;
-    CK(tc_scales(ctx, ctx->frhs2, frhs1_of(ctx), W2, L0, F));  // W2 = N2 - N1
-    CK(tc_prodf(ctx, false, W2, L0, F, W1, 0, nullptr, 1, L1));
-    CK(tc_prodf(ctx, false, W1, L1, F, W2, 0, nullptr, 1, L0));
-    CK(tc_prodf(ctx, false, W2, L0, F, W1, 2, nullptr, 1, L1));
-    CK(tc_prodf(ctx, true, W1, L1, F, W2, 0, nullptr, 1, L0));
-    CK(tc_prodf(ctx, true, W2, L0, F, W1, 0, nullptr, 1, L1));
-    CK(tc_prodf(ctx, true, W1, L1, F, fu_of(ctx), 0, nullptr, 2, nullptr));
-    if (ctx->nch > 0)
-      CK(mass_fix(fu_of(ctx) + off, ctx->n, ctx->massPart, ctx->massPart + 2 * mass_partials(), ctx->massRes,
-                  ctx->stream));
-    return SCLET_OK;
-  }
   CK(tc_slice(ctx, ctx->frhs2, frhs1_of(ctx), F));
   CK(tc_prod(ctx, false, ctx->P, ctx->scaleP, F, ctx->W1, 0, nullptr, 1));
   CK(tc_slice(ctx, ctx->W1, nullptr, F));
@@ -1089,13 +1020,8 @@ int sclet_mode_product(sclet_ctx *ctx, int inverse, const double *in, double *ou
     f64_to_f32<<<grid_of(n3), 256, 0, ctx->stream>>>(ctx->stage64, tmp, n3, 0.0);
     launch_counter()++;
     CK(cudaGetLastError());
-    if (ctx->tcf) {
-      CK(tc_scales(ctx, tmp, nullptr, nullptr, ctx->lmax[0], 1));
-      CK(tc_prodf(ctx, inverse != 0, tmp, ctx->lmax[0], 1, tmp + n3, 0, nullptr, 1, nullptr));
-    } else {
-      CK(tc_slice(ctx, tmp, nullptr, 1));
-      CK(tc_prod(ctx, inverse != 0, ctx->P, ctx->scaleP, 1, tmp + n3, 0, nullptr, 1));
-    }
+    CK(tc_slice(ctx, tmp, nullptr, 1));
+    CK(tc_prod(ctx, inverse != 0, ctx->P, ctx->scaleP, 1, tmp + n3, 0, nullptr, 1));
     f32_to_f64<<<grid_of(n3), 256, 0, ctx->stream>>>(tmp + n3, ctx->stage64, n3, 0.0);
     launch_counter()++;
     CK(cudaGetLastError());

@@ -14,6 +14,9 @@
 // The scratch array is shared by every call on a device: calls that overlap in
 // time on one device (different streams, or host threads without ordering)
 // race on it and give wrong results; order them on one stream.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -38,6 +41,25 @@ __device__ __align__(256) double g_check_scratch[kScratchDoubles];
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 double *g_scratch_addr[kMaxDevices];  // device address of g_check_scratch, per device
+CUcontext g_scratch_ctx[kMaxDevices];  // the context that address belongs to
+
+// The current driver context, through the runtime's driver entry point (no
+// link against the driver library); null when it cannot be asked.
+CUcontext current_context() {
+  static PFN_cuCtxGetCurrent_v4000 fn = nullptr;
+  static bool looked = false;
+  if (!looked) {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuCtxGetCurrent_v4000)f;
+    looked = true;
+  }
+  CUcontext c = nullptr;
+  if (fn && fn(&c) != CUDA_SUCCESS) c = nullptr;
+  return c;
+}
 
 struct Lam36 {
   double v[36];
@@ -54,7 +76,9 @@ void set_msg(char *msg, size_t len, const char *text) {
 
 // Looks the array's address up once per device, with that device current.
 // The first call on a device therefore does this set-up (it may also load the
-// module); make that first call before capturing a stream.
+// module); make that first call before capturing a stream.  A new context on
+// the device (after cudaDeviceReset, or a context the caller made current)
+// holds its own copy of the array, so the look-up is repeated for it.
 int scratch_address(double **out, char *msg, size_t len) {
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
@@ -66,8 +90,11 @@ int scratch_address(double **out, char *msg, size_t len) {
     set_msg(msg, len, "device ordinal beyond the per-device table (64 devices)");
     return SCLET_ERR_ARG;
   }
+  // null before the runtime's first use on this thread (the look-up below
+  // makes the device's primary context current)
+  const CUcontext ctx = current_context();
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_scratch_addr[dev]) {
+  if (!g_scratch_addr[dev] || !ctx || g_scratch_ctx[dev] != ctx) {
     void *p = nullptr;
     e = cudaGetSymbolAddress(&p, g_check_scratch);
     if (e != cudaSuccess || !p) {
@@ -77,6 +104,7 @@ int scratch_address(double **out, char *msg, size_t len) {
       return SCLET_ERR_CUDA;
     }
     g_scratch_addr[dev] = static_cast<double *>(p);
+    g_scratch_ctx[dev] = current_context();
   }
   *out = g_scratch_addr[dev];
   return SCLET_OK;

@@ -26,12 +26,6 @@ struct TcArgs {
   const float2 *coef2[2];
   int nac, F;
   int *err;                 // set to 1 when a bounded wait gives up
-  // FP32-input form (launch_modeprod_tcf): line maxima |x| of the input rows
-  // ([count][n*n], float bits) and, when not null, of the output's rows along
-  // the next contraction (atomic maxima; zeroed by the caller)
-  const unsigned *lmax_in;
-  unsigned *lmax_out;
-  const float *xin;         // [count][n*n][n] FP32 input rows (set by launch_modeprod_tcf)
 };
 
 int tc_kp(int n);
@@ -50,14 +44,5 @@ cudaError_t tc_make_coefs(float4 *coef, float2 *coef2, int n, int kind, const do
 // out[t] = mat x in[t] (contracting the row axis, rotating), count tensors
 cudaError_t launch_modeprod_tc(const __nv_bfloat16 *mat, const __nv_bfloat16 *planes, int count, const TcArgs &args,
                                cudaStream_t s);
-// The same product from FP32 input rows x ([count][n*n][n]), sliced in shared
-// memory with the scales of args.lmax_in; needs n % 4 == 0 (TMA row pitch).
-bool tc_fp32_input_ok(int n);
-cudaError_t launch_modeprod_tcf(const __nv_bfloat16 *mat, const float *x, int count, const TcArgs &args,
-                                cudaStream_t s);
-// Line maxima of FP32 rows of n (x - sub when sub is given, then also written
-// to diff) as float bits into lmax[count][n*n].
-cudaError_t tc_line_max(const float *x, const float *sub, float *diff, unsigned *lmax, int n, int count,
-                        cudaStream_t s);
 
 }  // namespace sclet

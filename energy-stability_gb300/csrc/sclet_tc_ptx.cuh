@@ -1,7 +1,6 @@
-// Device and host helpers shared by the tensor-core mode-n product kernels
-// (k_modeprod_tc.cu: slice planes in global memory; k_modeprod_tcf.cu: FP32
-// input sliced in shared memory): tile constants, mbarrier / TMA / tcgen05
-// wrappers, the cluster tile order and the tensor-map encoder.
+// Device and host helpers of the tensor-core mode-n product kernel
+// (k_modeprod_tc.cu): tile constants, mbarrier / TMA / tcgen05 wrappers, the
+// tile order and the tensor-map encoder.
 #pragma once
 
 #include <cuda.h>
@@ -26,12 +25,6 @@ constexpr int ACC_COLS = NACC * BN;   // one accumulator set
 constexpr int NBUF = 512 / ACC_COLS;   // accumulator sets in tensor memory (1 or 2)
 constexpr int TMEM_COLS = NBUF * ACC_COLS;
 constexpr int THREADS = 192;          // producer, MMA, four epilogue warps
-// Cluster of CA x CR CTAs: CR consecutive 128-wide input tiles times CA
-// consecutive a'-tiles.  CTAs of the same a'-tile share the matrix slices and
-// CTAs of the same input tile share the input slices: each CTA loads a share
-// of the planes for its partners (TMA multicast), dividing the L2 reads of
-// the matrix operand by CR and of the input operand by CA.  CA = 2 when the
-// a'-tile count is even (with CR = 2), else 1 (with CR = 4): four CTAs.
 constexpr long long WAIT_LIMIT = 1LL << 22;  // polls (with backoff) before giving up
 static_assert(TMEM_COLS <= 512, "tensor memory holds 512 columns");
 static_assert(SMEM_BYTES <= 227 * 1024, "shared memory per CTA");
@@ -116,43 +109,6 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
   for (int j = 0; j < 32; j++) v[j] = __uint_as_float(r[j]);
 }
 
-__device__ __forceinline__ uint32_t cluster_rank() {
-  uint32_t r;
-  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-  return r;
-}
-__device__ __forceinline__ uint32_t cluster_index() {
-  uint32_t r;
-  asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
-  return r;
-}
-__device__ __forceinline__ uint32_t cluster_count() {
-  uint32_t r;
-  asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(r));
-  return r;
-}
-// every thread of every CTA of the cluster
-__device__ __forceinline__ void cluster_sync_all() {
-  asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
-}
-// TMA load delivered to the same shared-memory offset of every CTA in mask,
-// each CTA's barrier at the same offset receiving the bytes
-__device__ __forceinline__ void tma_load_3d_mc(void *dst, const CUtensorMap *map, int x, int y, int z, uint64_t *bar,
-                                               uint16_t mask) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster [%0], [%1, {%2, "
-      "%3, %4}], [%5], %6;" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar)), "h"(mask)
-      : "memory");
-}
-// MMA completion signalled on the barrier at the same offset in every CTA of mask
-__device__ __forceinline__ void mma_commit_mc(uint64_t *bar, uint16_t mask) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
-                   smem_u32(bar)),
-               "h"(mask)
-               : "memory");
-}
-
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
@@ -168,17 +124,13 @@ __device__ __forceinline__ float pow2_scale(float m) {
   return ldexpf(1.0f, e);
 }
 
-// Tile of the CTA with a'-rank ra and r-rank rr in group gam: groups of CA
-// a'-tiles fastest, then groups of CR input tiles, then the tensor.  The last
-// group of a tensor may name input tiles past the end: their loads read zeros
-// and their stores are skipped.
-template <int CA, int CR>
-__device__ __forceinline__ TileIdx tile_of(int gam, int ra, int rr, int a_groups, int r_groups) {
+// Output tile gam: a'-tiles fastest, then input tiles, then the tensor.
+__device__ __forceinline__ TileIdx tile_of(int gam, int a_tiles, int r_tiles) {
   TileIdx x;
-  x.a_tile = (gam % a_groups) * CA + ra;
-  const int rest = gam / a_groups;
-  x.r_tile = (rest % r_groups) * CR + rr;
-  x.t = rest / r_groups;
+  x.a_tile = gam % a_tiles;
+  const int rest = gam / a_tiles;
+  x.r_tile = rest % r_tiles;
+  x.t = rest / r_tiles;
   return x;
 }
 

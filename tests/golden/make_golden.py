@@ -26,7 +26,11 @@ BIN = os.path.join(ROOT, "oracle", "_ref", "ScLETD_ref")
 RUNNER = os.path.join(ROOT, "oracle", "ref_runner.py")
 
 
-EIGEN_DIR = "/root/reference/source_beta_to_alpha"
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import ref_paths  # noqa: E402
+
+# the reference checkout: SCLET_REFERENCE_ROOT, else the build recipe's default
+EIGEN_DIR = os.path.join(ref_paths.reference_root(), "source_beta_to_alpha")
 
 
 def eigen260():

@@ -56,3 +56,26 @@ def test_reference_arm_two_ranks_prints_once(oracle_lib):
     line = lines[0]
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port" and line["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_gpus_flag_starts_the_ranks(oracle_lib):
+    """--gpus 2 without a launcher starts two ranks itself (torchrun on
+    127.0.0.1); rank 0 alone prints."""
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--gpus", "2", "--size", "8",
+                        "--steps", "1", "--warmup", "0"],
+                       capture_output=True, text=True, timeout=600, env=_env(), cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [json.loads(ln) for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1 and lines[0]["n_gpus"] == 2, r.stdout
+
+
+def test_cpu_sample_reports_the_steps_it_timed(oracle_lib):
+    """A time budget shorter than one step times exactly one step, and the
+    sample says the rate is extrapolated from fewer steps than asked."""
+    sys.path.insert(0, ROOT)
+    import bench
+    rate, cores, secs, done = bench.cpu_oracle_rate(bench.workload(8, seed=3), 5, 0, budget_s=0.0)
+    assert done == 1 and rate > 0 and secs > 0
+    text = bench.sample_text(done, 5, 0, cores, secs)
+    assert "1 of 5 asked" in text and "extrapolated" in text
+    assert "extrapolated" not in bench.sample_text(5, 5, 0, cores, secs)

@@ -29,12 +29,18 @@ def _noalloc(sg, params, precision, dev_fields, form, dev_out):
     return rc, msg.value.decode()
 
 
+@pytest.mark.parametrize("anisotropic", [1, 0])
 @pytest.mark.parametrize("precision_name", ["FP64", "MIXED"])
-def test_noalloc_diagnostics_match_context_path(precision_name, sclet_lib):
+def test_noalloc_diagnostics_match_context_path(precision_name, anisotropic, sclet_lib):
+    """anisotropic = 1: the energy's gradient tensors are the file tensors;
+    0: diag(kk), which the entry point builds itself."""
     torch = pytest.importorskip("torch")
     sg = sclet_lib
     precision = getattr(sg, precision_name)
-    case = bench.workload(24, seed=5)  # 4 AC + 1 CH fields, anisotropic
+    case = bench.workload(24, seed=5)  # 4 AC + 1 CH fields
+    case.anisotropic = anisotropic
+    if not anisotropic:
+        case.kk = (0.5, 0.4, 0.3)  # distinct diagonal entries
     params = _params(sg, case)
     u0 = bench.block_fields(case)
     s = sg.Solver(params, precision)
@@ -49,13 +55,22 @@ def test_noalloc_diagnostics_match_context_path(precision_name, sclet_lib):
         s.set_fields(state)
     dtype = torch.float64 if precision == sg.FP64 else torch.float32
     dev = torch.from_numpy(np.ascontiguousarray(state)).to(device="cuda:0", dtype=dtype)
+    outs = [torch.full((4 * s.F,), float("nan"), dtype=torch.float64, device="cuda:0") for _ in range(4)]
+    # a first call does the per-device set-up; later calls must leave the
+    # device's free memory as it was
+    rc, msg = _noalloc(sg, params, precision, dev, 1, outs[0])
+    assert rc == 0, msg
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info(0)[0]
     for form in (0, 1):
         want = s.check_soln(form)
         for call in range(2):
-            out = torch.full((4 * s.F,), float("nan"), dtype=torch.float64, device="cuda:0")
+            out = outs[2 * form + call]
+            out.fill_(float("nan"))
             rc, msg = _noalloc(sg, params, precision, dev, form, out)
             assert rc == 0, msg
             torch.cuda.synchronize()
+            assert torch.cuda.mem_get_info(0)[0] == free0, "free device memory changed"
             got = out.cpu().numpy().reshape(s.F, 4)
             np.testing.assert_allclose(got, want, rtol=1e-12, atol=0,
                                        err_msg=f"{precision_name} form {form} call {call}")
