@@ -5,10 +5,12 @@
 //   sum_m epn2/2 grad(eta_m).lambda_m.grad(eta_m)  [+ epn2/2 |grad c|^2]
 //   + Landau energy of the averages.
 // form 0 reproduces the reference's hard-coded 2-3-4 polynomial and its
-// separate CH energy ((c^2-1)^2/4); form 1 is the plugin's total free energy.
+// separate CH energy ((c^2-1)^2/4); form 1 is the plugin's total free energy
+// (its F_bulk, sclet_physics.cuh, plus the gradient terms).
 // Sums are compensated (TwoSum pairs) in FP64 and reduced in a fixed order,
 // so the result is deterministic.
 #include "sclet_internal.cuh"
+#include "sclet_physics.cuh"
 
 namespace sclet {
 
@@ -158,7 +160,7 @@ __device__ __forceinline__ void block_record(double (&mxd)[MAXF], double (&mnd)[
 }
 
 
-template <typename T>
+template <typename PL, typename T>
 __global__ void __launch_bounds__(EB) energy_partial_kernel(Phys ph, const T *__restrict__ u, const double *__restrict__ elam,
                                                             int form, double *__restrict__ part) {
   // Per-cell arithmetic in the state's precision T: the cell terms of an FP32
@@ -173,8 +175,9 @@ __global__ void __launch_bounds__(EB) energy_partial_kernel(Phys ph, const T *__
   T L[4][9];
   for (int m = 0; m < 4; m++)
     for (int k = 0; k < 9; k++) L[m][k] = (T)elam[9 * m + k];
-  const T a2h = (T)(ph.a2 / 2.0), a4q = (T)(ph.a4 / 4.0), a6s = (T)(ph.a6 / 6.0), g = (T)ph.g, th = (T)ph.th;
-  const T Ah = (T)(ph.A / 2.0);
+  T Kt[16];  // plugin constants
+#pragma unroll
+  for (int k = 0; k < 16; k++) Kt[k] = (T)ph.K[k];
   T mx[MAXF], mn[MAXF];
   Acc<T> vsum[MAXF], eac_p, ech_p;
   long long cnt = 0;
@@ -200,6 +203,7 @@ __global__ void __launch_bounds__(EB) energy_partial_kernel(Phys ph, const T *__
     if (i >= n - 3 || j >= n - 3 || k >= n - 3) continue;
     T avg[MAXF];
     double cbar = 0.0;  // true concentration average, exact sum of the 8 values
+    double cst = 0.0;   // the same of the stored values (c - cshift)
     T e_ac = (T)0, e_ch = (T)0;
 #pragma unroll
     for (int f = 0; f < MAXF; f++) {
@@ -229,7 +233,8 @@ __global__ void __launch_bounds__(EB) energy_partial_kernel(Phys ph, const T *__
         cs.add(v5);
         cs.add(v6);
         cs.add(v7);
-        cbar = cs.value() * 0.125 + cshift;
+        cst = cs.value() * 0.125;
+        cbar = cst + cshift;
       }
     }
     if (form == 0) {
@@ -247,22 +252,12 @@ __global__ void __launch_bounds__(EB) energy_partial_kernel(Phys ph, const T *__
         e_ch += (c * c - (T)1) * (c * c - (T)1) * (T)0.25;
       }
     } else {
-      T fl = (T)0, s2 = (T)0;
+      sclet_acv<T> ac[4];
+      sclet_chv<T> ch[1];
 #pragma unroll
-      for (int m = 0; m < 4; m++) {
-        if (m >= nac) break;
-        const T u2 = avg[m] * avg[m];
-        s2 += u2;
-        fl += a2h * u2 + a4q * u2 * u2 + a6s * u2 * u2 * u2;
-#pragma unroll
-        for (int q = m + 1; q < 4; q++)
-          if (q < nac) fl += g * u2 * avg[q] * avg[q];
-      }
-      if (ph.nch > 0) {
-        const T cd = (T)(cbar - ph.c0);
-        fl += Ah * cd * cd - th * cd * s2;
-      }
-      e_ac += fl;
+      for (int m = 0; m < 4; m++) ac[m].u = m < nac ? avg[m] : (T)0;
+      ch[0].c = (T)cst;
+      e_ac += PL::template f_bulk<T>(ac, ch, nac, ph.nch, Kt);
     }
     eac_p.add(e_ac);
     ech_p.add(e_ch);
@@ -316,33 +311,32 @@ __device__ __forceinline__ float pair_sum(Pair a, Pair b) {
 // parameters: read from the constant bank, never recomputed in the loop)
 struct EConst {
   float i4hx, i4hy, i4hz, half_epn2;
-  float a2h, a4q, a6s, g, th, Ah;
+  float K[16];       // plugin constants, the reference composition c0 (if any) as 0
   float p2, p3, p4;  // the 2-3-4 polynomial of energy form 0
   Pair kdp, kcp;     // cshift - c0 and cshift as float pairs
 };
 
+// The plugin sees the concentration as c - c0 (exact in pair arithmetic from
+// the stored c - cshift) with its c0 constant 0, where it names one.
+template <typename PL>
 static EConst econst(const Phys &ph) {
   EConst c;
   c.i4hx = (float)(0.25 / ph.h[0]);
   c.i4hy = (float)(0.25 / ph.h[1]);
   c.i4hz = (float)(0.25 / ph.h[2]);
   c.half_epn2 = (float)(0.5 * ph.epn2);
-  c.a2h = (float)(ph.a2 / 2.0);
-  c.a4q = (float)(ph.a4 / 4.0);
-  c.a6s = (float)(ph.a6 / 6.0);
-  c.g = (float)ph.g;
-  c.th = (float)ph.th;
-  c.Ah = (float)(ph.A / 2.0);
+  for (int k = 0; k < 16; k++) c.K[k] = (float)ph.K[k];
+  const double kd = PL::c0_index >= 0 ? -ph.K[PL::c0_index] : 0.0;  // ph.K holds c0 - cshift
+  if (PL::c0_index >= 0) c.K[PL::c0_index] = 0.0f;
+  c.kdp = Pair{(float)kd, (float)(kd - (double)(float)kd)};
   c.p2 = (float)(2376.0 / 2372.0 / 2.0);
   c.p3 = (float)((7128.0 + 12.0 * 2372.0) / 2372.0 / 3.0);
   c.p4 = (float)((4752.0 + 12.0 * 2372.0) / 2372.0 / 4.0);
-  const double kd = ph.cshift - ph.c0;
-  c.kdp = Pair{(float)kd, (float)(kd - (double)(float)kd)};
   c.kcp = Pair{(float)ph.cshift, (float)(ph.cshift - (double)(float)ph.cshift)};
   return c;
 }
 
-template <int NAC, int NCH>
+template <typename PL, int NAC, int NCH>
 __global__ void __launch_bounds__(256, 2) energy_partial_f32(Phys ph, EConst ec, const float *__restrict__ u,
                                                              const double *__restrict__ elam, int form,
                                                              double *__restrict__ part) {
@@ -358,7 +352,9 @@ __global__ void __launch_bounds__(256, 2) energy_partial_f32(Phys ph, EConst ec,
   }
   __syncthreads();
   const float i4hx = ec.i4hx, i4hy = ec.i4hy, i4hz = ec.i4hz, half_epn2 = ec.half_epn2;
-  const float a2h = ec.a2h, a4q = ec.a4q, a6s = ec.a6s, g = ec.g, th = ec.th, Ah = ec.Ah;
+  float Kt[16];
+#pragma unroll
+  for (int k = 0; k < 16; k++) Kt[k] = ec.K[k];
   const float p2 = ec.p2, p3 = ec.p3, p4 = ec.p4;
   const Pair kdp = ec.kdp, kcp = ec.kcp;
   float mx[F], mn[F];
@@ -460,17 +456,12 @@ __global__ void __launch_bounds__(256, 2) energy_partial_f32(Phys ph, EConst ec,
           }
           if (NCH > 0) e_ch += (cval * cval - 1.0f) * (cval * cval - 1.0f) * 0.25f;
         } else {
-          float fl = 0.0f, s2 = 0.0f;
+          sclet_acv<float> ac[NAC > 0 ? NAC : 1];
+          sclet_chv<float> ch[1];
 #pragma unroll
-          for (int m = 0; m < (NAC < 4 ? NAC : 4); m++) {
-            const float u2 = avg[m] * avg[m];
-            s2 += u2;
-            fl += a2h * u2 + a4q * u2 * u2 + a6s * u2 * u2 * u2;
-#pragma unroll
-            for (int q = m + 1; q < (NAC < 4 ? NAC : 4); q++) fl += g * u2 * avg[q] * avg[q];
-          }
-          if (NCH > 0) fl += Ah * cd * cd - th * cd * s2;
-          e_ac += fl;
+          for (int m = 0; m < NAC; m++) ac[m].u = avg[m];
+          ch[0].c = cd;
+          e_ac += PL::template f_bulk<float>(ac, ch, NAC, NCH, Kt);
         }
         eac_p.add(e_ac);
         ech_p.add(e_ch);
@@ -563,32 +554,43 @@ int check_soln_partials(int n) {
   return u > 152 * 4 ? 152 * 4 : (u < 1 ? 1 : u);
 }
 
-template <int NAC, int NCH>
+template <typename PL, int NAC, int NCH>
 static void launch_f32(const Phys &ph, const float *u, const double *elam, int form, double *partials, int npart,
                        cudaStream_t s) {
-  energy_partial_f32<NAC, NCH><<<npart, dim3(32, 8), 0, s>>>(ph, econst(ph), u, elam, form, partials);
+  energy_partial_f32<PL, NAC, NCH><<<npart, dim3(32, 8), 0, s>>>(ph, econst<PL>(ph), u, elam, form, partials);
+}
+
+template <typename PL, typename T>
+static cudaError_t check_soln_pl(const Phys &ph, const T *u, const double *elam, int form, double *partials,
+                                 int npart, cudaStream_t s) {
+  if constexpr (sizeof(T) == 4) {
+    const float *uf = u;
+    switch (ph.nac * 2 + ph.nch) {
+      case 1: launch_f32<PL, 0, 1>(ph, uf, elam, form, partials, npart, s); break;
+      case 2: launch_f32<PL, 1, 0>(ph, uf, elam, form, partials, npart, s); break;
+      case 3: launch_f32<PL, 1, 1>(ph, uf, elam, form, partials, npart, s); break;
+      case 4: launch_f32<PL, 2, 0>(ph, uf, elam, form, partials, npart, s); break;
+      case 5: launch_f32<PL, 2, 1>(ph, uf, elam, form, partials, npart, s); break;
+      case 6: launch_f32<PL, 3, 0>(ph, uf, elam, form, partials, npart, s); break;
+      case 7: launch_f32<PL, 3, 1>(ph, uf, elam, form, partials, npart, s); break;
+      case 8: launch_f32<PL, 4, 0>(ph, uf, elam, form, partials, npart, s); break;
+      default: launch_f32<PL, 4, 1>(ph, uf, elam, form, partials, npart, s); break;
+    }
+  } else {
+    energy_partial_kernel<PL, T><<<npart, EB, 0, s>>>(ph, u, elam, form, partials);
+  }
+  return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_check_soln(const Phys &ph, const T *u, const double *elam, int form, double *partials, int npart,
                               double *out, cudaStream_t s) {
   if (ph.F < 1 || ph.F > MAXF || ph.nac > 4 || ph.nch > 1) return cudaErrorInvalidValue;
-  if constexpr (sizeof(T) == 4) {
-    const float *uf = u;
-    switch (ph.nac * 2 + ph.nch) {
-      case 1: launch_f32<0, 1>(ph, uf, elam, form, partials, npart, s); break;
-      case 2: launch_f32<1, 0>(ph, uf, elam, form, partials, npart, s); break;
-      case 3: launch_f32<1, 1>(ph, uf, elam, form, partials, npart, s); break;
-      case 4: launch_f32<2, 0>(ph, uf, elam, form, partials, npart, s); break;
-      case 5: launch_f32<2, 1>(ph, uf, elam, form, partials, npart, s); break;
-      case 6: launch_f32<3, 0>(ph, uf, elam, form, partials, npart, s); break;
-      case 7: launch_f32<3, 1>(ph, uf, elam, form, partials, npart, s); break;
-      case 8: launch_f32<4, 0>(ph, uf, elam, form, partials, npart, s); break;
-      default: launch_f32<4, 1>(ph, uf, elam, form, partials, npart, s); break;
-    }
-  } else {
-    energy_partial_kernel<T><<<npart, EB, 0, s>>>(ph, u, elam, form, partials);
-  }
+  cudaError_t e = with_physics(ph.physics, [&](auto *tag) {
+    using PL = std::remove_pointer_t<decltype(tag)>;
+    return check_soln_pl<PL, T>(ph, u, elam, form, partials, npart, s);
+  });
+  if (e != cudaSuccess) return e;
   energy_final_kernel<<<1, 32 * (3 * MAXF + 2), 0, s>>>(ph, form, partials, npart, out);
   launch_counter() += 2;
   return cudaGetLastError();

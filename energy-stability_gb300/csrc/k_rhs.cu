@@ -14,9 +14,10 @@
 //   N_c = lap(t) (zero outside) - mu(outside) / h^2 on faces, with
 //   mu = LCI (epn2 lap(c) - CH_f) at the periodic image of the outside cell
 //   (ch_mu, trans.c:1433-1937).
-// The physics plugin is the Landau 2-4-6 form with a cross term and a c-eta
-// coupling (the drop-in replacement of formula.c:9-56).
+// AC_f and CH_f come from the run's physics plugin (the drop-in form of
+// formula.c:9-56, sclet_physics.cuh), a template parameter of every kernel.
 #include "sclet_internal.cuh"
+#include "sclet_physics.cuh"
 
 namespace sclet {
 
@@ -26,7 +27,7 @@ struct P {
   T epn2, hx, hy, hz, LE, KE, LCI, KCI, es;
   T ih2x, ih2y, ih2z;   // 1 / h^2 per axis
   T i2hx, i2hy, i2hz;   // 1 / (2 h) per axis
-  T a2, a4, a6, g, th, c0, A;
+  T K[16];              // plugin constants (reference composition shifted by cshift)
   // anisotropic term folded: kan[m][3 r + c] = epn2 LE (1/2h_r) lam_m[r][c] (1/2h_c),
   // the flux row r differenced along axis r
   T kan[4][9];
@@ -41,7 +42,7 @@ static P<T> to_p(const Phys &ph) {
   p.ih2z = (T)(1.0 / (ph.h[2] * ph.h[2]));
   p.i2hx = (T)(0.5 / ph.h[0]); p.i2hy = (T)(0.5 / ph.h[1]); p.i2hz = (T)(0.5 / ph.h[2]);
   p.LE = (T)ph.LE; p.KE = (T)ph.KE; p.LCI = (T)ph.LCI; p.KCI = (T)ph.KCI; p.es = (T)ph.elastic_scale;
-  p.a2 = (T)ph.a2; p.a4 = (T)ph.a4; p.a6 = (T)ph.a6; p.g = (T)ph.g; p.th = (T)ph.th; p.c0 = (T)(ph.c0 - ph.cshift); p.A = (T)ph.A;
+  for (int k = 0; k < 16; k++) p.K[k] = (T)ph.K[k];
   const double i2h[3] = {0.5 / ph.h[0], 0.5 / ph.h[1], 0.5 / ph.h[2]};
   for (int m = 0; m < 4; m++)
     for (int k = 0; k < 9; k++) {
@@ -50,24 +51,26 @@ static P<T> to_p(const Phys &ph) {
   return p;
 }
 
-// dF/deta_m of the plugin (AC_f), NAC fields known at compile time.
-template <typename T, int NAC>
+// AC_f(m) / CH_f(0) of plugin PL at one cell: NAC order parameters e (known
+// at compile time) and the stored concentration c.
+template <typename PL, typename T, int NAC>
 __device__ __forceinline__ T ac_f_n(const P<T> &p, const T *e, T c, int m) {
-  T u = e[m], u2 = u * u, others = (T)0;
+  sclet_acv<T> ac[NAC > 0 ? NAC : 1];
+  sclet_chv<T> ch[1];
 #pragma unroll
-  for (int k = 0; k < NAC; k++)
-    if (k != m) others += e[k] * e[k];
-  T f = p.a2 * u + p.a4 * u2 * u + p.a6 * u2 * u2 * u + (T)2 * p.g * u * others;
-  if (p.nch > 0) f -= (T)2 * p.th * (c - p.c0) * u;
-  return f;
+  for (int k = 0; k < NAC; k++) ac[k].u = e[k];
+  ch[0].c = c;
+  return PL::template ac_f<T>(ac, ch, NAC, p.nch, p.K, m);
 }
 
-// dF/dc of the plugin (CH_f).
-template <typename T>
-__device__ inline T ch_f(const P<T> &p, const T *e, T c) {
-  T s = (T)0;
-  for (int k = 0; k < p.nac; k++) s += e[k] * e[k];
-  return p.A * (c - p.c0) - p.th * s;
+template <typename PL, typename T>
+__device__ __forceinline__ T ch_f(const P<T> &p, const T *e, T c) {
+  sclet_acv<T> ac[4];
+  sclet_chv<T> ch[1];
+#pragma unroll
+  for (int k = 0; k < 4; k++) ac[k].u = e[k];
+  ch[0].c = c;
+  return PL::template ch_f<T>(ac, ch, p.nac, 1, p.K, 0);
 }
 
 __device__ inline long long L3(int n, int z, int y, int x) { return ((long long)z * n + y) * n + x; }
@@ -85,7 +88,7 @@ constexpr int ZC = 32;             // planes per CTA
 constexpr int HX = RX + 4, HY = RY + 4;
 constexpr int PLANE = HX * HY;     // one haloed plane
 
-template <typename T, int NAC, bool ANISO>
+template <typename PL, typename T, int NAC, bool ANISO>
 __global__ void __launch_bounds__(RX * RY) rhs_ac_kernel(P<T> p, const T *__restrict__ u, const T *__restrict__ felas,
                                                          T *__restrict__ out) {
   extern __shared__ unsigned char smem_raw[];
@@ -156,7 +159,7 @@ __global__ void __launch_bounds__(RX * RY) rhs_ac_kernel(P<T> p, const T *__rest
         const T *um = u + m * n3;
         const T *rg = ring + (size_t)m * 5 * PLANE;
         T v = p.LE * p.KE * e[m];
-        v -= p.LE * ac_f_n<T, NAC>(p, e, c, m);
+        v -= p.LE * ac_f_n<PL, T, NAC>(p, e, c, m);
         if (face) {
           const int iz = img(n, z), iy = img(n, y), ix = img(n, x), lo = img(n, -1), hi = img(n, n);
           const T w = p.LE * p.epn2;
@@ -199,7 +202,7 @@ __global__ void __launch_bounds__(RX * RY) rhs_ac_kernel(P<T> p, const T *__rest
 
 // t = -LCI KCI c + LCI CH_f, minus the face liftings (first part of
 // ch_calc_FU_ConstantMobility).
-template <typename T>
+template <typename PL, typename T>
 __global__ void __launch_bounds__(RX * RY) rhs_ch_t_kernel(P<T> p, const T *__restrict__ u, T *__restrict__ t) {
   const int n = p.n;
   const int x = blockIdx.x * RX + threadIdx.x, y = blockIdx.y * RY + threadIdx.y, z = blockIdx.z;
@@ -213,7 +216,7 @@ __global__ void __launch_bounds__(RX * RY) rhs_ch_t_kernel(P<T> p, const T *__re
     if (m < p.nac) e[m] = u[m * n3 + l];
   const T c = cf[l];
   T v = -p.LCI * p.KCI * c;
-  v += p.LCI * ch_f(p, e, c);
+  v += p.LCI * ch_f<PL>(p, e, c);
   if (x == 0 || x == n - 1 || y == 0 || y == n - 1 || z == 0 || z == n - 1) {
     const int iz = img(n, z), iy = img(n, y), ix = img(n, x), lo = img(n, -1), hi = img(n, n);
     const T w = p.LCI * p.epn2;
@@ -228,7 +231,7 @@ __global__ void __launch_bounds__(RX * RY) rhs_ch_t_kernel(P<T> p, const T *__re
 }
 
 // Boundary chemical potential at periodic image cell (z,y,x) (ch_mu).
-template <typename T>
+template <typename PL, typename T>
 __device__ inline T ch_mu_at(const P<T> &p, const T *__restrict__ u, int z, int y, int x) {
   int n = p.n;
   long long n3 = (long long)n * n * n;
@@ -237,15 +240,15 @@ __device__ inline T ch_mu_at(const P<T> &p, const T *__restrict__ u, int z, int 
   T lap = (cf[L3(n, z, y, img(n, x - 1))] + (T)(-2.0) * cv + cf[L3(n, z, y, img(n, x + 1))]) * p.ih2x;
   lap += (cf[L3(n, z, img(n, y - 1), x)] + (T)(-2.0) * cv + cf[L3(n, z, img(n, y + 1), x)]) * p.ih2y;
   lap += (cf[L3(n, img(n, z - 1), y, x)] + (T)(-2.0) * cv + cf[L3(n, img(n, z + 1), y, x)]) * p.ih2z;
-  T e[4];
+  T e[4] = {(T)0, (T)0, (T)0, (T)0};
   for (int m = 0; m < p.nac; m++) e[m] = u[m * n3 + L3(n, z, y, x)];
   T mu = p.LCI * p.epn2 * lap;
-  mu -= p.LCI * ch_f(p, e, cv);
+  mu -= p.LCI * ch_f<PL>(p, e, cv);
   return mu;
 }
 
 // N_c = lap(t) (zero outside), minus mu(outside)/h^2 on faces.
-template <typename T>
+template <typename PL, typename T>
 __global__ void __launch_bounds__(RX * RY) rhs_ch_lap_kernel(P<T> p, const T *__restrict__ u, const T *__restrict__ t,
                                                              T *__restrict__ out) {
   const int n = p.n;
@@ -262,18 +265,18 @@ __global__ void __launch_bounds__(RX * RY) rhs_ch_lap_kernel(P<T> p, const T *__
   v += (ff + fk - (T)2 * tc) * p.ih2z;
   if (x == 0 || x == n - 1 || y == 0 || y == n - 1 || z == 0 || z == n - 1) {
     const int iz = img(n, z), iy = img(n, y), ix = img(n, x), lo = img(n, -1), hi = img(n, n);
-    if (x == 0) v -= ch_mu_at(p, u, iz, iy, lo) * p.ih2x;
-    if (x == n - 1) v -= ch_mu_at(p, u, iz, iy, hi) * p.ih2x;
-    if (y == 0) v -= ch_mu_at(p, u, iz, lo, ix) * p.ih2y;
-    if (y == n - 1) v -= ch_mu_at(p, u, iz, hi, ix) * p.ih2y;
-    if (z == 0) v -= ch_mu_at(p, u, lo, iy, ix) * p.ih2z;
-    if (z == n - 1) v -= ch_mu_at(p, u, hi, iy, ix) * p.ih2z;
+    if (x == 0) v -= ch_mu_at<PL>(p, u, iz, iy, lo) * p.ih2x;
+    if (x == n - 1) v -= ch_mu_at<PL>(p, u, iz, iy, hi) * p.ih2x;
+    if (y == 0) v -= ch_mu_at<PL>(p, u, iz, lo, ix) * p.ih2y;
+    if (y == n - 1) v -= ch_mu_at<PL>(p, u, iz, hi, ix) * p.ih2y;
+    if (z == 0) v -= ch_mu_at<PL>(p, u, lo, iy, ix) * p.ih2z;
+    if (z == n - 1) v -= ch_mu_at<PL>(p, u, hi, iy, ix) * p.ih2z;
   }
   out[l] = v;
 }
 
-template <typename T>
-cudaError_t launch_rhs(const Phys &ph, const T *u, const T *felas, T *out, T *scratch, cudaStream_t s) {
+template <typename PL, typename T>
+static cudaError_t launch_rhs_pl(const Phys &ph, const T *u, const T *felas, T *out, T *scratch, cudaStream_t s) {
   P<T> p = to_p<T>(ph);
   long long n3 = (long long)ph.n * ph.n * ph.n;
   const dim3 blk(RX, RY), grd((ph.n + RX - 1) / RX, (ph.n + RY - 1) / RY, ph.n);
@@ -282,10 +285,11 @@ cudaError_t launch_rhs(const Phys &ph, const T *u, const T *felas, T *out, T *sc
     const dim3 gac((ph.n + RX - 1) / RX, (ph.n + RY - 1) / RY, (ph.n + ZC - 1) / ZC);
     cudaError_t e = cudaSuccess;
     switch (ph.nac * 2 + (ph.anisotropic ? 1 : 0)) {
-#define SCLET_RHS_AC(NAC, AN)                                                                                   \
-  case NAC * 2 + AN:                                                                                            \
-    e = cudaFuncSetAttribute(rhs_ac_kernel<T, NAC, AN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-    if (e == cudaSuccess) rhs_ac_kernel<T, NAC, AN><<<gac, blk, smem, s>>>(p, u, felas, out);                    \
+#define SCLET_RHS_AC(NAC, AN)                                                                                  \
+  case NAC * 2 + AN:                                                                                           \
+    e = cudaFuncSetAttribute(rhs_ac_kernel<PL, T, NAC, AN>, cudaFuncAttributeMaxDynamicSharedMemorySize,        \
+                             (int)smem);                                                                       \
+    if (e == cudaSuccess) rhs_ac_kernel<PL, T, NAC, AN><<<gac, blk, smem, s>>>(p, u, felas, out);               \
     break;
       SCLET_RHS_AC(1, 0) SCLET_RHS_AC(1, 1) SCLET_RHS_AC(2, 0) SCLET_RHS_AC(2, 1)
       SCLET_RHS_AC(3, 0) SCLET_RHS_AC(3, 1) SCLET_RHS_AC(4, 0) SCLET_RHS_AC(4, 1)
@@ -295,13 +299,23 @@ cudaError_t launch_rhs(const Phys &ph, const T *u, const T *felas, T *out, T *sc
     if (e != cudaSuccess) return e;
     launch_counter()++;
   }
-  for (int m = 0; m < ph.nch; m++) {
-    // one conserved field (the plugin's CH_f is defined for c_0 only)
-    rhs_ch_t_kernel<T><<<grd, blk, 0, s>>>(p, u, scratch);
-    rhs_ch_lap_kernel<T><<<grd, blk, 0, s>>>(p, u, scratch, out + (long long)ph.nac * n3);
-    launch_counter() += 2;
+  if (PL::max_nch > 0) {
+    for (int m = 0; m < ph.nch; m++) {
+      // one conserved field (the plugins' CH_f is defined for c_0 only)
+      rhs_ch_t_kernel<PL, T><<<grd, blk, 0, s>>>(p, u, scratch);
+      rhs_ch_lap_kernel<PL, T><<<grd, blk, 0, s>>>(p, u, scratch, out + (long long)ph.nac * n3);
+      launch_counter() += 2;
+    }
   }
   return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_rhs(const Phys &ph, const T *u, const T *felas, T *out, T *scratch, cudaStream_t s) {
+  return with_physics(ph.physics, [&](auto *tag) {
+    using PL = std::remove_pointer_t<decltype(tag)>;
+    return launch_rhs_pl<PL, T>(ph, u, felas, out, scratch, s);
+  });
 }
 
 template cudaError_t launch_rhs<double>(const Phys &, const double *, const double *, double *, double *, cudaStream_t);

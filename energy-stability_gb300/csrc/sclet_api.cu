@@ -18,6 +18,7 @@
 
 #include "sclet_gb300.h"
 #include "sclet_internal.cuh"
+#include "sclet_physics.cuh"
 #include "sclet_tc.cuh"
 
 namespace sclet {
@@ -196,7 +197,8 @@ int upload_eigen(sclet_ctx *ctx, const double *d, const double *v, const double 
     const double kk[3] = {p.kkx, p.kky, p.kkz};
     for (int kind = 0; kind < 2; kind++)
       CK(tc_make_coefs(ctx->coef[kind], ctx->coef2[kind], n, kind, ctx->dd[0], ctx->dd[1], ctx->dd[2], kk, p.epn2,
-                       p.dt, p.landau[7 + 2 * kind], p.landau[8 + 2 * kind], ctx->stream));
+                       p.dt, kind == 0 ? ctx->ph.LE : ctx->ph.LCI, kind == 0 ? ctx->ph.KE : ctx->ph.KCI,
+                       ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     if (ctx->nch > 0) return mass_weights_setup(ctx, v, vi);
     return SCLET_OK;
@@ -489,18 +491,12 @@ int sclet_create(const sclet_params *p, int precision, int device, sclet_ctx **o
     for (int i = 0; i < 3; i++)
       for (int j = 0; j < 3; j++) ph.lam[m][i * 3 + j] = (i == j ? ph.kk[i] : 0.0) - p->lambda_file[m][i * 3 + j];
   ph.elastic_scale = p->elastic_scale;
-  ph.a2 = p->landau[0];
-  ph.a4 = p->landau[1];
-  ph.a6 = p->landau[2];
-  ph.g = p->landau[3];
-  ph.th = p->landau[4];
-  ph.c0 = p->landau[5];
-  ph.cshift = (precision == SCLET_MIXED && ctx->nch > 0) ? ph.c0 : 0.0;
-  ph.A = p->landau[6];
-  ph.LE = p->landau[7];
-  ph.KE = p->landau[8];
-  ph.LCI = p->landau[9];
-  ph.KCI = p->landau[10];
+  // init_KL and the plugin's constants (formula.c:9-19)
+  if (const char *why = physics_setup(p, precision, &ph)) {
+    g_create_error = why;
+    delete ctx;
+    return SCLET_ERR_UNSUPPORTED;
+  }
 
   int rc = SCLET_OK;
   cudaError_t e;

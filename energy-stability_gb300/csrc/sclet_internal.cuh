@@ -17,12 +17,18 @@ struct Phys {
   double kk[3];
   double lam[4][9];      // F2 tensors: diag(kk) - file tensor, row-major
   double elastic_scale;
-  double a2, a4, a6, g, th, c0, A, LE, KE, LCI, KCI;
+  // physics plugin (SCLET_PHYSICS_*) and its constants as the kernels see
+  // them (the reference composition shifted by cshift, see below); LE, KE,
+  // LCI, KCI from the plugin's init_KL
+  int physics;
+  double K[16];
+  double LE, KE, LCI, KCI;
   // Offset of the stored conserved field: the device holds c - cshift.  The
   // mixed form stores c - c0 (cshift = c0), which keeps FP32 storage and the
   // transforms at the scale of the fluctuations; the scheme is linear in c
   // and the constant state c0 is a fixed point, so this changes nothing in
-  // exact arithmetic.  0 in the FP64 form.
+  // exact arithmetic.  It needs a plugin whose c enters only as c - c0
+  // (SCLET_C0_INDEX); 0 otherwise and in the FP64 form.
   double cshift;
 };
 

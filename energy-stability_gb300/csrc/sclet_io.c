@@ -131,6 +131,19 @@ int sclet_read_case(const char *dir, const char *suffix, sclet_params *p) {
       if ((rc = sclet_read_landau_input(path, p)) != SCLET_OK) return rc;
     }
   }
+  snprintf(path, sizeof path, "%s/physics_input.txt", dir);
+  {
+    FILE *f = fopen(path, "r");
+    if (f) {
+      char name[64] = {0};
+      int ok = fscanf(f, "%63s", name) == 1;
+      fclose(f);
+      if (!ok) return SCLET_ERR_IO;
+      if (strcmp(name, "landau246") == 0) p->physics = SCLET_PHYSICS_LANDAU246;
+      else if (strcmp(name, "formula234") == 0) p->physics = SCLET_PHYSICS_FORMULA234;
+      else return SCLET_ERR_ARG;
+    }
+  }
   return SCLET_OK;
 }
 

@@ -23,6 +23,7 @@
 
 #include "../../include/sclet_gb300.h"
 #include "sclet_internal.cuh"
+#include "sclet_physics.cuh"
 
 namespace sclet {
 namespace {
@@ -173,17 +174,11 @@ extern "C" int sclet_check_soln_noalloc(const sclet_params *p, int precision, co
   ph.kk[0] = p->kkx;
   ph.kk[1] = p->kky;
   ph.kk[2] = p->kkz;
-  ph.a2 = p->landau[0];
-  ph.a4 = p->landau[1];
-  ph.a6 = p->landau[2];
-  ph.g = p->landau[3];
-  ph.th = p->landau[4];
-  ph.c0 = p->landau[5];
-  ph.A = p->landau[6];
-  ph.LE = p->landau[7];
-  ph.KE = p->landau[8];
-  ph.LCI = p->landau[9];
-  ph.KCI = p->landau[10];
+  // the caller's blocks hold c itself (no stored offset), whatever the precision
+  if (const char *why = physics_setup(p, SCLET_FP64, &ph)) {
+    set_msg(msg, msg_len, why);
+    return SCLET_ERR_UNSUPPORTED;
+  }
   // Gradient tensor of each order parameter in the energy: the file tensor
   // when the run is anisotropic, diag(kk) otherwise.
   Lam36 lam;

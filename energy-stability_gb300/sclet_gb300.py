@@ -17,6 +17,7 @@ LIB_PATH = os.path.join(HERE, "libsclet_gb300.so")
 
 AC, CH = 0, 1
 FP64, MIXED = 0, 1
+PHYSICS_LANDAU246, PHYSICS_FORMULA234 = 0, 1
 
 _c_dp = ctypes.POINTER(ctypes.c_double)
 
@@ -43,6 +44,7 @@ class Params(ctypes.Structure):
         ("eigenstrain", ctypes.c_double * 36),
         ("lambda_file", ctypes.c_double * 36),
         ("landau", ctypes.c_double * 11),
+        ("physics", ctypes.c_int),
     ]
 
 

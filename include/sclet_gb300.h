@@ -45,6 +45,17 @@ extern "C" {
 #define SCLET_FP64 0
 #define SCLET_MIXED 1
 
+/* Physics plugins (sclet_params.physics), the drop-in replacements of the
+ * reference's formula.c (init_KL, AC_f, CH_f; source_beta_to_omega/src/
+ * formula.c:9-56), each one source compiled for the host and the device
+ * (energy-stability_gb300/plugins/):
+ *   SCLET_PHYSICS_LANDAU246  Landau 2-4-6 with cross term and c-eta coupling,
+ *                            constants from landau_input.txt (landau[])
+ *   SCLET_PHYSICS_FORMULA234 the reference's own formula.c: LE = 1, KE = 42,
+ *                            the 2-3-4 polynomial; order parameters only */
+#define SCLET_PHYSICS_LANDAU246 0
+#define SCLET_PHYSICS_FORMULA234 1
+
 typedef struct sclet_ctx sclet_ctx;
 
 /* Everything the reference reads from its input files. */
@@ -75,8 +86,12 @@ typedef struct sclet_params {
    * the file tensors; the step uses diag(kk) - lambda_file */
   double lambda_file[4][9];
   /* physics plugin constants (replaces the compile-time constants of
-   * source_beta_to_omega/src/formula.c:9-38): a2 a4 a6 g th c0 A LE KE LCI KCI */
+   * source_beta_to_omega/src/formula.c:9-38): a2 a4 a6 g th c0 A LE KE LCI KCI
+   * for SCLET_PHYSICS_LANDAU246 */
   double landau[11];
+  /* which physics plugin (SCLET_PHYSICS_*); the reference selects its
+   * formula.c at link time.  Default SCLET_PHYSICS_LANDAU246. */
+  int physics;
 } sclet_params;
 
 /* Diagnostics of one state (check_soln_new, field.c:407-678), per field. */
@@ -95,7 +110,10 @@ int sclet_read_elastic_input(const char *path, sclet_params *p);
 int sclet_read_anisotropic_input(const char *path, sclet_params *p);
 /* init_KL() constants of the physics plugin (formula.c:9-19); 11 numbers */
 int sclet_read_landau_input(const char *path, sclet_params *p);
-/* All of the above from a run directory, as main() does (ScLETD.c:15-72). */
+/* All of the above from a run directory, as main() does (ScLETD.c:15-72);
+ * landau_input.txt and physics_input.txt (one word: the plugin name,
+ * "landau246" or "formula234") are optional.  The reference picks its
+ * formula.c when it is built; physics_input.txt is this library's stand-in. */
 int sclet_read_case(const char *dir, const char *suffix, sclet_params *p);
 /* One eigen variant as read_matrices() reads it (vars.c:370-476):
  * d<k><n>.dat (n values), v<k><n>.dat and vi<k><n>.dat (n x n, row by row).

@@ -138,6 +138,10 @@ def cubic_voigt(c11: float, c12: float, c44: float) -> np.ndarray:
     return c
 
 
+# physics plugin names of physics_input.txt (read by sclet_read_case)
+PHYSICS_NAMES = {0: "landau246", 1: "formula234"}
+
+
 @dataclasses.dataclass
 class Case:
     big_n: int = 64                 # physical edge N; block edge n = N + 4
@@ -160,6 +164,7 @@ class Case:
     eta_range: Sequence[float] = (-0.01, 0.01)
     c_range: Sequence[float] = (0.48, 0.52)
     suffix: str = "case"
+    physics: int = 0                # 0 Landau 2-4-6 plugin, 1 the reference's own formula.c
 
     @property
     def n(self) -> int:
@@ -211,6 +216,9 @@ def write_case(case: Case, dirpath: str, eigen: bool = True, fields: bool = True
             fp.write("\n")
     with open(os.path.join(dirpath, "landau_input.txt"), "w") as fp:
         fp.write(" ".join(repr(float(x)) for x in case.landau) + "\n")
+    if case.physics:
+        with open(os.path.join(dirpath, "physics_input.txt"), "w") as fp:
+            fp.write(PHYSICS_NAMES[case.physics] + "\n")
     for kind, m, vals in (case.initial_fields() if fields else []):
         with open(os.path.join(dirpath, "input", f"field_iter0_{kind}{m}_000.txt"), "w") as fp:
             np.savetxt(fp, vals.reshape(-1), fmt="%.17g")

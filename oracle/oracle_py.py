@@ -29,9 +29,9 @@ class OrcCfg(ctypes.Structure):
         ("h", ctypes.c_double * 3), ("kk", ctypes.c_double * 3),
         ("lam", ctypes.c_double * 36),
         ("elastic_scale", ctypes.c_double),
-        ("a2", ctypes.c_double), ("a4", ctypes.c_double), ("a6", ctypes.c_double),
-        ("g", ctypes.c_double), ("th", ctypes.c_double), ("c0", ctypes.c_double),
-        ("A", ctypes.c_double), ("LE", ctypes.c_double), ("KE", ctypes.c_double),
+        ("physics", ctypes.c_int),
+        ("K", ctypes.c_double * 16),
+        ("LE", ctypes.c_double), ("KE", ctypes.c_double),
         ("LCI", ctypes.c_double), ("KCI", ctypes.c_double),
         ("mp", _dp * 3), ("mpi", _dp * 3), ("dd", _dp * 3),
         ("bn", _dp),
@@ -98,6 +98,11 @@ def load_case(case_dir: str, suffix: str, fields=None) -> Dict:
         lam_file[: p["nac"]] = np.array(an[: 9 * p["nac"]]).reshape(p["nac"], 3, 3)
     p["lam_file"] = lam_file
     p["landau"] = _read_numbers(os.path.join(case_dir, "landau_input.txt"))
+    p["physics"] = 0
+    phys = os.path.join(case_dir, "physics_input.txt")
+    if os.path.exists(phys):
+        with open(phys) as fp:
+            p["physics"] = {"landau246": 0, "formula234": 1}[fp.read().split()[0]]
     # eigen data of the Dirichlet-Dirichlet variant (id 3, src/vars.c:488-582):
     # the case's files when written, else the closed form
     if os.path.exists(os.path.join(case_dir, f"d3{n}.dat")):
@@ -149,7 +154,13 @@ class Oracle:
         for i, v in enumerate(lam.reshape(-1)):
             c.lam[i] = v
         c.elastic_scale = p["elastic_scale"]
-        (c.a2, c.a4, c.a6, c.g, c.th, c.c0, c.A, c.LE, c.KE, c.LCI, c.KCI) = p["landau"]
+        # physics plugin: 0 the Landau 2-4-6 form (landau_input.txt), 1 the
+        # reference's own formula.c (2-3-4, LE = 1, KE = 42)
+        c.physics = p.get("physics", 0)
+        for i, v in enumerate(p["landau"] if c.physics == 0 else []):
+            c.K[i] = v
+        if self.lib.orc_physics_setup(ctypes.byref(c)) != 0:
+            raise ValueError(f"unknown physics plugin {c.physics}")
         # matrices column-major like the reference (element (r, c) at c*n + r)
         self._keep = []
         for d in range(3):

@@ -3,7 +3,7 @@ directory written by oracle/cases.py and saves arrays to an .npz file.
 Test infrastructure; each run is a fresh process (the reference keeps its state
 in process globals).
 
-    python oracle/ref_runner.py LIB CASE_DIR SUFFIX STEPS OUT.npz [--probe|--rhs]
+    python oracle/ref_runner.py LIB CASE_DIR SUFFIX STEPS OUT.npz [--probe|--rhs|--check]
 
 Saved arrays (n = block edge incl. ghosts, layout [z, y, x]):
   ac{m} / ch{m}      field after STEPS loop passes
@@ -20,6 +20,8 @@ With --probe the first pass is replaced by a halo probe: every cell of every
 field is set to a unique code (its linear index + 1 + 10^7 * field) before
 transfer() and calc_mu(), so the saved ghost cells and boundary values name the
 cell they were copied from.
+With --check the reference's own check_soln_new runs after every pass, as in
+its time loop, and writes its CSV logs under CASE_DIR/output/.
 """
 import ctypes
 import os
@@ -61,7 +63,7 @@ def main(argv):
     kinds = [(0, "ac", m) for m in range(nac)] + [(1, "ch", m) for m in range(nch)]
     save["init_fields"] = np.stack([arr(k, m, 0, n3).copy() for k, _, m in kinds]).reshape(-1, n, n, n)
 
-    lib.ref_set_check(0)
+    lib.ref_set_check(1 if "--check" in argv else 0)
     if probe:
         for f, (k, _, m) in enumerate(kinds):
             a = arr(k, m, 0, n3)

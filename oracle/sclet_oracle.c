@@ -7,6 +7,17 @@
 #include "sclet_oracle.h"
 #include "ref_shims/oracle_fft.h"
 
+/* the physics plugins: the same sources the device kernels compile */
+#include "../energy-stability_gb300/plugins/sclet_plugin.h"
+#define SCLET_PLUGIN_NS(x) landau246_##x
+#include "../energy-stability_gb300/plugins/landau246.h"
+#undef SCLET_PLUGIN_NS
+#define SCLET_PLUGIN_NS(x) formula234_##x
+#include "../energy-stability_gb300/plugins/formula234.h"
+#undef SCLET_PLUGIN_NS
+#undef K
+#undef real
+
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -93,23 +104,50 @@ void orc_boundary_values(int n, const double *f, double *faces) {
 }
 
 /* ---------------------------------------------------------------------- */
-/* Physics plugin (the 2-4-6 Landau form of oracle/ref_plugin), restated.  */
+/* Physics plugin of the run: AC_f / CH_f at one cell (formula.c:28-56, as  */
+/* SWTICH_AC_FIELD1 / SWITCH_CH_FIELD1 load ac[m].u and ch[m].c,            */
+/* ScLETD.h:108-135).                                                       */
 /* ---------------------------------------------------------------------- */
-static double ac_f(const orc_cfg *c, const double *e, double cval, int m) {
-  double u = e[m], u2 = u * u, others = 0.0, f;
+static void load_cell(const orc_cfg *c, const double *e, double cval, sclet_acv *ac, sclet_chv *ch) {
   int k;
-  for (k = 0; k < c->nac; k++)
-    if (k != m) others += e[k] * e[k];
-  f = c->a2 * u + c->a4 * u2 * u + c->a6 * u2 * u2 * u + 2.0 * c->g * u * others;
-  if (c->nch > 0) f -= 2.0 * c->th * (cval - c->c0) * u;
-  return f;
+  for (k = 0; k < 4; k++) ac[k].u = k < c->nac ? e[k] : 0.0;
+  ch[0].c = cval;
+}
+
+static double ac_f(const orc_cfg *c, const double *e, double cval, int m) {
+  sclet_acv ac[4];
+  sclet_chv ch[1];
+  load_cell(c, e, cval, ac, ch);
+  if (c->physics == 1) return formula234_AC_f(ac, ch, c->nac, c->nch, c->K, m);
+  return landau246_AC_f(ac, ch, c->nac, c->nch, c->K, m);
 }
 
 static double ch_f(const orc_cfg *c, const double *e, double cval) {
-  double s = 0.0;
-  int k;
-  for (k = 0; k < c->nac; k++) s += e[k] * e[k];
-  return c->A * (cval - c->c0) - c->th * s;
+  sclet_acv ac[4];
+  sclet_chv ch[1];
+  load_cell(c, e, cval, ac, ch);
+  if (c->physics == 1) return formula234_CH_f(ac, ch, c->nac, c->nch, c->K, 0);
+  return landau246_CH_f(ac, ch, c->nac, c->nch, c->K, 0);
+}
+
+static double f_bulk(const orc_cfg *c, const double *e, double cval) {
+  sclet_acv ac[4];
+  sclet_chv ch[1];
+  load_cell(c, e, cval, ac, ch);
+  if (c->physics == 1) return formula234_F_bulk(ac, ch, c->nac, c->nch, c->K);
+  return landau246_F_bulk(ac, ch, c->nac, c->nch, c->K);
+}
+
+int orc_physics_setup(orc_cfg *c) {
+  sclet_kl kl;
+  if (c->physics == 0) landau246_init_KL(c->K, &kl);
+  else if (c->physics == 1) formula234_init_KL(c->K, &kl);
+  else return -1;
+  c->LE = kl.LE;
+  c->KE = kl.KE;
+  c->LCI = kl.LCI;
+  c->KCI = kl.KCI;
+  return 0;
 }
 
 /* ---------------------------------------------------------------------- */
@@ -549,8 +587,6 @@ void orc_step(const orc_cfg *c, double *u, double *felas, double *fstate) {
 /* Diagnostics                                                             */
 /* ---------------------------------------------------------------------- */
 static double landau_energy(const orc_cfg *c, const double *e, double cv) {
-  int m, k;
-  double f = 0.0;
   if (c->energy_form == 0) {
     /* the reference's hard-coded polynomial, field.c:508 (four fields) */
     double s2 = e[0] * e[0] + e[1] * e[1] + e[2] * e[2] + e[3] * e[3];
@@ -558,17 +594,7 @@ static double landau_energy(const orc_cfg *c, const double *e, double cv) {
     return (2376.0 / 2372.0 / 2.0) * s2 - ((7128.0 + 12.0 * 2372.0) / 2372.0 / 3.0) * s3 +
            ((4752.0 + 12.0 * 2372.0) / 2372.0 / 4.0) * s2 * s2;
   }
-  for (m = 0; m < c->nac; m++) {
-    double u2 = e[m] * e[m];
-    f += c->a2 / 2.0 * u2 + c->a4 / 4.0 * u2 * u2 + c->a6 / 6.0 * u2 * u2 * u2;
-    for (k = m + 1; k < c->nac; k++) f += c->g * u2 * e[k] * e[k];
-  }
-  if (c->nch > 0) {
-    double s = 0.0;
-    for (m = 0; m < c->nac; m++) s += e[m] * e[m];
-    f += c->A / 2.0 * (cv - c->c0) * (cv - c->c0) - c->th * (cv - c->c0) * s;
-  }
-  return f;
+  return f_bulk(c, e, cv);
 }
 
 /* check_soln_new, field.c:407-678.  Per field: max, min, vol = sum(u + 1) h^3

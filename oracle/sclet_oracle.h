@@ -26,8 +26,12 @@ typedef struct {
   double kk[3];     /* per-axis weights of the implicit AC operator */
   double lam[4][3][3]; /* F2 tensors = diag(kk) - file tensor, per AC field */
   double elastic_scale;
-  /* physics plugin constants: a2 a4 a6 g th c0 A LE KE LCI KCI */
-  double a2, a4, a6, g, th, c0, A, LE, KE, LCI, KCI;
+  /* physics plugin (numbered as SCLET_PHYSICS_* of include/sclet_gb300.h)
+   * and its constants K (for the Landau plugin: a2 a4 a6 g th c0 A LE KE LCI
+   * KCI); LE, KE, LCI, KCI from the plugin's init_KL (orc_physics_setup) */
+  int physics;
+  double K[16];
+  double LE, KE, LCI, KCI;
   /* per-axis eigen data: V and V^-1 stored column-major (element (r, c) at
    * c*n + r) as the reference keeps MPX / MPXI; eigenvalues already / h^2. */
   const double *mp[3], *mpi[3], *dd[3];
@@ -75,6 +79,10 @@ void orc_step(const orc_cfg *c, double *u, double *felas, double *fstate);
 /* Diagnostics of check_soln_new (field.c:407-678): per field max, min, vol,
  * and the free energy.  out: (nac+nch)*4 doubles. */
 void orc_check_soln(const orc_cfg *c, const double *u, double *out);
+
+/* init_KL of the plugin c->physics (formula.c:9-19): fills LE, KE, LCI, KCI
+ * from K.  Returns 0, or -1 for an unknown plugin. */
+int orc_physics_setup(orc_cfg *c);
 
 /* Threads used by the oracle's parallel loops (OpenMP when built with it). */
 int orc_threads(void);

@@ -86,3 +86,25 @@ def test_closed_form_eigen_matches_case_files(sclet_lib, tmp_path):
     np.testing.assert_allclose(d, fd, rtol=0, atol=1e-14)
     np.testing.assert_allclose(v, fv, rtol=0, atol=1e-14)
     np.testing.assert_allclose(vi, fvi, rtol=0, atol=1e-14)
+
+
+def test_physics_plugin_selection(sclet_lib, tmp_path):
+    """physics_input.txt names the plugin; a plugin that cannot run the case
+    (the reference's formula.c has no concentration physics) or an unknown id
+    is refused before any device work, with a message instead of an exit."""
+    L = sclet_lib.lib()
+    c = case_defs.write("formula234", str(tmp_path))
+    p = sclet_lib.read_case(str(tmp_path), "formula234")
+    assert p.physics == sclet_lib.PHYSICS_FORMULA234
+    p.nch = 1
+    h = ctypes.c_void_p()
+    assert L.sclet_create(ctypes.byref(p), sclet_lib.FP64, 0, ctypes.byref(h)) == 4  # SCLET_ERR_UNSUPPORTED
+    assert b"concentration" in L.sclet_last_error(None)
+    p.nch = 0
+    p.physics = 7
+    assert L.sclet_create(ctypes.byref(p), sclet_lib.FP64, 0, ctypes.byref(h)) == 4
+    assert b"physics plugin" in L.sclet_last_error(None)
+    (tmp_path / "physics_input.txt").write_text("nosuchplugin\n")
+    p2 = sclet_lib.Params()
+    assert L.sclet_read_case(str(tmp_path).encode(), b"formula234", ctypes.byref(p2)) == 1  # SCLET_ERR_ARG
+    assert c.physics == 1

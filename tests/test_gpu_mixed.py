@@ -181,3 +181,13 @@ def test_mixed_conserves_ch_mass_like_fp64(sclet_lib):
         vols[prec] = s.check_soln(1)[case.nac, 2]
         s.close()
     assert abs(vols[sg.MIXED] - vols[sg.FP64]) <= 1e-10 * abs(vols[sg.FP64]), vols
+
+
+def test_mixed_matches_fp64_reference_formula(sclet_lib):
+    """The reference's own physics plugin (formula.c: LE = 1, KE = 42, the
+    2-3-4 polynomial) through both forms: 32^3, 4 order parameters,
+    elasticity, 100 steps."""
+    case = cases.Case(big_n=32, steps=100, seed=78, dt=0.002, physics=1, suffix="f234")
+    errs, eerr = _mixed_vs_fp64(sclet_lib, case, 100)
+    assert max(errs) <= 1e-5, errs
+    assert eerr <= 1e-6, eerr
