@@ -1,0 +1,339 @@
+// Kernels of the learned coarse-step corrector: a periodic 3x3x3 convolution
+// network on BF16 activations with FP32 accumulation.
+//
+// Activation layout: channels last, 32 BF16 channels per cell (64 bytes),
+// one haloed block of Np^3 cells per sample (Np = N + 2: the N^3 periodic
+// grid plus one periodic image layer per side), samples stacked in z:
+// cell(b, zh, yh, xh) = ((b Np + zh) Np + yh) Np + xh.
+//
+// conv_tc_kernel is an implicit GEMM on the 5th-generation tensor cores:
+//   D[cell][co] = sum_{tap, ci} A[cell + off(tap)][ci] * W[tap][co][ci]
+// with M = 128 cells, N = 32 output channels and K = 27 taps x 32 input
+// channels.  A tile is 128 consecutive "slots" of one haloed plane (slot =
+// yh Np + xh); for every tap the 128 input rows are again consecutive cells
+// (shifted by dz Np^2 + dy Np + dx), so each tap is one TMA box of 128 x 64 B,
+// whatever N is.  Slots in the x- or y-halo produce outputs that are dropped.
+// The weights (27 x 32 x 32 BF16, 54 KB) stay in shared memory.  Warp 0
+// issues TMA, warp 1 issues the MMAs (54 per tile: two K = 16 steps per tap)
+// into one of four 32-column TMEM accumulators, warps 2-5 drain them and run
+// the fused epilogue (bias, ReLU, residual, ReLU-mask, FP32 planar output).
+// The same kernel computes the data gradient of a convolution with the
+// weights flipped and transposed (the adjoint of a periodic convolution).
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+#include <stdint.h>
+
+#include <mutex>
+
+#include "sclet_internal.cuh"
+#include "sclet_tc.cuh"
+#include "sclet_tc_ptx.cuh"
+#include "sclet_conv.cuh"
+
+namespace sclet {
+namespace conv {
+
+using tc::fence_after;
+using tc::fence_before;
+using tc::mbar_arrive;
+using tc::mbar_expect_tx;
+using tc::mbar_init;
+using tc::mbar_wait;
+using tc::mma_bf16;
+using tc::mma_commit;
+using tc::smem_desc;
+using tc::smem_u32;
+using tc::tmem_ld32;
+
+constexpr int ROWS = 128;                  // cells per tile (MMA M)
+constexpr int STAGES = 8;                  // tap tiles in flight
+constexpr int ATILE = ROWS * CH * 2;       // 8 KB: 128 cells x 32 channels
+constexpr int WTILE = CH * CH * 2;         // 2 KB: one tap's 32 x 32 weights
+constexpr int NACC = 4;                    // TMEM accumulators of 32 columns
+constexpr int TMEM_COLS = NACC * CH;       // 128
+constexpr int THREADS = 192;
+constexpr int SMEM_BYTES = TAPS * WTILE + STAGES * ATILE + 1024;
+static_assert(SMEM_BYTES <= 227 * 1024, "shared memory per CTA");
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// tile -> (sample b, plane zh in 1..N, first slot s0 of the plane)
+struct Tile {
+  int b, zh, s0;
+};
+__device__ __forceinline__ Tile tile_of(int t, int N, int Np, int per_plane) {
+  Tile x;
+  const int j = t % per_plane;
+  const int bz = t / per_plane;
+  x.zh = 1 + bz % N;
+  x.b = bz / N;
+  x.s0 = Np + j * ROWS;
+  return x;
+}
+
+__device__ __forceinline__ float bf(uint32_t w, int hi) {
+  return __uint_as_float(hi ? (w & 0xffff0000u) : (w << 16));
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
+    conv_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmW, ConvArgs g) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ __align__(8) uint64_t full_bar[STAGES];
+  __shared__ __align__(8) uint64_t empty_bar[STAGES];
+  __shared__ __align__(8) uint64_t tfull_bar[NACC];
+  __shared__ __align__(8) uint64_t tempty_bar[NACC];
+  __shared__ __align__(8) uint64_t w_bar;
+  __shared__ __align__(8) uint64_t done_bar;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int failed;
+  __shared__ float s_bias[CH];
+
+  uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint8_t *wsm = base;                    // 27 tap tiles of weights
+  uint8_t *asm_ = base + TAPS * WTILE;    // STAGES input tiles
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int N = g.N, Np = N + 2;
+  const int per_plane = (N * Np + ROWS - 1) / ROWS;
+  const int total = g.batch * N * per_plane;
+  const long long plane = (long long)Np * Np;
+
+  if (threadIdx.x < CH) s_bias[threadIdx.x] = g.bias ? g.bias[threadIdx.x] : 0.0f;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; s++) {
+      mbar_init(&full_bar[s], 1);
+      mbar_init(&empty_bar[s], 1);
+    }
+    for (int b = 0; b < NACC; b++) {
+      mbar_init(&tfull_bar[b], 1);
+      mbar_init(&tempty_bar[b], 4);
+    }
+    mbar_init(&w_bar, 1);
+    mbar_init(&done_bar, 1);
+    failed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      mbar_expect_tx(&w_bar, TAPS * WTILE);
+      for (int t = 0; t < TAPS; t++) tma_load_2d(wsm + t * WTILE, &tmW, 0, t * CH, &w_bar);
+      int it = 0;
+      for (int tile = blockIdx.x; tile < total && !*(volatile int *)&failed; tile += gridDim.x) {
+        const Tile ti = tile_of(tile, N, Np, per_plane);
+        const long long pbase = ((long long)ti.b * Np + ti.zh) * plane + ti.s0;
+        for (int tap = 0; tap < TAPS; tap++, it++) {
+          const int s = it % STAGES;
+          if (it >= STAGES && !mbar_wait(&empty_bar[s], ((it / STAGES) & 1) ^ 1)) {
+            failed = 1;
+            break;
+          }
+          const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
+          const long long row = pbase + dz * plane + dy * Np + dx;
+          mbar_expect_tx(&full_bar[s], ATILE);
+          tma_load_2d(asm_ + s * ATILE, &tmA, 0, (int)row, &full_bar[s]);
+        }
+      }
+      if (*(volatile int *)&failed) {
+        for (int i = it - STAGES < 0 ? 0 : it - STAGES; i < it; i++) mbar_wait(&full_bar[i % STAGES], (i / STAGES) & 1);
+      }
+      mbar_wait(&w_bar, 0);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = tc::idesc_bf16(ROWS, CH);
+      bool ok = mbar_wait(&w_bar, 0);
+      if (!ok) failed = 1;
+      fence_after();
+      int it = 0, j = 0;
+      const uint32_t w0 = smem_u32(wsm), a0 = smem_u32(asm_);
+      for (int tile = blockIdx.x; ok && tile < total && !*(volatile int *)&failed; tile += gridDim.x, j++) {
+        const int b = j % NACC;
+        if (j >= NACC && !mbar_wait(&tempty_bar[b], ((j / NACC) & 1) ^ 1)) {
+          failed = 1;
+          break;
+        }
+        fence_after();
+        const uint32_t acc = tmem + (uint32_t)(b * CH);
+        for (int tap = 0; tap < TAPS; tap++, it++) {
+          const int s = it % STAGES;
+          if (!mbar_wait(&full_bar[s], (it / STAGES) & 1)) {
+            ok = false;
+            break;
+          }
+          fence_after();
+#pragma unroll
+          for (int ks = 0; ks < 2; ks++) {
+            const uint64_t da = smem_desc(a0 + s * ATILE + ks * 32);
+            const uint64_t dw = smem_desc(w0 + tap * WTILE + ks * 32);
+            mma_bf16(acc, da, dw, idesc, (tap == 0 && ks == 0) ? 0u : 1u);
+          }
+          mma_commit(&empty_bar[s]);
+        }
+        if (!ok) {
+          failed = 1;
+          break;
+        }
+        mma_commit(&tfull_bar[b]);
+      }
+      mma_commit(&done_bar);
+      if (!mbar_wait(&done_bar, 0)) failed = 1;
+    }
+  } else {
+    const int q = warp & 3;
+    const int row = q * 32 + lane;
+    int j = 0;
+    for (int tile = blockIdx.x; tile < total; tile += gridDim.x, j++) {
+      const int b = j % NACC;
+      int ok = 1;
+      if (lane == 0) ok = mbar_wait(&tfull_bar[b], (j / NACC) & 1) ? 1 : 0;
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) {
+        if (lane == 0) failed = 1;
+        break;
+      }
+      fence_after();
+      float acc[CH];
+      tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * CH), acc);
+      fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&tempty_bar[b]);
+      const Tile ti = tile_of(tile, N, Np, per_plane);
+      const int s = ti.s0 + row;
+      const int yh = s / Np, xh = s - yh * Np;
+      if (yh >= 1 && yh <= N && xh >= 1 && xh <= N) {
+        const long long cell = ((long long)ti.b * Np + ti.zh) * plane + s;
+        if (g.mode == CONV_OUT_F32) {
+          // FP32 planar output of the first `cout` channels (owned cells)
+          const long long n3 = (long long)N * N * N;
+          const long long own = ((long long)(ti.zh - 1) * N + (yh - 1)) * N + (xh - 1);
+          float *o = g.outf + (long long)ti.b * g.cout * n3 + own;
+#pragma unroll
+          for (int c = 0; c < CH; c++)
+            if (c < g.cout) o[c * n3] = (acc[c] + s_bias[c]) * g.scale;
+        } else {
+          float v[CH];
+          if (g.mode == CONV_RELU) {
+#pragma unroll
+            for (int c = 0; c < CH; c++) v[c] = fmaxf(acc[c] + s_bias[c], 0.0f);
+          } else if (g.mode == CONV_LINEAR) {
+#pragma unroll
+            for (int c = 0; c < CH; c++) v[c] = acc[c] + s_bias[c];
+          } else {
+            const uint4 *src = reinterpret_cast<const uint4 *>(g.aux + cell * CH);
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+              const uint4 w = src[k];
+              const uint32_t ww[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+              for (int h = 0; h < 8; h++) {
+                const int c = k * 8 + h;
+                const float a = bf(ww[h >> 1], h & 1);
+                v[c] = g.mode == CONV_RESIDUAL ? a + (acc[c] + s_bias[c]) : (a > 0.0f ? acc[c] : 0.0f);
+              }
+            }
+          }
+          uint4 *dst = reinterpret_cast<uint4 *>(g.out + cell * CH);
+#pragma unroll
+          for (int k = 0; k < 4; k++) {
+            uint32_t w[4];
+#pragma unroll
+            for (int h = 0; h < 4; h++) {
+              const __nv_bfloat162 p = __floats2bfloat162_rn(v[k * 8 + 2 * h], v[k * 8 + 2 * h + 1]);
+              w[h] = *reinterpret_cast<const uint32_t *>(&p);
+            }
+            dst[k] = make_uint4(w[0], w[1], w[2], w[3]);
+          }
+        }
+      }
+      if (__any_sync(0xffffffffu, *(volatile int *)&failed != 0)) break;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && failed) atomicExch(g.err, 1);
+  if (warp == 1) {
+    fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+  }
+}
+
+
+// 2-D BF16 tensor map with 64-byte swizzle: rows of 32 channels (64 B),
+// `rows` rows, boxes of 32 x box_rows.
+static cudaError_t make_map_rows(CUtensorMap *map, const void *ptr, long long rows, int box_rows) {
+  auto fn = encode_fn();
+  if (!fn) return cudaErrorNotSupported;
+  cuuint64_t dims[2] = {(cuuint64_t)CH, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)CH * 2};
+  cuuint32_t box[2] = {(cuuint32_t)CH, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(ptr), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+// per device: the shared-memory attribute and the resident CTA count
+static cudaError_t conv_setup(int *ctas) {
+  constexpr int MAXDEV = 64;
+  static std::mutex mu;
+  static int resident[MAXDEV] = {0};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= MAXDEV) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!resident[dev]) {
+    e = cudaFuncSetAttribute(conv_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0, sms = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, conv_tc_kernel, THREADS, SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    resident[dev] = per_sm * sms;
+  }
+  *ctas = resident[dev];
+  return cudaSuccess;
+}
+
+}  // namespace conv
+
+cudaError_t launch_conv(const __nv_bfloat16 *in, const __nv_bfloat16 *w, const ConvArgs &args, cudaStream_t s) {
+  int ctas = 0;
+  cudaError_t e = conv::conv_setup(&ctas);
+  if (e != cudaSuccess) return e;
+  const int N = args.N, Np = N + 2;
+  if (N < 2 || args.batch < 1) return cudaErrorInvalidValue;
+  const long long cells = (long long)args.batch * Np * Np * Np;
+  if (cells >= 0x7fffffffLL) return cudaErrorInvalidValue;
+  CUtensorMap ma, mw;
+  if ((e = conv::make_map_rows(&ma, in, cells, conv::ROWS)) != cudaSuccess) return e;
+  if ((e = conv::make_map_rows(&mw, w, (long long)TAPS * CH, CH)) != cudaSuccess) return e;
+  const long long per_plane = ((long long)N * Np + conv::ROWS - 1) / conv::ROWS;
+  const long long tiles = (long long)args.batch * N * per_plane;
+  const int grid = (int)(tiles < ctas ? tiles : ctas);
+  conv::conv_tc_kernel<<<grid, conv::THREADS, conv::SMEM_BYTES, s>>>(ma, mw, args);
+  launch_counter()++;
+  return cudaGetLastError();
+}
+
+}  // namespace sclet

@@ -1096,3 +1096,61 @@ int sclet_stage_times(const sclet_ctx *ctx, float *ms, int *launches, int nclass
 }
 
 }  // extern "C"
+
+// ---- owned cells as FP32 planar device blocks (the learned step) ----------
+namespace {
+template <typename T>
+__global__ void owned_export_kernel(const T *__restrict__ u, float *__restrict__ dst, int n, int nac, double shift) {
+  const int N = n - 4;
+  const long long n3 = (long long)N * N * N, b3 = (long long)n * n * n;
+  const int f = blockIdx.y;
+  const double sh = f >= nac ? shift : 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3; i += (long long)gridDim.x * blockDim.x) {
+    const int z = (int)(i / ((long long)N * N)), y = (int)((i / N) % N), x = (int)(i % N);
+    dst[f * n3 + i] = (float)((double)u[f * b3 + ((long long)(z + 2) * n + y + 2) * n + x + 2] + sh);
+  }
+}
+template <typename T>
+__global__ void owned_import_kernel(const float *__restrict__ src, T *__restrict__ u, int n, int nac, double shift) {
+  const int N = n - 4;
+  const long long n3 = (long long)N * N * N, b3 = (long long)n * n * n;
+  const int f = blockIdx.y;
+  const double sh = f >= nac ? shift : 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3; i += (long long)gridDim.x * blockDim.x) {
+    const int z = (int)(i / ((long long)N * N)), y = (int)((i / N) % N), x = (int)(i % N);
+    u[f * b3 + ((long long)(z + 2) * n + y + 2) * n + x + 2] = (T)((double)src[f * n3 + i] - sh);
+  }
+}
+}  // namespace
+
+namespace sclet {
+int ctx_export_owned(sclet_ctx *ctx, float *dst) {
+  const long long n3 = (long long)(ctx->n - 4) * (ctx->n - 4) * (ctx->n - 4);
+  const dim3 grid(grid_of(n3), ctx->F);
+  if (mixed(ctx))
+    owned_export_kernel<float><<<grid, 256, 0, ctx->stream>>>(fu_of(ctx), dst, ctx->n, ctx->nac, ctx->ph.cshift);
+  else
+    owned_export_kernel<double><<<grid, 256, 0, ctx->stream>>>(u_of(ctx), dst, ctx->n, ctx->nac, 0.0);
+  launch_counter()++;
+  CK(cudaGetLastError());
+  return SCLET_OK;
+}
+int ctx_import_owned(sclet_ctx *ctx, const float *src) {
+  const long long n3 = (long long)(ctx->n - 4) * (ctx->n - 4) * (ctx->n - 4);
+  const dim3 grid(grid_of(n3), ctx->F);
+  if (mixed(ctx))
+    owned_import_kernel<float><<<grid, 256, 0, ctx->stream>>>(src, fu_of(ctx), ctx->n, ctx->nac, ctx->ph.cshift);
+  else
+    owned_import_kernel<double><<<grid, 256, 0, ctx->stream>>>(src, u_of(ctx), ctx->n, ctx->nac, 0.0);
+  launch_counter()++;
+  CK(cudaGetLastError());
+  return SCLET_OK;
+}
+int ctx_device(const sclet_ctx *ctx) { return ctx->device; }
+double ctx_dt(const sclet_ctx *ctx) { return ctx->p.dt; }
+int ctx_nac(const sclet_ctx *ctx) { return ctx->nac; }
+int ctx_fail(sclet_ctx *ctx, int code, const char *msg) {
+  ctx->err = msg;
+  return code;
+}
+}  // namespace sclet

@@ -48,6 +48,16 @@ class Params(ctypes.Structure):
     ]
 
 
+class LearnedStats(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_longlong), ("fallbacks", ctypes.c_longlong),
+                ("energy_fail", ctypes.c_longlong), ("mass_fail", ctypes.c_longlong),
+                ("deviation_fail", ctypes.c_longlong), ("deviation_checks", ctypes.c_longlong),
+                ("max_deviation", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class Diag(ctypes.Structure):
     _fields_ = [("max", ctypes.c_double), ("min", ctypes.c_double), ("vol", ctypes.c_double),
                 ("energy", ctypes.c_double)]
@@ -115,6 +125,24 @@ SIGNATURES = {
     "sclet_launch_count": (ctypes.c_longlong, [ctypes.c_void_p]),
     "sclet_host_alloc": (ctypes.c_void_p, [ctypes.c_size_t]),
     "sclet_host_free": (None, [ctypes.c_void_p]),
+    "sclet_net_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_ulonglong, ctypes.c_float,
+                                         ctypes.POINTER(ctypes.c_void_p)]),
+    "sclet_net_destroy": (None, [ctypes.c_void_p]),
+    "sclet_net_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+    "sclet_net_stream": (ctypes.c_void_p, [ctypes.c_void_p]),
+    "sclet_net_param_count": (ctypes.c_longlong, []),
+    "sclet_net_get_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "sclet_net_set_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "sclet_net_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                          ctypes.c_void_p]),
+    "sclet_net_sync": (ctypes.c_int, [ctypes.c_void_p]),
+    "sclet_net_gradient": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]),
+    "sclet_net_train_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                             ctypes.c_void_p, ctypes.c_float, ctypes.POINTER(ctypes.c_double)]),
+    "sclet_learned_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                           ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                           ctypes.c_void_p]),
     "sclet_check_soln_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                                                 ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]),
 }

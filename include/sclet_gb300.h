@@ -308,6 +308,69 @@ void sclet_host_free(void *ptr);
 int sclet_check_soln_noalloc(const sclet_params *p, int precision, const void *fields, int energy_form,
                              double *out, void *stream, char *msg, size_t msg_len);
 
+/* ---- learned coarse-step corrector --------------------------------------- */
+/* No counterpart in the reference (its CNN, source_beta_to_alpha/src/CNN.cpp,
+ * is an unrelated detector).  A 3-D residual convolution network (3x3x3
+ * periodic kernels, SCLET_NET_WIDTH channels, SCLET_NET_BLOCKS residual
+ * blocks of two convolutions, ReLU; BF16 weights and activations, FP32
+ * accumulation, FP32 master weights and Adam) that maps (coarse ETD state,
+ * start state) to a correction of the coarse state toward the state after
+ * the fine steps it replaces.  Forward and backward run on the project's own
+ * kernels (tcgen05 implicit-GEMM convolutions).  Device arrays are FP32
+ * planar over the owned cells: in [batch][SCLET_NET_IN][N^3] (the coarse
+ * state's fields, then the start state's), out / target
+ * [batch][SCLET_NET_OUT][N^3]; N a periodic grid edge >= 4. */
+#define SCLET_NET_IN 8
+#define SCLET_NET_OUT 4
+#define SCLET_NET_WIDTH 32
+#define SCLET_NET_BLOCKS 4
+typedef struct sclet_net sclet_net;
+/* Deterministic initial parameters from seed; out_scale multiplies the
+ * output (the correction starts at zero: the output layer is zero). */
+int sclet_net_create(int device, unsigned long long seed, float out_scale, sclet_net **out);
+void sclet_net_destroy(sclet_net *net);
+const char *sclet_net_last_error(const sclet_net *net);
+void *sclet_net_stream(const sclet_net *net);
+/* FP32 parameters: weights [layer][27 taps][32 out][32 in] (taps
+ * t = 9 (dz+1) + 3 (dy+1) + (dx+1); unused input/output channels zero), then
+ * biases [layer][32], for 2 + 2 SCLET_NET_BLOCKS layers. */
+long long sclet_net_param_count(void);
+int sclet_net_get_params(sclet_net *net, float *host);
+int sclet_net_set_params(sclet_net *net, const float *host);
+/* out = net(in), queued on the network's stream (sclet_net_sync waits). */
+int sclet_net_forward(sclet_net *net, int N, int batch, const float *in, float *out);
+int sclet_net_sync(sclet_net *net);
+/* loss = mean of (net(in) - target)^2 over every value, and the gradient of
+ * every parameter (grad_host: sclet_net_param_count floats, may be NULL).
+ * Synchronous. */
+int sclet_net_gradient(sclet_net *net, int N, int batch, const float *in, const float *target, double *loss,
+                       float *grad_host);
+/* sclet_net_gradient followed by one Adam step (beta 0.9 / 0.999). */
+int sclet_net_train_step(sclet_net *net, int N, int batch, const float *in, const float *target, float lr,
+                         double *loss);
+
+/* Coarse steps judged by the plain-ETD checks.  coarse and fine are two
+ * contexts of the same run on one device, coarse.dt = ratio * fine.dt.  Each
+ * of nsteps steps: one ETD step of coarse from state u0 (the coarse
+ * context's state), corrected by the network when net is not NULL; then
+ *   energy:    the free energy (check_soln_new, the plugin's total form) must
+ *              not exceed that of u0 by more than energy_tol relative;
+ *   mass:      each conserved field's integral must equal u0's to 1e-10
+ *              relative (the correction of a conserved field has its mean
+ *              removed, so this holds up to the FP32 rounding of the state);
+ *   deviation: every check_every steps (0: never) the fine context runs ratio
+ *              steps from u0, and the per-field relative L2 distance of the
+ *              step's result from it must not exceed deviation_bound.
+ * A step that fails any check is replaced by ratio fine steps from u0
+ * (the fallback).  The coarse context holds the accepted state after each
+ * step.  Counters accumulate into st. */
+typedef struct sclet_learned_stats {
+  long long steps, fallbacks, energy_fail, mass_fail, deviation_fail, deviation_checks;
+  double max_deviation;
+} sclet_learned_stats;
+int sclet_learned_step(sclet_ctx *coarse, sclet_ctx *fine, sclet_net *net, int ratio, int nsteps, int check_every,
+                       double deviation_bound, double energy_tol, sclet_learned_stats *st);
+
 #ifdef __cplusplus
 }
 #endif
