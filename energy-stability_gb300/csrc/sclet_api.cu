@@ -208,11 +208,11 @@ int upload_eigen(sclet_ctx *ctx, const double *d, const double *v, const double 
     CK(cudaMemcpyAsync(ctx->Vi[ax], vi, sizeof(double) * n * n, cudaMemcpyHostToDevice, ctx->stream));
   }
   const sclet_params &p = ctx->p;
-  const double *lan = p.landau;
+  const Phys &ph = ctx->ph;  // LE, KE, LCI, KCI from the plugin's init_KL
   phi_kernel<<<grid_of(ctx->n3), 256, 0, ctx->stream>>>(ctx->phi1[0], ctx->phi2[0], n, 0, ctx->dd[0], ctx->dd[1],
-                                                        ctx->dd[2], p.kkx, p.kky, p.kkz, p.epn2, p.dt, lan[7], lan[8]);
+                                                        ctx->dd[2], p.kkx, p.kky, p.kkz, p.epn2, p.dt, ph.LE, ph.KE);
   phi_kernel<<<grid_of(ctx->n3), 256, 0, ctx->stream>>>(ctx->phi1[1], ctx->phi2[1], n, 1, ctx->dd[0], ctx->dd[1],
-                                                        ctx->dd[2], p.kkx, p.kky, p.kkz, p.epn2, p.dt, lan[9], lan[10]);
+                                                        ctx->dd[2], p.kkx, p.kky, p.kkz, p.epn2, p.dt, ph.LCI, ph.KCI);
   launch_counter() += 2;
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));
