@@ -51,13 +51,44 @@ __global__ void field_sum_kernel(const float *__restrict__ d, long long n3, int 
   if (threadIdx.x == 0) atomicAdd(&sums[f], red[0]);
 }
 
-// x += d, minus d's mean for the conserved fields (f >= nac)
-__global__ void correct_kernel(float *__restrict__ x, const float *__restrict__ d, long long n3, int nac,
-                               const double *__restrict__ sums) {
+// dx = xc - x0 (all fields), and the sum of its squares into *sq
+__global__ void increment_kernel(const float *__restrict__ xc, const float *__restrict__ x0, float *__restrict__ dx,
+                                 long long count, double *__restrict__ sq) {
+  __shared__ double red[256];
+  double s = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x) {
+    const float d = xc[i] - x0[i];
+    dx[i] = d;
+    s += (double)d * d;
+  }
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) atomicAdd(sq, red[0]);
+}
+
+// the increment's RMS s = sqrt(sq / count); dx /= s (dx stays 0 when s = 0)
+__global__ void normalise_kernel(float *__restrict__ dx, long long count, const double *__restrict__ sq) {
+  const double ms = *sq / (double)count;
+  const float inv = ms > 0.0 ? (float)(1.0 / sqrt(ms)) : 0.0f;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x)
+    dx[i] *= inv;
+}
+
+// x = xc + s d (s the increment's RMS), minus the mean of s d for the
+// conserved fields (f >= nac)
+__global__ void correct_kernel(float *__restrict__ x, const float *__restrict__ xc, const float *__restrict__ d,
+                               long long n3, int nac, const double *__restrict__ sums, const double *__restrict__ sq,
+                               long long count) {
   const int f = blockIdx.y;
-  const float mean = f >= nac ? (float)(sums[f] / (double)n3) : 0.0f;
+  const double ms = *sq / (double)count;
+  const float sc = (float)sqrt(ms);
+  const float mean = f >= nac ? (float)(sums[f] / (double)n3) * sc : 0.0f;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3; i += (long long)gridDim.x * blockDim.x)
-    x[f * n3 + i] += d[f * n3 + i] - mean;
+    x[f * n3 + i] = xc[f * n3 + i] + (sc * d[f * n3 + i] - mean);
 }
 
 // per field: sums[2 f] += (a - b)^2, sums[2 f + 1] += b^2
@@ -93,12 +124,14 @@ int blocks_for(long long n) {
 }
 
 struct Buffers {
-  float *xin = nullptr;    // [2F][N^3]: the step's result, then the start state u0
-  float *delta = nullptr;  // [F][N^3]
+  float *xin = nullptr;    // [2F][N^3]: the start state u0, then the normalised coarse increment
+  float *xc = nullptr;     // [F][N^3]: the coarse step's result, then the corrected state
+  float *delta = nullptr;  // [F][N^3]: the network's output
   float *xf = nullptr;     // [F][N^3]: fine steps from u0
-  double *sums = nullptr;  // 2F
+  double *sums = nullptr;  // 2F + 1
   ~Buffers() {
     cudaFree(xin);
+    cudaFree(xc);
     cudaFree(delta);
     cudaFree(xf);
     cudaFree(sums);
@@ -138,10 +171,12 @@ extern "C" int sclet_learned_step(sclet_ctx *coarse, sclet_ctx *fine, sclet_net 
   cudaStream_t s = (cudaStream_t)sclet_stream(coarse), sf = (cudaStream_t)sclet_stream(fine);
   Buffers b;
   LK(cudaMalloc(&b.xin, sizeof(float) * 2 * F * n3));
+  LK(cudaMalloc(&b.xc, sizeof(float) * F * n3));
   LK(cudaMalloc(&b.delta, sizeof(float) * F * n3));
   LK(cudaMalloc(&b.xf, sizeof(float) * F * n3));
-  LK(cudaMalloc(&b.sums, sizeof(double) * 2 * F));
-  float *x0 = b.xin + F * n3;
+  LK(cudaMalloc(&b.sums, sizeof(double) * (2 * F + 1)));
+  float *x0 = b.xin, *dx = b.xin + F * n3;
+  double *sq = b.sums + 2 * F;
   std::vector<sclet_diag> d0(F), d1(F);
   LR(sclet_check_soln(coarse, 1, d0.data()));
   const dim3 grid(blocks_for(n3), F);
@@ -149,17 +184,23 @@ extern "C" int sclet_learned_step(sclet_ctx *coarse, sclet_ctx *fine, sclet_net 
     LR(ctx_export_owned(coarse, x0));
     LR(sclet_step(coarse, 1));
     if (net) {
-      LR(ctx_export_owned(coarse, b.xin));
+      // input: u0 and the coarse increment scaled to unit RMS; the output is
+      // the correction in units of that RMS
+      LR(ctx_export_owned(coarse, b.xc));
+      LK(cudaMemsetAsync(b.sums, 0, sizeof(double) * (2 * F + 1), s));
+      increment_kernel<<<blocks_for(F * n3), 256, 0, s>>>(b.xc, x0, dx, F * n3, sq);
+      LK(cudaGetLastError());
+      normalise_kernel<<<blocks_for(F * n3), 256, 0, s>>>(dx, F * n3, sq);
+      LK(cudaGetLastError());
       int rc = net_forward_on(net, N, 1, b.xin, b.delta, s);
       if (rc != SCLET_OK) return ctx_fail(coarse, rc, net_error(net));
-      LK(cudaMemsetAsync(b.sums, 0, sizeof(double) * 2 * F, s));
       if (F > nac) {
         field_sum_kernel<<<dim3(blocks_for(n3), F - nac), 256, 0, s>>>(b.delta, n3, nac, b.sums);
         LK(cudaGetLastError());
       }
-      correct_kernel<<<grid, 256, 0, s>>>(b.xin, b.delta, n3, nac, b.sums);
+      correct_kernel<<<grid, 256, 0, s>>>(b.xc, b.xc, b.delta, n3, nac, b.sums, sq, F * n3);
       LK(cudaGetLastError());
-      LR(ctx_import_owned(coarse, b.xin));
+      LR(ctx_import_owned(coarse, b.xc));
     }
     LR(sclet_check_soln(coarse, 1, d1.data()));
     bool ok = true, have_fine = false;
@@ -179,10 +220,10 @@ extern "C" int sclet_learned_step(sclet_ctx *coarse, sclet_ctx *fine, sclet_net 
       LR(ctx_import_owned(fine, x0));
       LR(sclet_step(fine, ratio));
       LR(ctx_export_owned(fine, b.xf));
-      LR(ctx_export_owned(coarse, b.xin));
+      LR(ctx_export_owned(coarse, b.xc));
       LK(cudaStreamSynchronize(sf));
       LK(cudaMemsetAsync(b.sums, 0, sizeof(double) * 2 * F, s));
-      dist_kernel<<<grid, 256, 0, s>>>(b.xin, b.xf, n3, b.sums);
+      dist_kernel<<<grid, 256, 0, s>>>(b.xc, b.xf, n3, b.sums);
       LK(cudaGetLastError());
       std::vector<double> h(2 * F);
       LK(cudaMemcpyAsync(h.data(), b.sums, sizeof(double) * 2 * F, cudaMemcpyDeviceToHost, s));

@@ -4,12 +4,15 @@ solver itself, the training loop, and coarse stepping judged by the plain-ETD
 checks.  Device arrays are torch CUDA tensors (device memory only; every
 computation runs in libsclet_gb300.so).
 
-Training pair of a run at fine step t (ratio = coarse dt / fine dt):
-  input  = [coarse(u_t), u_t]            owned cells, FP32, 8 channels
-  target = fine^ratio(u_t) - coarse(u_t)  4 channels
+Training pair of a run at fine step t (ratio = coarse dt / fine dt), with
+D = coarse(u_t) - u_t the coarse increment and s its RMS over all cells and
+fields:
+  input  = [u_t, D / s]                      owned cells, FP32, 8 channels
+  target = (fine^ratio(u_t) - coarse(u_t)) / s   4 channels
 where coarse is one ETD step of the mixed-precision form with the coarse dt
 (the step the corrector is deployed on) and fine^ratio is ratio ETD steps of
-the fine dt.
+the fine dt.  The learned step (sclet_learned_step) forms the same input and
+applies s times the output.
 """
 from __future__ import annotations
 
@@ -153,8 +156,11 @@ def make_pairs(make_case, seeds: Iterable[int], sample_steps: Sequence[int], rat
             fine.step(ratio)
             t += ratio
             uf = fine.get_fields()
-            xs.append(np.concatenate([owned(uc), owned(u)]).astype(np.float32))
-            ys.append((owned(uf) - owned(uc)).astype(np.float32))
+            u0, c1, f1 = owned(u), owned(uc), owned(uf)
+            d = c1 - u0
+            s = float(np.sqrt(np.mean(d * d))) or 1.0
+            xs.append(np.concatenate([u0, d / s]).astype(np.float32))
+            ys.append(((f1 - c1) / s).astype(np.float32))
     fine.close()
     coarse.close()
     X = torch.from_numpy(np.stack(xs)).to(f"cuda:{device}")
@@ -185,7 +191,8 @@ def train(net: Net, X, Y, iters: int, batch: int, lr: float, seed: int = 0, lr_f
 
 def relative_errors(net: Optional[Net], X, Y) -> np.ndarray:
     """Per pair: ||coarse + correction - fine|| / ||fine - coarse|| over all
-    fields (net None: the coarse step alone, which gives 1)."""
+    fields (net None: the coarse step alone, which gives 1; the pair's scale
+    cancels)."""
     import torch
     out = []
     for i in range(X.shape[0]):

@@ -92,32 +92,36 @@ def forward(params, inp, out_scale, bf16_round=False):
     return y, cache
 
 
-def loss_and_grad(params, inp, target, out_scale):
+def loss_and_grad(params, inp, target, out_scale, bf16_round=False):
     """FP64 loss and the analytic gradient of every parameter (layout of
-    sclet_net_get_params)."""
-    y, c = forward(params, inp, out_scale)
+    sclet_net_get_params).  bf16_round=True also rounds, as the GPU stores
+    them, the activations of the forward pass and the activation gradients
+    of the backward pass (the output gradient, and each adjoint
+    convolution's result) to BF16; the sums stay exact."""
+    rnd = bf16 if bf16_round else (lambda a: a)
+    y, c = forward(params, inp, out_scale, bf16_round=bf16_round)
     W = c["W"]
     count = y.size
-    r = y - target
+    r = y.astype(np.float32).astype(np.float64) - target if bf16_round else y - target
     loss = float(np.sum(r * r) / count)
     gW = np.zeros_like(W)
     gb = np.zeros((LAYERS, CH))
     gy = np.zeros((y.shape[0], CH) + y.shape[2:])
-    gy[:, :NOUT] = 2.0 * r / count * out_scale
+    gy[:, :NOUT] = rnd(r * np.float32(2.0 / count * out_scale))
     L = LAYERS - 1
     h = c[f"h{BLOCKS}"]
     gW[L] = wgrad(h, gy)
     gb[L] = gy.sum(axis=(0, 2, 3, 4))
-    gh = conv_adjoint(gy, W[L])
+    gh = rnd(conv_adjoint(gy, W[L]))
     for k in range(BLOCKS - 1, -1, -1):
         l1, l2 = 2 * k + 1, 2 * k + 2
         rk, hk = c[f"r{k}"], c[f"h{k}"]
         gW[l2] = wgrad(rk, gh)
         gb[l2] = gh.sum(axis=(0, 2, 3, 4))
-        ga = conv_adjoint(gh, W[l2]) * (rk > 0)
+        ga = rnd(conv_adjoint(gh, W[l2]) * (rk > 0))
         gW[l1] = wgrad(hk, ga)
         gb[l1] = ga.sum(axis=(0, 2, 3, 4))
-        gh = gh + conv_adjoint(ga, W[l1])
+        gh = rnd(gh + conv_adjoint(ga, W[l1]))
     ga = gh * (c["h0"] > 0)
     gW[0] = wgrad(c["x"], ga)
     gb[0] = ga.sum(axis=(0, 2, 3, 4))

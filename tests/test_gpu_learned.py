@@ -26,12 +26,6 @@ def _torch():
     return pytest.importorskip("torch")
 
 
-def _bf16_params(p):
-    """The weights as the GPU rounds them (biases stay FP32)."""
-    W, b = co.unpack(p)
-    return co.pack(co.bf16(W), b)
-
-
 @pytest.mark.parametrize("N,B", [(16, 2), (12, 1), (40, 1)])
 def test_forward_matches_oracle(N, B, learned):
     torch = _torch()
@@ -61,14 +55,16 @@ def test_gradients_match_oracle(learned):
     net = learned.Net(seed=1, out_scale=scale)
     net.set_params(p)
     loss, g = net.gradient(torch.from_numpy(inp).cuda(), torch.from_numpy(tgt).cuda())
-    want_loss, want = co.loss_and_grad(_bf16_params(p.astype(np.float64)), inp.astype(np.float64),
-                                       tgt.astype(np.float64), scale)
-    assert loss == pytest.approx(want_loss, rel=2e-2)
+    # the oracle with the GPU's BF16 storage emulated (weights, activations,
+    # activation gradients), exact sums
+    want_loss, want = co.loss_and_grad(p.astype(np.float64), inp.astype(np.float64), tgt.astype(np.float64), scale,
+                                       bf16_round=True)
+    assert loss == pytest.approx(want_loss, rel=1e-3)
     gW, gb = co.unpack(g.astype(np.float64))
     wW, wb = co.unpack(want)
     for layer in range(co.LAYERS):
-        assert rel(gW[layer], wW[layer]) <= 3e-2, (layer, rel(gW[layer], wW[layer]))
-        assert rel(gb[layer], wb[layer]) <= 3e-2, (layer, rel(gb[layer], wb[layer]))
+        assert rel(gW[layer], wW[layer]) <= 1.5e-2, (layer, rel(gW[layer], wW[layer]))
+        assert rel(gb[layer], wb[layer]) <= 1.5e-2, (layer, rel(gb[layer], wb[layer]))
     net.close()
 
 
@@ -84,9 +80,8 @@ def test_training_gains_over_coarse_step(learned):
     samples = [0, 40, 120, 240, 400]
     X, Y = learned.make_pairs(_omega, range(12), samples, 8)
     Xh, Yh = learned.make_pairs(_omega, range(100, 103), samples, 8)
-    scale = float(torch.sqrt(torch.mean(Y * Y)))
-    net = learned.Net(seed=5, out_scale=scale)
-    losses = learned.train(net, X, Y, iters=400, batch=4, lr=2e-3)
+    net = learned.Net(seed=5, out_scale=1.0)
+    losses = learned.train(net, X, Y, iters=600, batch=4, lr=1e-3)
     assert np.mean(losses[-40:]) < 0.5 * np.mean(losses[:10]), (losses[:10], losses[-40:])
     err = learned.relative_errors(net, Xh, Yh)
     # 1.0 is the coarse step without the corrector
@@ -136,6 +131,10 @@ def test_deviation_bound_is_checked(learned, sclet_lib):
     st = learned.learned_steps(coarse, fine, None, 8, 4, check_every=2, deviation_bound=1e-12)
     assert st["deviation_checks"] == 2 and st["deviation_fail"] == 2 and st["fallbacks"] == 2, st
     assert st["max_deviation"] > 1e-6
+    for s in (fine, coarse):
+        s.close()
+    # fresh contexts: the elastic scratch carries state between steps
+    case, fine, coarse, u0 = _solvers(learned, sg, 6)
     plain = sg.Solver(learned.case_params(case, dt=0.08), sg.MIXED)
     plain.set_fields(u0)
     plain.step(3)

@@ -44,7 +44,10 @@ def test_tc_mode_product_accuracy(big_n, sclet_lib):
     s.close()
 
 
-def _mixed_vs_fp64(sg, case, steps):
+def _mixed_vs_fp64(sg, case, steps, every=1):
+    """Both forms from the same state for `steps` steps: per-field relative L2
+    over the owned cells at the end, and the energy-curve error max |dE| /
+    max |E| over the diagnostics taken every `every` steps."""
     p = params_for(sg, case)
     u0 = bench.block_fields(case)
     out = {}
@@ -52,15 +55,19 @@ def _mixed_vs_fp64(sg, case, steps):
         s = sg.Solver(p, prec)
         s.set_fields(u0)
         energies = []
-        for k in range(steps):
-            s.step(1)
+        done = 0
+        while done < steps:
+            k = min(every, steps - done)
+            s.step(k)
+            done += k
             energies.append(s.check_soln()[0, 3])
         out[prec] = (s.get_fields(), np.array(energies))
         s.sync()
         s.close()
     (u64, e64), (u32, e32) = out[sg.FP64], out[sg.MIXED]
-    errs = [rel(u32[f][2:-2, 2:-2, 2:-2], u64[f][2:-2, 2:-2, 2:-2]) for f in range(u64.shape[0])]
-    eerr = np.max(np.abs(e32 - e64) / np.abs(e64))
+    own = (slice(2, -2),) * 3
+    errs = [rel(u32[f][own], u64[f][own]) for f in range(u64.shape[0])]
+    eerr = float(np.max(np.abs(e32 - e64)) / np.max(np.abs(e64)))
     return errs, eerr
 
 
@@ -72,10 +79,21 @@ def test_mixed_matches_fp64_beta_omega_64(sclet_lib):
     assert eerr <= 1e-6, eerr
 
 
-def test_mixed_matches_fp64_beta_alpha_192(sclet_lib):
-    """The 192^3 coupled CH + AC workload of the benchmark, 50 steps."""
+def test_mixed_matches_fp64_beta_alpha_192_2000_steps(sclet_lib):
+    """The 192^3 coupled CH + AC workload (one conserved concentration, four
+    order parameters, c-eta coupling, anisotropic, elastic, dt 0.005) for its
+    2000 steps: per field <= 1e-5, energy curve within 1e-6."""
     case = bench.workload(192, seed=9)
-    errs, eerr = _mixed_vs_fp64(sclet_lib, case, 50)
+    errs, eerr = _mixed_vs_fp64(sclet_lib, case, 2000, every=100)
+    assert max(errs) <= 1e-5, errs
+    assert eerr <= 1e-6, eerr
+
+
+def test_mixed_matches_fp64_beta_alpha_512(sclet_lib):
+    """The 512^3 workload of the benchmark (block 516^3, 5 fields, about 30 GB
+    for the FP64 form), 20 steps."""
+    case = bench.workload(512, seed=9)
+    errs, eerr = _mixed_vs_fp64(sclet_lib, case, 20, every=5)
     assert max(errs) <= 1e-5, errs
     assert eerr <= 1e-6, eerr
 

@@ -104,11 +104,37 @@ def test_all_options_match_oracle(tmp_path, sclet_lib, oracle_lib):
     np.testing.assert_allclose(eg, eo, rtol=1e-10, atol=1e-13)
 
 
-def test_beta_omega_64_cubed_1000_steps(tmp_path, sclet_lib, oracle_lib):
-    """The beta->omega plain-ETD workload: 64^3, 4 order parameters, Landau
-    2-4-6, cubic elasticity, dt = 0.01, 1000 steps: per-field relative L2
-    <= 1e-10 against the oracle."""
-    case = cases.Case(big_n=64, steps=1000, seed=2024, suffix="omega64")
-    errs, eg, eo = _oracle_vs_gpu(tmp_path, sclet_lib, oracle_lib, case, 1000)
+def test_beta_omega_64_cubed_1000_steps(tmp_path, sclet_lib):
+    """The beta->omega plain-ETD workload (64^3, 4 order parameters, Landau
+    2-4-6, cubic elasticity, dt = 0.01) for 1000 steps against the
+    reference's own code (fixture tests/golden/beta_omega_64_1000.npz, made by
+    tests/golden/make_long_golden.py from oracle/_ref): per-field relative L2
+    <= 1e-10 after 1000 steps, the check_soln_new record of every pass within
+    1e-10, and the free energy of the run (the plugin's, energy form 1 with
+    the dynamics' gradient tensors diag(kk)) non-increasing from pass to
+    pass.  The reference's own energy column is its hard-coded 2-3-4
+    polynomial without gradient terms here, which this physics does not
+    decrease, so it is compared but not tested for monotonicity."""
+    import make_long_golden
+    case = make_long_golden.long_case()
+    g = np.load(os.path.join(case_defs.HERE, "beta_omega_64_1000.npz"))
+    d = str(tmp_path)
+    cases.write_case(case, d)
+    s = solver_for(sclet_lib, d, case.suffix)
+    zero, dyn = np.zeros((4, 3, 3)), np.array([np.diag(case.kk)] * 4)
+    ours, free = [], []
+    for k in range(case.steps):
+        s.set_energy_tensors(zero)  # the reference's energy without ANISOTROPIC
+        ours.append(s.check_soln(form=0))
+        s.set_energy_tensors(dyn)
+        free.append(s.check_soln(form=1)[0, 3])
+        s.step(1)
+    ours = np.stack(ours, axis=1)  # [field][pass][max, min, vol, energy]
+    u = s.get_fields()
+    s.close()
+    own = (slice(2, -2),) * 3
+    errs = [rel(u[f][own], g["final"][f]) for f in range(case.nac)]
     assert max(errs) <= 1e-10, errs
-    np.testing.assert_allclose(eg[:, 3], eo[:, 3], rtol=1e-10)
+    np.testing.assert_allclose(ours, g["diag"], rtol=1e-10, atol=1e-13)
+    free = np.array(free)
+    assert np.all(np.diff(free) <= 1e-12 * np.abs(free[:-1])), "free energy increased"
