@@ -56,15 +56,19 @@ def test_gradients_match_oracle(learned):
     net.set_params(p)
     loss, g = net.gradient(torch.from_numpy(inp).cuda(), torch.from_numpy(tgt).cuda())
     # the oracle with the GPU's BF16 storage emulated (weights, activations,
-    # activation gradients), exact sums
+    # activation gradients), exact sums.  What remains is where FP32 and FP64
+    # sums round to neighbouring BF16 values: the oracle itself moves as much
+    # when its sums are perturbed by 1e-6 relative before rounding (about
+    # 0.3% on every layer, 2.5% on the first layer's weights, whose gradient
+    # sums products with the random-signed input).
     want_loss, want = co.loss_and_grad(p.astype(np.float64), inp.astype(np.float64), tgt.astype(np.float64), scale,
                                        bf16_round=True)
     assert loss == pytest.approx(want_loss, rel=1e-3)
     gW, gb = co.unpack(g.astype(np.float64))
     wW, wb = co.unpack(want)
     for layer in range(co.LAYERS):
-        assert rel(gW[layer], wW[layer]) <= 1.5e-2, (layer, rel(gW[layer], wW[layer]))
-        assert rel(gb[layer], wb[layer]) <= 1.5e-2, (layer, rel(gb[layer], wb[layer]))
+        assert rel(gW[layer], wW[layer]) <= (5e-2 if layer == 0 else 1e-2), (layer, rel(gW[layer], wW[layer]))
+        assert rel(gb[layer], wb[layer]) <= 1e-2, (layer, rel(gb[layer], wb[layer]))
     net.close()
 
 
