@@ -51,41 +51,55 @@ __global__ void field_sum_kernel(const float *__restrict__ d, long long n3, int 
   if (threadIdx.x == 0) atomicAdd(&sums[f], red[0]);
 }
 
-// dx = xc - x0 (all fields), and the sum of its squares into *sq
+// dx = xc - x0 (all fields); sums of squares of dx into sq[0] and of x0 into sq[1]
 __global__ void increment_kernel(const float *__restrict__ xc, const float *__restrict__ x0, float *__restrict__ dx,
                                  long long count, double *__restrict__ sq) {
-  __shared__ double red[256];
-  double s = 0.0;
+  __shared__ double red[2][256];
+  double s = 0.0, u = 0.0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x) {
-    const float d = xc[i] - x0[i];
+    const float a = x0[i], d = xc[i] - a;
     dx[i] = d;
     s += (double)d * d;
+    u += (double)a * a;
   }
-  red[threadIdx.x] = s;
+  red[0][threadIdx.x] = s;
+  red[1][threadIdx.x] = u;
   __syncthreads();
   for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    if (threadIdx.x < w) {
+      red[0][threadIdx.x] += red[0][threadIdx.x + w];
+      red[1][threadIdx.x] += red[1][threadIdx.x + w];
+    }
     __syncthreads();
   }
-  if (threadIdx.x == 0) atomicAdd(sq, red[0]);
+  if (threadIdx.x == 0) {
+    atomicAdd(&sq[0], red[0][0]);
+    atomicAdd(&sq[1], red[1][0]);
+  }
 }
 
-// the increment's RMS s = sqrt(sq / count); dx /= s (dx stays 0 when s = 0)
+// the pair's scale: the RMS of the coarse increment plus SCLET_NET_FLOOR
+// times the RMS of the start state (the floor keeps the scale away from zero
+// where the state has stopped moving)
+__device__ __forceinline__ double pair_scale(const double *sq, long long count) {
+  return sqrt(sq[0] / (double)count) + SCLET_NET_FLOOR * sqrt(sq[1] / (double)count);
+}
+
+// dx /= s (dx stays 0 when s = 0)
 __global__ void normalise_kernel(float *__restrict__ dx, long long count, const double *__restrict__ sq) {
-  const double ms = *sq / (double)count;
-  const float inv = ms > 0.0 ? (float)(1.0 / sqrt(ms)) : 0.0f;
+  const double sc = pair_scale(sq, count);
+  const float inv = sc > 0.0 ? (float)(1.0 / sc) : 0.0f;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x)
     dx[i] *= inv;
 }
 
-// x = xc + s d (s the increment's RMS), minus the mean of s d for the
-// conserved fields (f >= nac)
+// x = xc + s d (s the pair's scale), minus the mean of s d for the conserved
+// fields (f >= nac)
 __global__ void correct_kernel(float *__restrict__ x, const float *__restrict__ xc, const float *__restrict__ d,
                                long long n3, int nac, const double *__restrict__ sums, const double *__restrict__ sq,
                                long long count) {
   const int f = blockIdx.y;
-  const double ms = *sq / (double)count;
-  const float sc = (float)sqrt(ms);
+  const float sc = (float)pair_scale(sq, count);
   const float mean = f >= nac ? (float)(sums[f] / (double)n3) * sc : 0.0f;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3; i += (long long)gridDim.x * blockDim.x)
     x[f * n3 + i] = xc[f * n3 + i] + (sc * d[f * n3 + i] - mean);
@@ -128,7 +142,7 @@ struct Buffers {
   float *xc = nullptr;     // [F][N^3]: the coarse step's result, then the corrected state
   float *delta = nullptr;  // [F][N^3]: the network's output
   float *xf = nullptr;     // [F][N^3]: fine steps from u0
-  double *sums = nullptr;  // 2F + 1
+  double *sums = nullptr;  // 2F + 2
   ~Buffers() {
     cudaFree(xin);
     cudaFree(xc);
@@ -174,7 +188,7 @@ extern "C" int sclet_learned_step(sclet_ctx *coarse, sclet_ctx *fine, sclet_net 
   LK(cudaMalloc(&b.xc, sizeof(float) * F * n3));
   LK(cudaMalloc(&b.delta, sizeof(float) * F * n3));
   LK(cudaMalloc(&b.xf, sizeof(float) * F * n3));
-  LK(cudaMalloc(&b.sums, sizeof(double) * (2 * F + 1)));
+  LK(cudaMalloc(&b.sums, sizeof(double) * (2 * F + 2)));
   float *x0 = b.xin, *dx = b.xin + F * n3;
   double *sq = b.sums + 2 * F;
   std::vector<sclet_diag> d0(F), d1(F);
@@ -187,7 +201,7 @@ extern "C" int sclet_learned_step(sclet_ctx *coarse, sclet_ctx *fine, sclet_net 
       // input: u0 and the coarse increment scaled to unit RMS; the output is
       // the correction in units of that RMS
       LR(ctx_export_owned(coarse, b.xc));
-      LK(cudaMemsetAsync(b.sums, 0, sizeof(double) * (2 * F + 1), s));
+      LK(cudaMemsetAsync(b.sums, 0, sizeof(double) * (2 * F + 2), s));
       increment_kernel<<<blocks_for(F * n3), 256, 0, s>>>(b.xc, x0, dx, F * n3, sq);
       LK(cudaGetLastError());
       normalise_kernel<<<blocks_for(F * n3), 256, 0, s>>>(dx, F * n3, sq);

@@ -5,8 +5,9 @@ checks.  Device arrays are torch CUDA tensors (device memory only; every
 computation runs in libsclet_gb300.so).
 
 Training pair of a run at fine step t (ratio = coarse dt / fine dt), with
-D = coarse(u_t) - u_t the coarse increment and s its RMS over all cells and
-fields:
+D = coarse(u_t) - u_t the coarse increment and the scale
+s = RMS(D) + FLOOR RMS(u_t) (RMS over all cells and fields; the floor keeps s
+away from zero where the state has stopped moving):
   input  = [u_t, D / s]                      owned cells, FP32, 8 channels
   target = (fine^ratio(u_t) - coarse(u_t)) / s   4 channels
 where coarse is one ETD step of the mixed-precision form with the coarse dt
@@ -30,6 +31,15 @@ if HERE not in sys.path:
 import sclet_gb300 as sg  # noqa: E402
 
 NET_IN, NET_OUT = 8, 4
+FLOOR = 1e-3  # SCLET_NET_FLOOR
+
+
+def pair(u0: np.ndarray, c1: np.ndarray, f1: np.ndarray):
+    """(input, target, scale) of one training pair from the start state, the
+    coarse step's result and the fine steps' result (owned cells)."""
+    d = c1 - u0
+    s = float(np.sqrt(np.mean(d * d)) + FLOOR * np.sqrt(np.mean(u0 * u0))) or 1.0
+    return np.concatenate([u0, d / s]).astype(np.float32), ((f1 - c1) / s).astype(np.float32), s
 
 
 def _ptr(t) -> ctypes.c_void_p:
@@ -156,11 +166,9 @@ def make_pairs(make_case, seeds: Iterable[int], sample_steps: Sequence[int], rat
             fine.step(ratio)
             t += ratio
             uf = fine.get_fields()
-            u0, c1, f1 = owned(u), owned(uc), owned(uf)
-            d = c1 - u0
-            s = float(np.sqrt(np.mean(d * d))) or 1.0
-            xs.append(np.concatenate([u0, d / s]).astype(np.float32))
-            ys.append(((f1 - c1) / s).astype(np.float32))
+            x, y, _ = pair(owned(u), owned(uc), owned(uf))
+            xs.append(x)
+            ys.append(y)
     fine.close()
     coarse.close()
     X = torch.from_numpy(np.stack(xs)).to(f"cuda:{device}")
@@ -204,6 +212,25 @@ def relative_errors(net: Optional[Net], X, Y) -> np.ndarray:
         net.forward(X[i:i + 1].contiguous(), pred)
         out.append(float(torch.linalg.vector_norm(pred - y) / torch.linalg.vector_norm(y)))
     return np.array(out)
+
+
+def aggregate_error(net: Optional[Net], X, Y, S) -> float:
+    """Over all pairs, in the fields' own units (each pair's error times its
+    scale S[i]): sqrt(sum |s (correction - y)|^2 / sum |s y|^2), i.e. the
+    error left by the corrected coarse step relative to that of the coarse
+    step alone (1 without a corrector)."""
+    import torch
+    num = den = 0.0
+    for i in range(X.shape[0]):
+        y = Y[i:i + 1]
+        e = y if net is None else None
+        if net is not None:
+            pred = torch.empty_like(y)
+            net.forward(X[i:i + 1].contiguous(), pred)
+            e = pred - y
+        num += float(S[i]) ** 2 * float(torch.sum(e * e))
+        den += float(S[i]) ** 2 * float(torch.sum(y * y))
+    return (num / den) ** 0.5 if den > 0 else 0.0
 
 
 def learned_steps(coarse: "sg.Solver", fine: "sg.Solver", net: Optional[Net], ratio: int, nsteps: int,

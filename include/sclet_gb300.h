@@ -320,8 +320,10 @@ int sclet_check_soln_noalloc(const sclet_params *p, int precision, const void *f
  * planar over the owned cells: in [batch][SCLET_NET_IN][N^3], out / target
  * [batch][SCLET_NET_OUT][N^3]; N a periodic grid edge >= 4.  As the learned
  * step uses it, in holds the start state u0 and the coarse increment
- * (coarse(u0) - u0) divided by its RMS s, and s out is the correction of the
- * coarse state. */
+ * D = coarse(u0) - u0 divided by the scale s = RMS(D) + SCLET_NET_FLOOR RMS(u0)
+ * (RMS over every cell and field), and s out is the correction of the coarse
+ * state. */
+#define SCLET_NET_FLOOR 1e-3
 #define SCLET_NET_IN 8
 #define SCLET_NET_OUT 4
 #define SCLET_NET_WIDTH 32
@@ -355,7 +357,7 @@ int sclet_net_train_step(sclet_net *net, int N, int batch, const float *in, cons
  * contexts of the same run on one device, coarse.dt = ratio * fine.dt.  Each
  * of nsteps steps: one ETD step of coarse from state u0 (the coarse
  * context's state), corrected by the network when net is not NULL (input u0
- * and the increment over its RMS s, correction s times the output); then
+ * and the increment over the scale s, correction s times the output); then
  *   energy:    the free energy (check_soln_new, the plugin's total form) must
  *              not exceed that of u0 by more than energy_tol relative;
  *   mass:      each conserved field's integral must equal u0's to 1e-10
