@@ -67,6 +67,34 @@ def workload(big_n: int, seed: int) -> cases.Case:
         eta_range=(-0.01, 0.01), c_range=(0.48, 0.52), seed=seed, suffix="bench")
 
 
+ENSEMBLE_EDGES = (32, 48, 64, 80, 96)
+
+
+def ensemble_case(edge: int, seed: int, a2: float) -> cases.Case:
+    """One run of the batched beta->omega ensemble: four order parameters
+    U(-0.01, 0.01) from its seed, Landau 2-4-6 with its own a2, cubic
+    elasticity, dt 0.01."""
+    landau = list(cases.Case().landau)
+    landau[0] = a2
+    return cases.Case(big_n=edge, nac=4, nch=0, dt=0.01, steps=500, epn2=0.5, elastic=1, seed=seed,
+                      landau=tuple(landau), suffix="ens")
+
+
+def ensemble_runs(count: int = 256, seed: int = 2026):
+    """The ensemble's runs: (edge, seed, a2) with edges drawn from
+    ENSEMBLE_EDGES and a2 ~ U(-1.2, -0.8), seeded."""
+    rng = np.random.default_rng(seed)
+    edges = rng.choice(ENSEMBLE_EDGES, size=count)
+    a2 = rng.uniform(-1.2, -0.8, size=count)
+    return [(int(e), 10_000 + i, float(a)) for i, (e, a) in enumerate(zip(edges, a2))]
+
+
+def case_params(sg, case):
+    with tempfile.TemporaryDirectory() as td:
+        cases.write_case(case, td, eigen=False, fields=False)
+        return sg.read_case(td, case.suffix)
+
+
 def workload_name(big_n: int) -> str:
     return (f"beta-alpha coupled CH + 4 AC, {big_n}^3 periodic (block {big_n + 4}^3), Landau 2-4-6, "
             f"anisotropic, cubic elasticity, ETD1, dt 0.005")
@@ -317,6 +345,60 @@ def fp64_stage_roofline(case, stage_ms_per_step):
     return out
 
 
+def ensemble_bench(sg, local, steps: int, loop_steps: int = 5, count: int = 256):
+    """The batched ensemble: `count` runs (edges drawn from 32..96, own seeds
+    and a2) as one context per edge holding its runs side by side, tuned by
+    the autotuner, stepped by one captured graph over all edges; against the
+    single-run path looped over the runs (one context per run, ordinary
+    steps).  Device time (CUDA events) of `steps` ensemble steps and of
+    `loop_steps` steps of every single run; cell-updates/s over all runs."""
+    runs = ensemble_runs(count)
+    groups = {}
+    for edge, seed, a2 in runs:
+        groups.setdefault(edge, []).append((seed, a2))
+    solvers, tuned = [], {}
+    for edge in sorted(groups):
+        members = groups[edge]
+        p = case_params(sg, ensemble_case(edge, members[0][0], members[0][1]))
+        u0 = np.concatenate([block_fields(ensemble_case(edge, sd, a)) for sd, a in members])
+        s = sg.Solver(p, sg.MIXED, device=local, runs=len(members), krun=np.array([a for _, a in members]))
+        s.set_fields(u0)
+        s.step(1)
+        tuned[edge] = s.tune(2)
+        solvers.append(s)
+    cells = sum(e ** 3 for e, _, _ in runs)
+    ens = sg.Ensemble(solvers)
+    ens.step(3)
+    ens.sync()
+    ms = ens.time_steps(steps)
+    diag_ok = all(np.isfinite(s.check_soln(1)).all() for s in solvers)
+    ens.close()
+    for s in solvers:
+        s.close()
+    # the single-run path, looped
+    loop_ms = 0.0
+    for edge, seed, a2 in runs:
+        case = ensemble_case(edge, seed, a2)
+        s = sg.Solver(case_params(sg, case), sg.MIXED, device=local)
+        s.set_fields(block_fields(case))
+        s.step(2)
+        loop_ms += s.time_steps(loop_steps)
+        s.close()
+    batched = cells * steps / (ms / 1000.0)
+    looped = cells * loop_steps / (loop_ms / 1000.0)
+    return {
+        "workload": f"{count} beta-omega runs, edges {list(ENSEMBLE_EDGES)} (seeded), own seed and a2 U(-1.2,-0.8), "
+                    "4 order parameters, elastic, dt 0.01, FP32 fields / FP64 energy",
+        "runs_per_edge": {str(e): len(groups[e]) for e in sorted(groups)},
+        "cells_per_step": cells, "steps": steps, "ms_per_step": ms / steps,
+        "value": batched, "unit": UNIT,
+        "looped_single_run": {"value": looped, "steps_per_run": loop_steps, "ms_per_step_all_runs": loop_ms / loop_steps},
+        "speedup_vs_looped": batched / looped,
+        "tuned": {str(e): {"rhs_zplanes": z, "tc_ctas": c} for e, (z, c) in tuned.items()},
+        "diagnostics_finite": bool(diag_ok),
+    }
+
+
 def accuracy_check(sg, params, u0, steps, every, local):
     """Mixed against FP64 from the same state: at every `every` steps up to
     `steps`, relative L2 per field over the owned cells, the energy (pointwise
@@ -427,6 +509,9 @@ def run_gpu(args, world, rank, local):
         fp64 = {"value": cells / (ms64 / 1000.0), "ms_per_step": ms64 / args.steps,
                 "speedup_of_mixed": ms64 / ms_max, "stage_ms_per_step": st64,
                 "stage_hbm": fp64_stage_roofline(case, st64)}
+    ensemble = None
+    if precision == sg.MIXED and rank == 0 and args.ensemble_steps > 0:
+        ensemble = ensemble_bench(sg, local, args.ensemble_steps)
     accuracy = None
     if precision == sg.MIXED and rank == 0:
         acc_steps = args.accuracy_steps if args.accuracy_steps is not None else (10 if args.size >= 384 else 100)
@@ -460,7 +545,7 @@ def run_gpu(args, world, rank, local):
         "config": config_of(args.size, world), "precision": args.precision,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": bytes_step, "d2h_bytes_per_step": bytes_step},
         "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
-        "fp64": fp64, "accuracy_vs_fp64": accuracy,
+        "fp64": fp64, "accuracy_vs_fp64": accuracy, "ensemble": ensemble,
     }
     print(json.dumps(line), flush=True)
 
@@ -480,6 +565,8 @@ def main():
                     help="steps of the mixed-vs-FP64 check from the same state (0: skip; default 10 at 512^3, "
                          "100 below)")
     ap.add_argument("--accuracy-every", type=int, default=0, help="checkpoint interval of that check (0: end only)")
+    ap.add_argument("--ensemble-steps", type=int, default=500,
+                    help="timed steps of the batched 256-run ensemble beside the headline (0: skip)")
     args = ap.parse_args()
     if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
         # one process per GPU: start the replicas under torchrun

@@ -355,6 +355,10 @@ __global__ void __launch_bounds__(256, 2) energy_partial_f32(Phys ph, EConst ec,
   float Kt[16];
 #pragma unroll
   for (int k = 0; k < 16; k++) Kt[k] = ec.K[k];
+  // blockIdx.y = run: its fields, its plugin constant 0, its partial records
+  if (ph.krun) Kt[0] = (float)ph.krun[blockIdx.y];
+  u += (long long)blockIdx.y * F * n3;
+  part += (long long)blockIdx.y * gridDim.x * rec_len(F);
   const float p2 = ec.p2, p3 = ec.p3, p4 = ec.p4;
   const Pair kdp = ec.kdp, kcp = ec.kcp;
   float mx[F], mn[F];
@@ -512,6 +516,9 @@ __global__ void __launch_bounds__(256, 2) energy_partial_f32(Phys ph, EConst ec,
 __global__ void energy_final_kernel(Phys ph, int form, const double *__restrict__ part, int npart,
                                     double *__restrict__ out) {
   const int F = ph.F, L = rec_len(F);
+  // blockIdx.x = run
+  part += (long long)blockIdx.x * npart * L;
+  out += (long long)blockIdx.x * 4 * F;
   const double h3 = ph.h[0] * ph.h[1] * ph.h[2];
   __shared__ double res[4 * MAXF + 4];
   const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -557,7 +564,8 @@ int check_soln_partials(int n) {
 template <typename PL, int NAC, int NCH>
 static void launch_f32(const Phys &ph, const float *u, const double *elam, int form, double *partials, int npart,
                        cudaStream_t s) {
-  energy_partial_f32<PL, NAC, NCH><<<npart, dim3(32, 8), 0, s>>>(ph, econst<PL>(ph), u, elam, form, partials);
+  energy_partial_f32<PL, NAC, NCH><<<dim3(npart, ph.runs > 1 ? ph.runs : 1), dim3(32, 8), 0, s>>>(
+      ph, econst<PL>(ph), u, elam, form, partials);
 }
 
 template <typename PL, typename T>
@@ -586,12 +594,13 @@ template <typename T>
 cudaError_t launch_check_soln(const Phys &ph, const T *u, const double *elam, int form, double *partials, int npart,
                               double *out, cudaStream_t s) {
   if (ph.F < 1 || ph.F > MAXF || ph.nac > 4 || ph.nch > 1) return cudaErrorInvalidValue;
+  if (ph.runs > 1 && sizeof(T) != 4) return cudaErrorInvalidValue;  // several runs: FP32 states
   cudaError_t e = with_physics(ph.physics, [&](auto *tag) {
     using PL = std::remove_pointer_t<decltype(tag)>;
     return check_soln_pl<PL, T>(ph, u, elam, form, partials, npart, s);
   });
   if (e != cudaSuccess) return e;
-  energy_final_kernel<<<1, 32 * (3 * MAXF + 2), 0, s>>>(ph, form, partials, npart, out);
+  energy_final_kernel<<<ph.runs > 1 ? ph.runs : 1, 32 * (3 * MAXF + 2), 0, s>>>(ph, form, partials, npart, out);
   launch_counter() += 2;
   return cudaGetLastError();
 }

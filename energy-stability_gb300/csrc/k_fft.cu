@@ -340,6 +340,10 @@ struct LineIO {
   int n, nac;
   long long n3;
   float scale;     // 1 / N^3
+  // runs side by side: run r's grids at r N^3 of data0 / data1, its order
+  // parameters at u + r ustride, its force at felas + r fstride
+  int runs;
+  long long ustride, fstride;
 };
 
 // L lines per CTA.  axis 0: lines along x, lane order over t (pass A) and k1
@@ -351,9 +355,14 @@ __global__ void __launch_bounds__(L *(N1 > N2 ? N1 : N2))
   constexpr int N = N1 * N2;
   constexpr int RS = AXIS == 0 ? N2 + 1 : N2;  // row stride of a line's table (padded on axis 0)
   extern __shared__ float2 tab[];
-  float2 *data = blockIdx.y == 0 ? data0 : data1;
-  const int tid = threadIdx.x;
+  // blockIdx.y = run x (grid pair 0 or 1)
+  const int per = data1 != data0 ? 2 : 1;
+  const int run = blockIdx.y / per, pair = blockIdx.y - run * per;
   const long long NN = (long long)N * N;
+  float2 *data = (pair == 0 ? data0 : data1) + (long long)run * NN * N;
+  io.u += run * io.ustride;
+  io.felas += run * io.fstride;
+  const int tid = threadIdx.x;
   long long base;
   long long ps;  // element stride along the line
   if (AXIS == 0) {
@@ -373,7 +382,7 @@ __global__ void __launch_bounds__(L *(N1 > N2 ? N1 : N2))
     const int gl = blockIdx.x * L + l, z = gl / N, y = gl - z * N;
     return ((long long)(z + 2) * io.n + (y + 2)) * io.n + 2;
   };
-  const int f0 = 2 * blockIdx.y;
+  const int f0 = 2 * pair;
   if (tid < L * N2) {
     const int l = AXIS == 0 ? tid / N2 : tid % L, t = AXIS == 0 ? tid % N2 : tid / L;
     float2 v[N1];
@@ -442,7 +451,8 @@ static cudaError_t launch_one(float2 *z0, float2 *z1, const float2 *tw, const Li
     const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
   }
-  const dim3 grid((unsigned)((long long)N * N / L), z1 ? 2u : 1u);
+  const int runs = io.runs > 0 ? io.runs : 1;
+  const dim3 grid((unsigned)((long long)N * N / L), (z1 ? 2u : 1u) * runs);
   k<<<grid, L * (N1 > N2 ? N1 : N2), sm, s>>>(z0, z1 ? z1 : z0, tw, io);
   return cudaGetLastError();
 }
@@ -597,6 +607,9 @@ __global__ void contract_kernel(typename Cx<T>::t *z01, typename Cx<T>::t *z23, 
                                 int nac) {
   typedef typename Cx<T>::t C;
   const long long N3 = (long long)N * N * N;
+  // blockIdx.y = run: its grids at run N^3
+  z01 += blockIdx.y * N3;
+  if (z23) z23 += blockIdx.y * N3;
   for (int row = blockIdx.x; row < N * N; row += gridDim.x) {
   const int z = row / N, y = row - z * N;
   const int ym = y == 0 ? 0 : N - y, zm = z == 0 ? 0 : N - z;
@@ -675,6 +688,7 @@ __global__ void unpack_kernel(const typename Cx<T>::t *__restrict__ w01, const t
 
 struct ElasticPlan {
   int N, nac, fp32;
+  int runs;       // runs side by side (grids z01, z23 of runs N^3 each)
   Radices rad;
   void *tw;       // twiddles, complex of the working precision
   void *z01, *z23;
@@ -692,15 +706,17 @@ static int grid1(long long total) {
 }
 
 cudaError_t elastic_plan_create(ElasticPlan **out, int N, int nac, const double *voigt, const double *eps, int fp32,
-                                cudaStream_t s) {
+                                cudaStream_t s, int runs) {
   ElasticPlan *p = new ElasticPlan();
   memset(p, 0, sizeof *p);
   p->N = N;
   p->nac = nac;
   p->fp32 = fp32;
+  p->runs = runs > 0 ? runs : 1;
   p->first = true;
   p->rad = factor(N);
-  if (p->rad.count < 0 || nac < 1 || nac > 4) {
+  // several runs take the two-pass FP32 path only
+  if (p->rad.count < 0 || nac < 1 || nac > 4 || (p->runs > 1 && (!fp32 || fft2::pass_n1(N) == 0))) {
     delete p;
     return cudaErrorInvalidValue;
   }
@@ -708,8 +724,8 @@ cudaError_t elastic_plan_create(ElasticPlan **out, int N, int nac, const double 
   size_t csz = fp32 ? sizeof(float2) : sizeof(double2);
   cudaError_t e;
   if ((e = cudaMalloc(&p->tw, csz * N)) != cudaSuccess) goto fail;
-  if ((e = cudaMalloc(&p->z01, csz * N3)) != cudaSuccess) goto fail;
-  if (nac > 2 && (e = cudaMalloc(&p->z23, csz * N3)) != cudaSuccess) goto fail;
+  if ((e = cudaMalloc(&p->z01, csz * N3 * p->runs)) != cudaSuccess) goto fail;
+  if (nac > 2 && (e = cudaMalloc(&p->z23, csz * N3 * p->runs)) != cudaSuccess) goto fail;
   if ((e = cudaMalloc(&p->bn, (fp32 ? sizeof(float) : sizeof(double)) * 10 * N3)) != cudaSuccess) goto fail;
   {
     std::vector<double> twd(2 * N);
@@ -723,7 +739,7 @@ cudaError_t elastic_plan_create(ElasticPlan **out, int N, int nac, const double 
       for (int j = 0; j < 2 * N; j++) twf[j] = (float)twd[j];
       e = cudaMemcpyAsync(p->tw, twf.data(), sizeof(float) * 2 * N, cudaMemcpyHostToDevice, s);
       if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-      p->fast = fft2::pass_n1(N) != 0 && getenv("SCLET_FFT_GENERIC") == nullptr;
+      p->fast = fft2::pass_n1(N) != 0 && (p->runs > 1 || getenv("SCLET_FFT_GENERIC") == nullptr);
       if (e == cudaSuccess && p->fast) e = fft2::upload_constants(s);
     } else {
       e = cudaMemcpyAsync(p->tw, twd.data(), sizeof(double) * 2 * N, cudaMemcpyHostToDevice, s);
@@ -832,7 +848,7 @@ static dim3 rows_grid(int N) { return dim3((unsigned)(N * N < 152 * 16 ? N * N :
 static dim3 rows_block(int N) { return dim3((unsigned)(N >= 256 ? 256 : (N + 31) / 32 * 32)); }
 
 template <typename T>
-cudaError_t elastic_compute(ElasticPlan *p, const T *u, T *felas, int n, T *shell, cudaStream_t s) {
+cudaError_t elastic_compute(ElasticPlan *p, const T *u, T *felas, int n, T *shell, cudaStream_t s, long long ustride) {
   typedef typename Cx<T>::t C;
   const int N = p->N;
   const long long n3 = (long long)n * n * n;
@@ -846,13 +862,17 @@ cudaError_t elastic_compute(ElasticPlan *p, const T *u, T *felas, int n, T *shel
     io.nac = p->nac;
     io.n3 = n3;
     io.scale = (float)(1.0 / ((double)N * N * N));
+    io.runs = p->runs;
+    io.ustride = ustride;
+    io.fstride = (long long)p->nac * n3;
     const float2 *tw = (const float2 *)p->tw;
     for (int k = 0; k < 3; k++) {
       cudaError_t e = fft2::launch(N, -1, k, (float2 *)z01, (float2 *)z23, tw, io, s);
       launch_counter()++;
       if (e != cudaSuccess) return e;
     }
-    contract_kernel<T, float><<<rows_grid(N), rows_block(N), 0, s>>>(z01, z23, (const float *)p->bn, N, p->nac);
+    contract_kernel<T, float><<<dim3(rows_grid(N).x, p->runs), rows_block(N), 0, s>>>(z01, z23, (const float *)p->bn,
+                                                                                       N, p->nac);
     launch_counter()++;
     for (int k = 0; k < 3; k++) {
       cudaError_t e = fft2::launch(N, +1, k, (float2 *)z01, (float2 *)z23, tw, io, s);
@@ -872,25 +892,30 @@ cudaError_t elastic_compute(ElasticPlan *p, const T *u, T *felas, int n, T *shel
     unpack_kernel<T><<<rows_grid(N), rows_block(N), 0, s>>>(z01, z23, felas, N, p->nac);
     launch_counter()++;
   }
-  // ghost cells: the shared-scratch semantics, field by field in order
+  // ghost cells: the shared-scratch semantics, field by field in order (all
+  // runs of a field in one launch)
+  const long long fstride = (long long)p->nac * n3;
   for (int q = 0; q < p->nac; q++) {
     const T *prev = felas + (long long)((q + p->nac - 1) % p->nac) * n3;
+    long long pstride = fstride;
+    T *gbuf = shell;
     if (p->first && q == 0) {
       // before the first call the scratch block is all zero
       cudaMemsetAsync(shell, 0, sizeof(T) * n3, s);
       prev = shell;
-      cudaError_t e = launch_elastic_shell<T>(felas, prev, n, shell + n3, s);
-      if (e != cudaSuccess) return e;
-      continue;
+      pstride = 0;
+      gbuf = shell + n3;
     }
-    cudaError_t e = launch_elastic_shell<T>(felas + q * n3, prev, n, shell, s);
+    cudaError_t e = launch_elastic_shell<T>(felas + q * n3, prev, n, gbuf, s, p->runs, fstride, pstride);
     if (e != cudaSuccess) return e;
   }
   p->first = false;
   return cudaGetLastError();
 }
 
-template cudaError_t elastic_compute<double>(ElasticPlan *, const double *, double *, int, double *, cudaStream_t);
-template cudaError_t elastic_compute<float>(ElasticPlan *, const float *, float *, int, float *, cudaStream_t);
+template cudaError_t elastic_compute<double>(ElasticPlan *, const double *, double *, int, double *, cudaStream_t,
+                                             long long);
+template cudaError_t elastic_compute<float>(ElasticPlan *, const float *, float *, int, float *, cudaStream_t,
+                                            long long);
 
 }  // namespace sclet

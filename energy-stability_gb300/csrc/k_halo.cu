@@ -75,7 +75,11 @@ cudaError_t launch_ghost_fill(T *u, int count, int n, T *shell, cudaStream_t s) 
 // interior cell (this field's value) or a ghost cell (prev's value).
 template <typename T>
 __global__ void elastic_shell_gather(const T *__restrict__ fp, const T *__restrict__ prev, T *__restrict__ shell, int n,
-                                     long long ns) {
+                                     long long ns, long long fstride, long long pstride) {
+  // blockIdx.y = run
+  fp += blockIdx.y * fstride;
+  prev += blockIdx.y * pstride;
+  shell += blockIdx.y * ns;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ns; i += (long long)gridDim.x * blockDim.x) {
     int z, y, x;
     shell_cell(n, i, z, y, x);
@@ -89,20 +93,36 @@ __global__ void elastic_shell_gather(const T *__restrict__ fp, const T *__restri
   }
 }
 
+// one scatter of the shell of blockIdx.y's run (stride between runs' blocks)
 template <typename T>
-cudaError_t launch_elastic_shell(T *felas_p, const T *prev, int n, T *shell, cudaStream_t s) {
+__global__ void shell_scatter_runs(T *__restrict__ u, const T *__restrict__ shell, int n, long long ns,
+                                   long long stride) {
+  u += blockIdx.y * stride;
+  shell += blockIdx.y * ns;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < ns; i += (long long)gridDim.x * blockDim.x) {
+    int z, y, x;
+    shell_cell(n, i, z, y, x);
+    u[((long long)z * n + y) * n + x] = shell[i];
+  }
+}
+
+template <typename T>
+cudaError_t launch_elastic_shell(T *felas_p, const T *prev, int n, T *shell, cudaStream_t s, int runs,
+                                 long long fstride, long long pstride) {
   long long ns = shell_count(n);
-  int g = grid_for(ns);
-  elastic_shell_gather<T><<<g, 256, 0, s>>>(felas_p, prev, shell, n, ns);
-  ghost_scatter<T><<<g, 256, 0, s>>>(felas_p, shell, n, ns, 1);
+  const dim3 g(grid_for(ns), runs > 0 ? runs : 1);
+  elastic_shell_gather<T><<<g, 256, 0, s>>>(felas_p, prev, shell, n, ns, fstride, pstride);
+  shell_scatter_runs<T><<<g, 256, 0, s>>>(felas_p, shell, n, ns, fstride);
   launch_counter() += 2;
   return cudaGetLastError();
 }
 
 template cudaError_t launch_ghost_fill<double>(double *, int, int, double *, cudaStream_t);
 template cudaError_t launch_ghost_fill<float>(float *, int, int, float *, cudaStream_t);
-template cudaError_t launch_elastic_shell<double>(double *, const double *, int, double *, cudaStream_t);
-template cudaError_t launch_elastic_shell<float>(float *, const float *, int, float *, cudaStream_t);
+template cudaError_t launch_elastic_shell<double>(double *, const double *, int, double *, cudaStream_t, int,
+                                                  long long, long long);
+template cudaError_t launch_elastic_shell<float>(float *, const float *, int, float *, cudaStream_t, int, long long,
+                                                 long long);
 
 long long &launch_counter() {
   static long long c = 0;

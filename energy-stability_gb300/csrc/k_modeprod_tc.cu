@@ -569,7 +569,8 @@ cudaError_t launch_modeprod_tc(const __nv_bfloat16 *mat, const __nv_bfloat16 *pl
   g.bits = bits;
   const long long tiles = (long long)((n + tc::BM - 1) / tc::BM) * (((long long)n * n + tc::BN - 1) / tc::BN) * count;
   if (tiles > 0x7fffffffLL) return cudaErrorInvalidValue;
-  // persistent: as many CTAs as can be resident at once
+  // persistent: as many CTAs as can be resident at once (or the tuned count)
+  if (args.max_ctas > 0 && args.max_ctas < ctas) ctas = args.max_ctas;
   const int grid = (int)(tiles < ctas ? tiles : ctas);
   tc::modeprod_tc_kernel<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(ma, mb, g);
   launch_counter()++;

@@ -21,6 +21,8 @@
 
 namespace sclet {
 
+constexpr int ZC = 32;  // default z-planes per CTA of the Allen-Cahn kernel
+
 template <typename T>
 struct P {
   int n, nac, nch, F, aniso, elastic;
@@ -28,6 +30,8 @@ struct P {
   T ih2x, ih2y, ih2z;   // 1 / h^2 per axis
   T i2hx, i2hy, i2hz;   // 1 / (2 h) per axis
   T K[16];              // plugin constants (reference composition shifted by cshift)
+  int zc, runs;         // z-planes per CTA (AC kernel); runs side by side
+  const double *krun;   // per-run plugin constant 0, or null
   // anisotropic term folded: kan[m][3 r + c] = epn2 LE (1/2h_r) lam_m[r][c] (1/2h_c),
   // the flux row r differenced along axis r
   T kan[4][9];
@@ -43,6 +47,9 @@ static P<T> to_p(const Phys &ph) {
   p.i2hx = (T)(0.5 / ph.h[0]); p.i2hy = (T)(0.5 / ph.h[1]); p.i2hz = (T)(0.5 / ph.h[2]);
   p.LE = (T)ph.LE; p.KE = (T)ph.KE; p.LCI = (T)ph.LCI; p.KCI = (T)ph.KCI; p.es = (T)ph.elastic_scale;
   for (int k = 0; k < 16; k++) p.K[k] = (T)ph.K[k];
+  p.zc = ph.rhs_zc > 0 ? ph.rhs_zc : ZC;
+  p.runs = ph.runs > 0 ? ph.runs : 1;
+  p.krun = ph.krun;
   const double i2h[3] = {0.5 / ph.h[0], 0.5 / ph.h[1], 0.5 / ph.h[2]};
   for (int m = 0; m < 4; m++)
     for (int k = 0; k < 9; k++) {
@@ -80,23 +87,31 @@ __device__ inline long long L3(int n, int z, int y, int x) { return ((long long)
 constexpr int RX = 32, RY = 8;
 
 // Allen-Cahn right-hand side, 2.5-D: a CTA owns a 32 x 8 (x, y) tile and
-// marches over ZC planes in z, keeping for every order parameter a ring of five
+// marches over p.zc planes in z (ZC by default), keeping for every order parameter a ring of five
 // planes (z-2 .. z+2) with a two-cell halo in x and y in shared memory (zero
 // outside the block, as ac_calc_F2 reads it).  Each value comes from global
 // memory about once per CTA instead of once per stencil tap.
-constexpr int ZC = 32;             // planes per CTA
+// (ZC, the default planes per CTA, is defined at the top of the file)
 constexpr int HX = RX + 4, HY = RY + 4;
 constexpr int PLANE = HX * HY;     // one haloed plane
 
 template <typename PL, typename T, int NAC, bool ANISO>
-__global__ void __launch_bounds__(RX * RY) rhs_ac_kernel(P<T> p, const T *__restrict__ u, const T *__restrict__ felas,
+__global__ void __launch_bounds__(RX * RY) rhs_ac_kernel(P<T> p0, const T *__restrict__ u, const T *__restrict__ felas,
                                                          T *__restrict__ out) {
   extern __shared__ unsigned char smem_raw[];
   T *ring = reinterpret_cast<T *>(smem_raw);  // [nac][5][HY][HX]
-  const int n = p.n;
+  const int n = p0.n;
   const size_t n3 = (size_t)n * n * n;
+  // blockIdx.z = run x z-chunks
+  const int zchunks = (n + p0.zc - 1) / p0.zc;
+  const int run = blockIdx.z / zchunks, zci = blockIdx.z - run * zchunks;
+  P<T> p = p0;
+  if (p0.krun) p.K[0] = (T)p0.krun[run];
+  u += (size_t)run * p.F * n3;
+  felas += (size_t)run * p.nac * n3;
+  out += (size_t)run * p.F * n3;
   const int x0 = blockIdx.x * RX, y0 = blockIdx.y * RY;
-  const int zb = blockIdx.z * ZC, ze = zb + ZC < n ? zb + ZC : n;
+  const int zb = zci * p.zc, ze = zb + p.zc < n ? zb + p.zc : n;
   const int tid = threadIdx.y * RX + threadIdx.x;
   const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
   // this thread's share of one haloed plane of every order parameter:
@@ -203,11 +218,16 @@ __global__ void __launch_bounds__(RX * RY) rhs_ac_kernel(P<T> p, const T *__rest
 // t = -LCI KCI c + LCI CH_f, minus the face liftings (first part of
 // ch_calc_FU_ConstantMobility).
 template <typename PL, typename T>
-__global__ void __launch_bounds__(RX * RY) rhs_ch_t_kernel(P<T> p, const T *__restrict__ u, T *__restrict__ t) {
-  const int n = p.n;
-  const int x = blockIdx.x * RX + threadIdx.x, y = blockIdx.y * RY + threadIdx.y, z = blockIdx.z;
+__global__ void __launch_bounds__(RX * RY) rhs_ch_t_kernel(P<T> p0, const T *__restrict__ u, T *__restrict__ t) {
+  const int n = p0.n;
+  const int run = blockIdx.z / n;  // blockIdx.z = run x z
+  const int x = blockIdx.x * RX + threadIdx.x, y = blockIdx.y * RY + threadIdx.y, z = blockIdx.z - run * n;
   if (x >= n || y >= n) return;
   const size_t n3 = (size_t)n * n * n;
+  P<T> p = p0;
+  if (p0.krun) p.K[0] = (T)p0.krun[run];
+  u += (size_t)run * p.F * n3;
+  t += (size_t)run * n3;
   const size_t l = ((size_t)z * n + y) * n + x;
   const T *cf = u + p.nac * n3;
   T e[4] = {(T)0, (T)0, (T)0, (T)0};
@@ -249,11 +269,20 @@ __device__ inline T ch_mu_at(const P<T> &p, const T *__restrict__ u, int z, int 
 
 // N_c = lap(t) (zero outside), minus mu(outside)/h^2 on faces.
 template <typename PL, typename T>
-__global__ void __launch_bounds__(RX * RY) rhs_ch_lap_kernel(P<T> p, const T *__restrict__ u, const T *__restrict__ t,
+__global__ void __launch_bounds__(RX * RY) rhs_ch_lap_kernel(P<T> p0, const T *__restrict__ u, const T *__restrict__ t,
                                                              T *__restrict__ out) {
-  const int n = p.n;
-  const int x = blockIdx.x * RX + threadIdx.x, y = blockIdx.y * RY + threadIdx.y, z = blockIdx.z;
+  const int n = p0.n;
+  const int run = blockIdx.z / n;  // blockIdx.z = run x z
+  const int x = blockIdx.x * RX + threadIdx.x, y = blockIdx.y * RY + threadIdx.y, z = blockIdx.z - run * n;
   if (x >= n || y >= n) return;
+  P<T> p = p0;
+  if (p0.krun) p.K[0] = (T)p0.krun[run];
+  {
+    const size_t n3 = (size_t)n * n * n;
+    u += (size_t)run * p.F * n3;
+    t += (size_t)run * n3;
+    out += (size_t)run * p.F * n3;
+  }
   const size_t nn = (size_t)n * n;
   const size_t l = (size_t)z * nn + (size_t)y * n + x;
   const T tc = t[l];
@@ -279,10 +308,10 @@ template <typename PL, typename T>
 static cudaError_t launch_rhs_pl(const Phys &ph, const T *u, const T *felas, T *out, T *scratch, cudaStream_t s) {
   P<T> p = to_p<T>(ph);
   long long n3 = (long long)ph.n * ph.n * ph.n;
-  const dim3 blk(RX, RY), grd((ph.n + RX - 1) / RX, (ph.n + RY - 1) / RY, ph.n);
+  const dim3 blk(RX, RY), grd((ph.n + RX - 1) / RX, (ph.n + RY - 1) / RY, ph.n * p.runs);
   if (ph.nac > 0) {
     const size_t smem = sizeof(T) * ph.nac * 5 * PLANE;
-    const dim3 gac((ph.n + RX - 1) / RX, (ph.n + RY - 1) / RY, (ph.n + ZC - 1) / ZC);
+    const dim3 gac((ph.n + RX - 1) / RX, (ph.n + RY - 1) / RY, ((ph.n + p.zc - 1) / p.zc) * p.runs);
     cudaError_t e = cudaSuccess;
     switch (ph.nac * 2 + (ph.anisotropic ? 1 : 0)) {
 #define SCLET_RHS_AC(NAC, AN)                                                                                  \
@@ -303,7 +332,7 @@ static cudaError_t launch_rhs_pl(const Phys &ph, const T *u, const T *felas, T *
     for (int m = 0; m < ph.nch; m++) {
       // one conserved field (the plugins' CH_f is defined for c_0 only)
       rhs_ch_t_kernel<PL, T><<<grd, blk, 0, s>>>(p, u, scratch);
-      rhs_ch_lap_kernel<PL, T><<<grd, blk, 0, s>>>(p, u, scratch, out + (long long)ph.nac * n3);
+      rhs_ch_lap_kernel<PL, T><<<grd, blk, 0, s>>>(p, u, scratch, out + (long long)ph.nac * n3);  // per run: + r F n^3
       launch_counter() += 2;
     }
   }

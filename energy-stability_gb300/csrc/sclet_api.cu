@@ -37,6 +37,10 @@ struct sclet_ctx {
   int precision = SCLET_FP64, device = 0;
   int step_diag = -1;  // energy form of the diagnostics sclet_step queues after each step; -1 none
   int n = 0, F = 0, nac = 0, nch = 0;
+  // runs of the same size side by side (sclet_create_runs): FT = runs F
+  // stored fields, run r's at r F n^3; krun = per-run plugin constant 0
+  int runs = 1, FT = 0;
+  double *krun = nullptr;
   long long n3 = 0;
   Phys ph;
   cudaStream_t stream = nullptr;
@@ -81,6 +85,10 @@ struct sclet_ctx {
   float stage_ms[8] = {0};
   int stage_launches[8] = {0};
   long long launches0 = 0;
+  long long steps_done = 0;
+  // one step captured as a CUDA graph (sclet_graph_step)
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
 };
 
 static std::string g_create_error;
@@ -98,9 +106,9 @@ namespace {
 
 bool mixed(const sclet_ctx *ctx) { return ctx->precision == SCLET_MIXED; }
 double *u_of(sclet_ctx *ctx) { return ctx->state2; }
-double *rhs1_of(sclet_ctx *ctx) { return ctx->state2 + (long long)ctx->F * ctx->n3; }
+double *rhs1_of(sclet_ctx *ctx) { return ctx->state2 + (long long)ctx->FT * ctx->n3; }
 float *fu_of(sclet_ctx *ctx) { return ctx->fstate2; }
-float *frhs1_of(sclet_ctx *ctx) { return ctx->fstate2 + (long long)ctx->F * ctx->n3; }
+float *frhs1_of(sclet_ctx *ctx) { return ctx->fstate2 + (long long)ctx->FT * ctx->n3; }
 
 // phi1, phi2 of each field kind at eigen-mode (i, j, k), layout [k][j][i]
 // (ac_init_phi / ch_init_phi, vars.c:302-359).
@@ -144,16 +152,16 @@ __global__ void f32_to_f64(const float *__restrict__ a, double *__restrict__ b, 
 // all F fields between the FP64 host layout and the state: FP32 states hold
 // the conserved fields (f >= nac) relative to shift; grid y = field
 __global__ void fields_to_state(const double *__restrict__ a, float *__restrict__ b, long long n3, int nac,
-                                double shift) {
-  const double sh = (int)blockIdx.y >= nac ? shift : 0.0;
+                                double shift, int F) {
+  const double sh = (int)blockIdx.y % F >= nac ? shift : 0.0;
   const double *s = a + blockIdx.y * n3;
   float *d = b + blockIdx.y * n3;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3; i += (long long)gridDim.x * blockDim.x)
     d[i] = (float)(s[i] - sh);
 }
 __global__ void fields_from_state(const float *__restrict__ a, double *__restrict__ b, long long n3, int nac,
-                                  double shift) {
-  const double sh = (int)blockIdx.y >= nac ? shift : 0.0;
+                                  double shift, int F) {
+  const double sh = (int)blockIdx.y % F >= nac ? shift : 0.0;
   const float *s = a + blockIdx.y * n3;
   double *d = b + blockIdx.y * n3;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3; i += (long long)gridDim.x * blockDim.x)
@@ -317,7 +325,7 @@ int get_block(sclet_ctx *ctx, const double *src64, const float *src32, double *h
 // staging areas, copy streams and events of the pipelined transfers, on first use
 int ensure_io(sclet_ctx *ctx) {
   if (ctx->copy_in) return SCLET_OK;
-  const size_t bytes = sizeof(double) * ctx->F * ctx->n3;
+  const size_t bytes = sizeof(double) * ctx->FT * ctx->n3;
   if (!ctx->in_stage) CK(cudaMalloc(&ctx->in_stage, bytes));
   if (!ctx->out_stage) CK(cudaMalloc(&ctx->out_stage, bytes));
   cudaEvent_t *evs[] = {&ctx->in_ready, &ctx->in_free, &ctx->out_ready, &ctx->out_free};
@@ -338,14 +346,14 @@ extern "C" {
 int sclet_set_fields_async(sclet_ctx *ctx, const double *host) {
   int rc = ensure_io(ctx);
   if (rc != SCLET_OK) return rc;
-  const size_t bytes = sizeof(double) * ctx->F * ctx->n3;
+  const size_t bytes = sizeof(double) * ctx->FT * ctx->n3;
   CK(cudaStreamWaitEvent(ctx->copy_in, ctx->in_free, 0));
   CK(cudaMemcpyAsync(ctx->in_stage, host, bytes, cudaMemcpyHostToDevice, ctx->copy_in));
   CK(cudaEventRecord(ctx->in_ready, ctx->copy_in));
   CK(cudaStreamWaitEvent(ctx->stream, ctx->in_ready, 0));
   if (mixed(ctx)) {
-    fields_to_state<<<dim3(grid_of(ctx->n3), ctx->F), 256, 0, ctx->stream>>>(ctx->in_stage, fu_of(ctx), ctx->n3,
-                                                                            ctx->nac, ctx->ph.cshift);
+    fields_to_state<<<dim3(grid_of(ctx->n3), ctx->FT), 256, 0, ctx->stream>>>(ctx->in_stage, fu_of(ctx), ctx->n3,
+                                                                             ctx->nac, ctx->ph.cshift, ctx->F);
     launch_counter()++;
     CK(cudaGetLastError());
   } else {
@@ -358,11 +366,12 @@ int sclet_set_fields_async(sclet_ctx *ctx, const double *host) {
 int sclet_get_fields_async(sclet_ctx *ctx, double *host) {
   int rc = ensure_io(ctx);
   if (rc != SCLET_OK) return rc;
-  const size_t bytes = sizeof(double) * ctx->F * ctx->n3;
+  const size_t bytes = sizeof(double) * ctx->FT * ctx->n3;
   CK(cudaStreamWaitEvent(ctx->stream, ctx->out_free, 0));
   if (mixed(ctx)) {
-    fields_from_state<<<dim3(grid_of(ctx->n3), ctx->F), 256, 0, ctx->stream>>>(fu_of(ctx), ctx->out_stage, ctx->n3,
-                                                                              ctx->nac, ctx->ph.cshift);
+    fields_from_state<<<dim3(grid_of(ctx->n3), ctx->FT), 256, 0, ctx->stream>>>(fu_of(ctx), ctx->out_stage,
+                                                                               ctx->n3, ctx->nac, ctx->ph.cshift,
+                                                                               ctx->F);
     launch_counter()++;
     CK(cudaGetLastError());
   } else {
@@ -392,13 +401,15 @@ int sclet_get_fields(sclet_ctx *ctx, double *host) {
 const char *sclet_last_error(const sclet_ctx *ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
 
 int sclet_block_edge(const sclet_ctx *ctx) { return ctx->n; }
-int sclet_field_count(const sclet_ctx *ctx) { return ctx->F; }
+int sclet_field_count(const sclet_ctx *ctx) { return ctx->FT; }
 void *sclet_stream(const sclet_ctx *ctx) { return (void *)ctx->stream; }
 long long sclet_launch_count(const sclet_ctx *ctx) { return launch_counter() - ctx->launches0; }
 
 void sclet_destroy(sclet_ctx *ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
+  if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+  if (ctx->graph) cudaGraphDestroy(ctx->graph);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   if (ctx->copy_in) cudaStreamSynchronize(ctx->copy_in);
   if (ctx->copy_out) cudaStreamSynchronize(ctx->copy_out);
@@ -407,7 +418,7 @@ void sclet_destroy(sclet_ctx *ctx) {
                   ctx->fstate2, ctx->frhs2, ctx->ffelas, ctx->fscratch, ctx->fshell, ctx->W1, ctx->W2, ctx->P,
                   ctx->scaleP, ctx->rsV, ctx->rsVi, ctx->matV, ctx->matVi, ctx->stage64,
                   ctx->coef[0], ctx->coef[1], ctx->coef2[0], ctx->coef2[1], ctx->massW, ctx->massPart,
-                  ctx->massRes, ctx->in_stage, ctx->out_stage};
+                  ctx->massRes, ctx->in_stage, ctx->out_stage, ctx->krun};
   for (void *b : bufs) cudaFree(b);
   if (ctx->diag_host) cudaFreeHost(ctx->diag_host);
   for (int a = 0; a < 3; a++) {
@@ -430,8 +441,21 @@ void sclet_destroy(sclet_ctx *ctx) {
 }
 
 int sclet_create(const sclet_params *p, int precision, int device, sclet_ctx **out) {
+  return sclet_create_runs(p, 1, nullptr, precision, device, out);
+}
+
+int sclet_create_runs(const sclet_params *p, int runs, const double *krun, int precision, int device,
+                      sclet_ctx **out) {
   *out = nullptr;
   g_create_error.clear();
+  if (runs < 1) {
+    g_create_error = "runs must be at least 1";
+    return SCLET_ERR_ARG;
+  }
+  if (runs > 1 && (precision != SCLET_MIXED || p->nch != 0)) {
+    g_create_error = "several runs in one context: the mixed form, order parameters only (nch = 0)";
+    return SCLET_ERR_UNSUPPORTED;
+  }
   auto bad = [&](const char *m) {
     g_create_error = m;
     return SCLET_ERR_ARG;
@@ -466,15 +490,18 @@ int sclet_create(const sclet_params *p, int precision, int device, sclet_ctx **o
   ctx->nac = p->nac;
   ctx->nch = p->nch;
   ctx->F = p->nac + p->nch;
+  ctx->runs = runs;
+  ctx->FT = runs * ctx->F;
   ctx->n3 = (long long)ctx->n * ctx->n * ctx->n;
   ctx->launches0 = launch_counter();
-  const int n = ctx->n, F = ctx->F, N = n - 4;
+  const int n = ctx->n, F = ctx->F, N = n - 4, FT = ctx->FT;
   Phys &ph = ctx->ph;
   memset(&ph, 0, sizeof ph);
   ph.n = n;
   ph.nac = ctx->nac;
   ph.nch = ctx->nch;
   ph.F = F;
+  ph.runs = runs;
   ph.anisotropic = p->anisotropic;
   ph.elastic = p->elastic;
   ph.dt = p->dt;
@@ -514,8 +541,13 @@ int sclet_create(const sclet_params *p, int precision, int device, sclet_ctx **o
   for (int a = 0; a < 3; a++) CC(cudaMalloc(&ctx->dd[a], sizeof(double) * n));
   CC(cudaMalloc(&ctx->elam, sizeof(double) * 36));
   ctx->npart = check_soln_partials(n);
-  CC(cudaMalloc(&ctx->partials, sizeof(double) * ctx->npart * (4 * F + 4)));
-  CC(cudaHostAlloc(&ctx->diag_host, sizeof(double) * 4 * F, cudaHostAllocMapped | cudaHostAllocPortable));
+  CC(cudaMalloc(&ctx->partials, sizeof(double) * ctx->npart * (4 * F + 4) * runs));
+  CC(cudaHostAlloc(&ctx->diag_host, sizeof(double) * 4 * FT, cudaHostAllocMapped | cudaHostAllocPortable));
+  if (krun) {
+    CC(cudaMalloc(&ctx->krun, sizeof(double) * runs));
+    CC(cudaMemcpy(ctx->krun, krun, sizeof(double) * runs, cudaMemcpyHostToDevice));
+    ph.krun = ctx->krun;
+  }
   CC(cudaHostGetDevicePointer(&ctx->diag, ctx->diag_host, 0));
   CC(cudaMalloc(&ctx->dev_err, sizeof(int)));
   CC(cudaMemsetAsync(ctx->dev_err, 0, sizeof(int), s));
@@ -541,21 +573,23 @@ int sclet_create(const sclet_params *p, int precision, int device, sclet_ctx **o
     }
   } else {
     const size_t blk = sizeof(float) * ctx->n3;
-    CC(cudaMalloc(&ctx->fstate2, 2 * F * blk));
-    CC(cudaMemsetAsync(ctx->fstate2, 0, 2 * F * blk, s));
-    if (p->etd2) CC(cudaMalloc(&ctx->frhs2, F * blk));
-    CC(cudaMalloc(&ctx->ffelas, nfel * blk));
-    CC(cudaMemsetAsync(ctx->ffelas, 0, nfel * blk, s));
-    CC(cudaMalloc(&ctx->fscratch, 2 * blk));
-    CC(cudaMalloc(&ctx->fshell, sizeof(float) * F * shell_count(n)));
-    CC(cudaMalloc(&ctx->W1, 2 * F * blk));
-    CC(cudaMalloc(&ctx->W2, 2 * F * blk));
+    CC(cudaMalloc(&ctx->fstate2, 2 * FT * blk));
+    CC(cudaMemsetAsync(ctx->fstate2, 0, 2 * FT * blk, s));
+    if (p->etd2) CC(cudaMalloc(&ctx->frhs2, FT * blk));
+    CC(cudaMalloc(&ctx->ffelas, nfel * runs * blk));
+    CC(cudaMemsetAsync(ctx->ffelas, 0, nfel * runs * blk, s));
+    // elastic ghost shells of every run (and the zero block of the first
+    // call) or the CH scratch of every run
+    CC(cudaMalloc(&ctx->fscratch, (runs + 1) * blk));
+    CC(cudaMalloc(&ctx->fshell, sizeof(float) * FT * shell_count(n)));
+    CC(cudaMalloc(&ctx->W1, 2 * FT * blk));
+    CC(cudaMalloc(&ctx->W2, 2 * FT * blk));
     {
-      const size_t pbytes = sizeof(__nv_bfloat16) * plane_stride(ctx) * 2 * F;
+      const size_t pbytes = sizeof(__nv_bfloat16) * plane_stride(ctx) * 2 * FT;
       // pad columns of the slice planes are never written and must stay zero
       CC(cudaMalloc(&ctx->P, pbytes));
       CC(cudaMemsetAsync(ctx->P, 0, pbytes, s));
-      CC(cudaMalloc(&ctx->scaleP, sizeof(float) * 2 * F * n * n));
+      CC(cudaMalloc(&ctx->scaleP, sizeof(float) * 2 * FT * n * n));
     }
     CC(cudaMalloc(&ctx->matV, sizeof(__nv_bfloat16) * TC_PLANES_M * n * tc_kp(n)));
     CC(cudaMalloc(&ctx->matVi, sizeof(__nv_bfloat16) * TC_PLANES_M * n * tc_kp(n)));
@@ -593,7 +627,7 @@ int sclet_create(const sclet_params *p, int precision, int device, sclet_ctx **o
     }
   }
   if (p->elastic == 1) {
-    CC(elastic_plan_create(&ctx->elastic, N, ctx->nac, p->voigt, &p->eigenstrain[0][0], mixed(ctx) ? 1 : 0, s));
+    CC(elastic_plan_create(&ctx->elastic, N, ctx->nac, p->voigt, &p->eigenstrain[0][0], mixed(ctx) ? 1 : 0, s, runs));
   }
   CC(cudaStreamSynchronize(s));
 #undef CC
@@ -615,6 +649,7 @@ int sclet_set_energy_tensors(sclet_ctx *ctx, const double *lam) {
 }
 
 int sclet_set_field(sclet_ctx *ctx, int kind, int m, const double *block) {
+  if (ctx->runs > 1) return fail(ctx, SCLET_ERR_UNSUPPORTED, "per-field access to a context of several runs");
   int f = field_index(ctx, kind, m);
   if (f < 0) return fail(ctx, SCLET_ERR_ARG, "no such field");
   return mixed(ctx) ? put_block(ctx, block, nullptr, fu_of(ctx) + f * ctx->n3, f >= ctx->nac ? ctx->ph.cshift : 0.0)
@@ -622,6 +657,7 @@ int sclet_set_field(sclet_ctx *ctx, int kind, int m, const double *block) {
 }
 
 int sclet_get_field(sclet_ctx *ctx, int kind, int m, double *block) {
+  if (ctx->runs > 1) return fail(ctx, SCLET_ERR_UNSUPPORTED, "per-field access to a context of several runs");
   int f = field_index(ctx, kind, m);
   if (f < 0) return fail(ctx, SCLET_ERR_ARG, "no such field");
   return mixed(ctx) ? get_block(ctx, nullptr, fu_of(ctx) + f * ctx->n3, block, f >= ctx->nac ? ctx->ph.cshift : 0.0)
@@ -632,6 +668,7 @@ int sclet_get_field(sclet_ctx *ctx, int kind, int m, double *block) {
 static void make_rank_dir(const char *dir) { mkdir((std::string(dir) + "00").c_str(), 0755); }
 
 int sclet_write_chk(sclet_ctx *ctx, const char *dir, int chk, int irun) {
+  if (ctx->runs > 1) return fail(ctx, SCLET_ERR_UNSUPPORTED, "per-field access to a context of several runs");
   std::vector<double> blk(ctx->n3);
   char path[4096];
   make_rank_dir(dir);
@@ -646,6 +683,7 @@ int sclet_write_chk(sclet_ctx *ctx, const char *dir, int chk, int irun) {
 }
 
 int sclet_read_chk(sclet_ctx *ctx, const char *dir, int chk, int *irun) {
+  if (ctx->runs > 1) return fail(ctx, SCLET_ERR_UNSUPPORTED, "per-field access to a context of several runs");
   std::vector<double> blk(ctx->n3);
   char path[4096];
   for (int m = 0; m < ctx->nac; m++) {
@@ -659,6 +697,7 @@ int sclet_read_chk(sclet_ctx *ctx, const char *dir, int chk, int *irun) {
 }
 
 int sclet_field_u16(sclet_ctx *ctx, int kind, int m, unsigned short *out) {
+  if (ctx->runs > 1) return fail(ctx, SCLET_ERR_UNSUPPORTED, "per-field access to a context of several runs");
   int f = field_index(ctx, kind, m);
   if (f < 0) return fail(ctx, SCLET_ERR_ARG, "no such field");
   const int k = kind == SCLET_CH ? 1 : 0;
@@ -676,6 +715,7 @@ int sclet_field_u16(sclet_ctx *ctx, int kind, int m, unsigned short *out) {
 }
 
 int sclet_write_field2b(sclet_ctx *ctx, const char *data_dir, int irun, int mode) {
+  if (ctx->runs > 1) return fail(ctx, SCLET_ERR_UNSUPPORTED, "per-field access to a context of several runs");
   if (mode != 0 && mode != 1) return fail(ctx, SCLET_ERR_ARG, "mode must be 0 (order parameters) or 1 (concentrations)");
   const int kind = mode == 0 ? SCLET_AC : SCLET_CH, count = mode == 0 ? ctx->nac : ctx->nch;
   std::vector<unsigned short> codes(ctx->n3);
@@ -695,6 +735,7 @@ int sclet_write_field2b(sclet_ctx *ctx, const char *data_dir, int irun, int mode
 }
 
 int sclet_log_soln(sclet_ctx *ctx, const char *work_dir, int iter, int energy_form) {
+  if (ctx->runs > 1) return fail(ctx, SCLET_ERR_UNSUPPORTED, "per-field access to a context of several runs");
   std::vector<sclet_diag> d(ctx->nac + ctx->nch);
   int rc = sclet_check_soln(ctx, energy_form, d.data());
   if (rc != SCLET_OK) return rc;
@@ -710,6 +751,7 @@ int sclet_log_soln(sclet_ctx *ctx, const char *work_dir, int iter, int energy_fo
 }
 
 int sclet_write_vtk(sclet_ctx *ctx, const char *path, int istep) {
+  if (ctx->runs > 1) return fail(ctx, SCLET_ERR_UNSUPPORTED, "per-field access to a context of several runs");
   std::vector<double> blk((size_t)ctx->nac * ctx->n3);
   for (int m = 0; m < ctx->nac; m++) {
     int rc = sclet_get_field(ctx, SCLET_AC, m, blk.data() + (size_t)m * ctx->n3);
@@ -721,6 +763,7 @@ int sclet_write_vtk(sclet_ctx *ctx, const char *path, int istep) {
 }
 
 int sclet_load_restart(sclet_ctx *ctx, int kind, int m, const char *path) {
+  if (ctx->runs > 1) return fail(ctx, SCLET_ERR_UNSUPPORTED, "per-field access to a context of several runs");
   std::vector<double> blk(ctx->n3, 0.0);
   int f = field_index(ctx, kind, m);
   if (f < 0) return fail(ctx, SCLET_ERR_ARG, "no such field");
@@ -732,6 +775,7 @@ int sclet_load_restart(sclet_ctx *ctx, int kind, int m, const char *path) {
 }
 
 int sclet_get_rhs(sclet_ctx *ctx, int slot, int kind, int m, double *block) {
+  if (ctx->runs > 1) return fail(ctx, SCLET_ERR_UNSUPPORTED, "per-field access to a context of several runs");
   int f = field_index(ctx, kind, m);
   bool have2 = mixed(ctx) ? ctx->frhs2 != nullptr : ctx->rhs2 != nullptr;
   if (f < 0 || (slot != 1 && slot != 2) || (slot == 2 && !have2)) return fail(ctx, SCLET_ERR_ARG, "bad rhs slot");
@@ -740,6 +784,7 @@ int sclet_get_rhs(sclet_ctx *ctx, int slot, int kind, int m, double *block) {
 }
 
 int sclet_get_felas(sclet_ctx *ctx, int m, double *block) {
+  if (ctx->runs > 1) return fail(ctx, SCLET_ERR_UNSUPPORTED, "per-field access to a context of several runs");
   if (m < 0 || m >= ctx->nac) return fail(ctx, SCLET_ERR_ARG, "no such field");
   if (mixed(ctx)) return get_block(ctx, nullptr, ctx->ffelas + m * ctx->n3, block);
   return get_block(ctx, ctx->felas + m * ctx->n3, nullptr, block);
@@ -749,7 +794,7 @@ int sclet_transfer(sclet_ctx *ctx) {
   StageEv ev;
   long long l0 = launch_counter();
   stage_begin(ctx, 3, ev);
-  if (mixed(ctx)) CK(launch_ghost_fill<float>(fu_of(ctx), ctx->F, ctx->n, ctx->fshell, ctx->stream));
+  if (mixed(ctx)) CK(launch_ghost_fill<float>(fu_of(ctx), ctx->FT, ctx->n, ctx->fshell, ctx->stream));
   else CK(launch_ghost_fill<double>(u_of(ctx), ctx->F, ctx->n, ctx->shell, ctx->stream));
   stage_end(ctx, ev, l0);
   return SCLET_OK;
@@ -761,7 +806,8 @@ int sclet_elastic_calculate(sclet_ctx *ctx) {
   long long l0 = launch_counter();
   stage_begin(ctx, 2, ev);
   if (mixed(ctx))
-    CK(elastic_compute<float>(ctx->elastic, fu_of(ctx), ctx->ffelas, ctx->n, ctx->fscratch, ctx->stream));
+    CK(elastic_compute<float>(ctx->elastic, fu_of(ctx), ctx->ffelas, ctx->n, ctx->fscratch, ctx->stream,
+                              (long long)ctx->F * ctx->n3));
   else
     CK(elastic_compute<double>(ctx->elastic, u_of(ctx), ctx->felas, ctx->n, ctx->scratch, ctx->stream));
   stage_end(ctx, ev, l0);
@@ -802,6 +848,7 @@ static TcArgs tc_args(sclet_ctx *ctx, bool inverse, int count, float *out, int e
   g.nac = ctx->nac;
   g.F = ctx->F;
   g.err = ctx->dev_err;
+  g.max_ctas = ctx->ph.tc_ctas;
   return g;
 }
 
@@ -833,7 +880,7 @@ static cudaError_t tc_slice(sclet_ctx *ctx, const float *x, const float *sub, in
 // and N1 together, along z for u, then for N1 with the ETD update fused; V
 // along x, y, z back to the FP32 state.
 static int etd_update_mixed(sclet_ctx *ctx) {
-  const int F = ctx->F;
+  const int F = ctx->FT;  // every run's fields
   const long long ps = plane_stride(ctx), rows = (long long)ctx->n * ctx->n, n3 = ctx->n3;
   if (ctx->nch > 0)  // target mass of the conserved field from (u, N1)
     CK(mass_target(fu_of(ctx) + ctx->nac * n3, ctx->massW, frhs1_of(ctx) + ctx->nac * n3, nullptr, ctx->massW + n3,
@@ -859,7 +906,7 @@ static int etd_update_mixed(sclet_ctx *ctx) {
 
 // ETD2 corrector (ScLETD.c:159-188): u += V phi2 V^-1 (N2 - N1).
 static int etd2_correct_mixed(sclet_ctx *ctx) {
-  const int F = ctx->F;
+  const int F = ctx->FT;  // every run's fields
   const long long n3 = ctx->n3, off = ctx->nac * n3;
   if (ctx->nch > 0)  // target: current mass plus <w2, N2 - N1>
     CK(mass_target(fu_of(ctx) + off, nullptr, ctx->frhs2 + off, frhs1_of(ctx) + off, ctx->massW + 2 * n3, ctx->n,
@@ -952,6 +999,7 @@ int sclet_step(sclet_ctx *ctx, int nsteps) {
       if ((rc = sclet_etd2_correct(ctx)) != SCLET_OK) return rc;
     }
     if (ctx->step_diag >= 0 && (rc = queue_diagnostics(ctx, ctx->step_diag)) != SCLET_OK) return rc;
+    ctx->steps_done++;
   }
   return SCLET_OK;
 }
@@ -993,7 +1041,7 @@ int read_diagnostics(sclet_ctx *ctx, sclet_diag *out) {
   CK(cudaStreamSynchronize(ctx->stream));
   const double *h = ctx->diag_host;
   int nonfinite = 0;
-  for (int f = 0; f < ctx->F; f++) {
+  for (int f = 0; f < ctx->FT; f++) {
     out[f].max = h[4 * f];
     out[f].min = h[4 * f + 1];
     out[f].vol = h[4 * f + 2];
@@ -1008,6 +1056,7 @@ int read_diagnostics(sclet_ctx *ctx, sclet_diag *out) {
 extern "C" {
 
 int sclet_mode_product(sclet_ctx *ctx, int inverse, const double *in, double *out) {
+  if (ctx->runs > 1) return fail(ctx, SCLET_ERR_UNSUPPORTED, "per-field access to a context of several runs");
   const long long n3 = ctx->n3;
   if (mixed(ctx)) {
     // in -> FP32 scratch, slices, product, FP32 -> host FP64
@@ -1100,22 +1149,24 @@ int sclet_stage_times(const sclet_ctx *ctx, float *ms, int *launches, int nclass
 // ---- owned cells as FP32 planar device blocks (the learned step) ----------
 namespace {
 template <typename T>
-__global__ void owned_export_kernel(const T *__restrict__ u, float *__restrict__ dst, int n, int nac, double shift) {
+__global__ void owned_export_kernel(const T *__restrict__ u, float *__restrict__ dst, int n, int nac, double shift,
+                                    int F) {
   const int N = n - 4;
   const long long n3 = (long long)N * N * N, b3 = (long long)n * n * n;
   const int f = blockIdx.y;
-  const double sh = f >= nac ? shift : 0.0;
+  const double sh = f % F >= nac ? shift : 0.0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3; i += (long long)gridDim.x * blockDim.x) {
     const int z = (int)(i / ((long long)N * N)), y = (int)((i / N) % N), x = (int)(i % N);
     dst[f * n3 + i] = (float)((double)u[f * b3 + ((long long)(z + 2) * n + y + 2) * n + x + 2] + sh);
   }
 }
 template <typename T>
-__global__ void owned_import_kernel(const float *__restrict__ src, T *__restrict__ u, int n, int nac, double shift) {
+__global__ void owned_import_kernel(const float *__restrict__ src, T *__restrict__ u, int n, int nac, double shift,
+                                    int F) {
   const int N = n - 4;
   const long long n3 = (long long)N * N * N, b3 = (long long)n * n * n;
   const int f = blockIdx.y;
-  const double sh = f >= nac ? shift : 0.0;
+  const double sh = f % F >= nac ? shift : 0.0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3; i += (long long)gridDim.x * blockDim.x) {
     const int z = (int)(i / ((long long)N * N)), y = (int)((i / N) % N), x = (int)(i % N);
     u[f * b3 + ((long long)(z + 2) * n + y + 2) * n + x + 2] = (T)((double)src[f * n3 + i] - sh);
@@ -1126,22 +1177,24 @@ __global__ void owned_import_kernel(const float *__restrict__ src, T *__restrict
 namespace sclet {
 int ctx_export_owned(sclet_ctx *ctx, float *dst) {
   const long long n3 = (long long)(ctx->n - 4) * (ctx->n - 4) * (ctx->n - 4);
-  const dim3 grid(grid_of(n3), ctx->F);
+  const dim3 grid(grid_of(n3), ctx->FT);
   if (mixed(ctx))
-    owned_export_kernel<float><<<grid, 256, 0, ctx->stream>>>(fu_of(ctx), dst, ctx->n, ctx->nac, ctx->ph.cshift);
+    owned_export_kernel<float><<<grid, 256, 0, ctx->stream>>>(fu_of(ctx), dst, ctx->n, ctx->nac, ctx->ph.cshift,
+                                                              ctx->F);
   else
-    owned_export_kernel<double><<<grid, 256, 0, ctx->stream>>>(u_of(ctx), dst, ctx->n, ctx->nac, 0.0);
+    owned_export_kernel<double><<<grid, 256, 0, ctx->stream>>>(u_of(ctx), dst, ctx->n, ctx->nac, 0.0, ctx->F);
   launch_counter()++;
   CK(cudaGetLastError());
   return SCLET_OK;
 }
 int ctx_import_owned(sclet_ctx *ctx, const float *src) {
   const long long n3 = (long long)(ctx->n - 4) * (ctx->n - 4) * (ctx->n - 4);
-  const dim3 grid(grid_of(n3), ctx->F);
+  const dim3 grid(grid_of(n3), ctx->FT);
   if (mixed(ctx))
-    owned_import_kernel<float><<<grid, 256, 0, ctx->stream>>>(src, fu_of(ctx), ctx->n, ctx->nac, ctx->ph.cshift);
+    owned_import_kernel<float><<<grid, 256, 0, ctx->stream>>>(src, fu_of(ctx), ctx->n, ctx->nac, ctx->ph.cshift,
+                                                              ctx->F);
   else
-    owned_import_kernel<double><<<grid, 256, 0, ctx->stream>>>(src, u_of(ctx), ctx->n, ctx->nac, 0.0);
+    owned_import_kernel<double><<<grid, 256, 0, ctx->stream>>>(src, u_of(ctx), ctx->n, ctx->nac, 0.0, ctx->F);
   launch_counter()++;
   CK(cudaGetLastError());
   return SCLET_OK;
@@ -1154,3 +1207,130 @@ int ctx_fail(sclet_ctx *ctx, int code, const char *msg) {
   return code;
 }
 }  // namespace sclet
+
+// ---- CUDA graphs and the autotuner ------------------------------------------
+namespace {
+void drop_graph(sclet_ctx *ctx) {
+  if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+  if (ctx->graph) cudaGraphDestroy(ctx->graph);
+  ctx->graph_exec = nullptr;
+  ctx->graph = nullptr;
+}
+}  // namespace
+
+namespace sclet {
+// one step of ctx captured on its own stream into the capture that stream is
+// part of (the caller began it)
+int ctx_capture_step(sclet_ctx *ctx) { return sclet_step(ctx, 1); }
+long long ctx_steps_done(const sclet_ctx *ctx) { return ctx->steps_done; }
+}  // namespace sclet
+
+extern "C" {
+
+int sclet_graph_step(sclet_ctx *ctx, int nsteps) {
+  CK(cudaSetDevice(ctx->device));
+  if (nsteps <= 0) return SCLET_OK;
+  if (ctx->profiling) return fail(ctx, SCLET_ERR_ARG, "graph steps are not profiled per stage");
+  if (ctx->steps_done == 0) {
+    // the first step has its own set-up (elastic scratch, launch attributes)
+    int rc = sclet_step(ctx, 1);
+    if (rc != SCLET_OK) return rc;
+    nsteps--;
+  }
+  if (!ctx->graph_exec) {
+    const long long before = ctx->steps_done;
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed));
+    int rc = sclet_step(ctx, 1);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    ctx->steps_done = before;  // captured, not run
+    if (rc != SCLET_OK) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    CK(e);
+    ctx->graph = g;
+    CK(cudaGraphInstantiate(&ctx->graph_exec, ctx->graph, 0));
+  }
+  for (int k = 0; k < nsteps; k++) {
+    CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+    ctx->steps_done++;
+  }
+  return SCLET_OK;
+}
+
+int sclet_tune(sclet_ctx *ctx, int trials, int *choice) {
+  CK(cudaSetDevice(ctx->device));
+  if (!mixed(ctx)) return fail(ctx, SCLET_ERR_UNSUPPORTED, "the autotuner tunes the mixed form");
+  if (trials < 1) trials = 1;
+  if (ctx->steps_done == 0) {
+    int rc = sclet_step(ctx, 1);
+    if (rc != SCLET_OK) return rc;
+  }
+  // the state and the elastic force (whose ghost cells carry over between
+  // steps) are put back after every trial, so tuning changes no result
+  const size_t ub = sizeof(float) * ctx->FT * ctx->n3;
+  const size_t fb = sizeof(float) * (ctx->nac > 0 ? ctx->nac : 1) * ctx->runs * ctx->n3;
+  float *su = nullptr, *sf = nullptr;
+  CK(cudaMalloc(&su, ub));
+  cudaError_t e = cudaMalloc(&sf, fb);
+  if (e != cudaSuccess) {
+    cudaFree(su);
+    CK(e);
+  }
+  CK(cudaMemcpyAsync(su, fu_of(ctx), ub, cudaMemcpyDeviceToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(sf, ctx->ffelas, fb, cudaMemcpyDeviceToDevice, ctx->stream));
+  const int step_diag = ctx->step_diag;
+  auto trial = [&](int zc, int ctas, float *ms) -> int {
+    ctx->ph.rhs_zc = zc;
+    ctx->ph.tc_ctas = ctas;
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    int rc = sclet_step(ctx, 1);  // warm-up of this shape
+    CK(cudaEventRecord(a, ctx->stream));
+    if (rc == SCLET_OK) rc = sclet_step(ctx, trials);
+    CK(cudaEventRecord(b, ctx->stream));
+    CK(cudaEventSynchronize(b));
+    CK(cudaEventElapsedTime(ms, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    ctx->steps_done -= trials + 1;
+    CK(cudaMemcpyAsync(fu_of(ctx), su, ub, cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->ffelas, sf, fb, cudaMemcpyDeviceToDevice, ctx->stream));
+    return rc;
+  };
+  int dev = 0, sms = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  // coordinate search: z-planes per CTA of the RHS, then the persistent CTAs
+  // of the tensor-core products
+  const int zcs[] = {8, 16, 32, 64};
+  const int ctas[] = {sms, sms * 3 / 4, sms / 2};
+  int best_zc = 32, best_ctas = 0, rc = SCLET_OK;
+  float best = 1e30f, ms = 0.0f;
+  for (int zc : zcs) {
+    if ((rc = trial(zc, 0, &ms)) != SCLET_OK) break;
+    if (ms < best) best = ms, best_zc = zc;
+  }
+  best = 1e30f;
+  for (int c : ctas) {
+    if (rc != SCLET_OK) break;
+    if ((rc = trial(best_zc, c, &ms)) != SCLET_OK) break;
+    if (ms < best) best = ms, best_ctas = c;
+  }
+  ctx->step_diag = step_diag;
+  ctx->ph.rhs_zc = best_zc;
+  ctx->ph.tc_ctas = best_ctas;
+  cudaStreamSynchronize(ctx->stream);
+  cudaFree(su);
+  cudaFree(sf);
+  drop_graph(ctx);  // captured launches keep their old shapes
+  if (choice) {
+    choice[0] = best_zc;
+    choice[1] = best_ctas;
+  }
+  return rc;
+}
+
+}  // extern "C"

@@ -30,6 +30,14 @@ struct Phys {
   // exact arithmetic.  It needs a plugin whose c enters only as c - c0
   // (SCLET_C0_INDEX); 0 otherwise and in the FP64 form.
   double cshift;
+  // runs of the same block size held side by side (the batched ensemble):
+  // run r's fields are the F blocks at r F n^3; krun (device, runs values,
+  // or null) replaces plugin constant 0 per run (the Landau a2)
+  int runs;
+  const double *krun;
+  // launch shape chosen by the autotuner (0: the default)
+  int rhs_zc;       // z-planes per CTA of the Allen-Cahn right-hand side
+  int tc_ctas;      // persistent CTAs of the tensor-core products
 };
 
 // Geometry helpers (owned cells are 2 .. n-3 per axis, period N = n - 4).
@@ -93,8 +101,11 @@ cudaError_t launch_ghost_fill(T *u, int count, int n, T *shell, cudaStream_t s);
 // Elastic scratch semantics: felas_p (p in order) gets its ghost cells from
 // the fill of the shared scratch block (see k_halo.cu).  `prev` is the block
 // that was last filled (felas_{p-1}, or the last field of the previous call).
+// runs: blocks side by side, felas_p's at fstride and prev's at pstride
+// apart (0: one prev for all); shell holds runs * shell_count(n) values.
 template <typename T>
-cudaError_t launch_elastic_shell(T *felas_p, const T *prev, int n, T *shell, cudaStream_t s);
+cudaError_t launch_elastic_shell(T *felas_p, const T *prev, int n, T *shell, cudaStream_t s, int runs = 1,
+                                 long long fstride = 0, long long pstride = 0);
 
 // Right-hand sides of all fields into out (F blocks).  felas: nac blocks.
 template <typename T>
@@ -118,11 +129,14 @@ cudaError_t launch_modeprod_f64(const double *M, const double *in, const double 
 // Elastic force (FFT based) -- see k_fft.cu.
 struct ElasticPlan;
 cudaError_t elastic_plan_create(ElasticPlan **plan, int big_n, int nac, const double *voigt,
-                                const double *eps, int fp32, cudaStream_t s);
+                                const double *eps, int fp32, cudaStream_t s, int runs = 1);
 void elastic_plan_destroy(ElasticPlan *plan);
 // felas (nac blocks of n^3) from the AC fields u (first nac blocks).
+// runs (the plan's): run r's order parameters at u + r ustride, its force at
+// felas + r nac n^3; shell holds n^3 + runs * shell_count(n) values
 template <typename T>
-cudaError_t elastic_compute(ElasticPlan *plan, const T *u, T *felas, int n, T *shell, cudaStream_t s);
+cudaError_t elastic_compute(ElasticPlan *plan, const T *u, T *felas, int n, T *shell, cudaStream_t s,
+                            long long ustride = 0);
 
 // Diagnostics: out (F*4 doubles, device) per field max, min, vol, energy.
 template <typename T>

@@ -26,6 +26,7 @@ struct TcArgs {
   const float2 *coef2[2];
   int nac, F;
   int *err;                 // set to 1 when a bounded wait gives up
+  int max_ctas;             // persistent CTAs (0: as many as can be resident)
 };
 
 int tc_kp(int n);

@@ -95,6 +95,8 @@ SIGNATURES = {
     "sclet_field_u16": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
     "sclet_write_field2b": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int, ctypes.c_int]),
     "sclet_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "sclet_create_runs": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                          ctypes.POINTER(ctypes.c_void_p)]),
     "sclet_destroy": (None, [ctypes.c_void_p]),
     "sclet_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
     "sclet_set_eigen": (ctypes.c_int, [ctypes.c_void_p, _c_dp, _c_dp, _c_dp]),
@@ -143,6 +145,14 @@ SIGNATURES = {
     "sclet_learned_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                            ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                            ctypes.c_void_p]),
+    "sclet_graph_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "sclet_tune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "sclet_ensemble_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "sclet_ensemble_destroy": (None, [ctypes.c_void_p]),
+    "sclet_ensemble_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+    "sclet_ensemble_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "sclet_ensemble_sync": (ctypes.c_int, [ctypes.c_void_p]),
+    "sclet_ensemble_time_steps": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
     "sclet_check_soln_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                                                 ctypes.c_void_p, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]),
 }
@@ -209,14 +219,23 @@ def default_params() -> Params:
 class Solver:
     """One device-resident ETD state (a sclet_ctx)."""
 
-    def __init__(self, params: Params, precision: int = FP64, device: int = 0):
+    def __init__(self, params: Params, precision: int = FP64, device: int = 0, runs: int = 1,
+                 krun: Optional[np.ndarray] = None):
+        """runs > 1: that many independent runs side by side (sclet_create_runs),
+        krun their per-run plugin constant 0; arrays then hold runs * F blocks."""
         self.L = lib()
         h = ctypes.c_void_p()
-        rc = self.L.sclet_create(ctypes.byref(params), precision, device, ctypes.byref(h))
+        if runs == 1 and krun is None:
+            rc = self.L.sclet_create(ctypes.byref(params), precision, device, ctypes.byref(h))
+        else:
+            kr = None if krun is None else np.ascontiguousarray(krun, dtype=np.float64)
+            rc = self.L.sclet_create_runs(ctypes.byref(params), runs, None if kr is None else kr.ctypes.data, precision,
+                                          device, ctypes.byref(h))
         if rc != 0:
             raise ScletError(f"sclet_create failed ({rc}): {self.L.sclet_last_error(None).decode()}")
         self.h = h
         self.params = params
+        self.runs = runs
         self.n = self.L.sclet_block_edge(h)
         self.F = self.L.sclet_field_count(h)
         self.nac = params.nac
@@ -300,6 +319,16 @@ class Solver:
     def step(self, k: int = 1):
         self._ck(self.L.sclet_step(self.h, k), "step")
 
+    def graph_step(self, k: int = 1):
+        """k steps replayed from one captured CUDA graph (sclet_graph_step)."""
+        self._ck(self.L.sclet_graph_step(self.h, k), "graph_step")
+
+    def tune(self, trials: int = 3):
+        """Autotuned launch shapes (sclet_tune): (RHS z-planes, tensor-core CTAs)."""
+        c = (ctypes.c_int * 2)()
+        self._ck(self.L.sclet_tune(self.h, trials, c), "tune")
+        return c[0], c[1]
+
     def sync(self):
         self._ck(self.L.sclet_sync(self.h), "sync")
 
@@ -368,3 +397,45 @@ class Solver:
 
     def launch_count(self) -> int:
         return int(self.L.sclet_launch_count(self.h))
+
+
+class Ensemble:
+    """Contexts advanced together by one captured graph (sclet_ensemble_*)."""
+
+    def __init__(self, solvers: List["Solver"]):
+        self.L = lib()
+        self.solvers = solvers
+        arr = (ctypes.c_void_p * len(solvers))(*[s.h.value for s in solvers])
+        h = ctypes.c_void_p()
+        rc = self.L.sclet_ensemble_create(arr, len(solvers), ctypes.byref(h))
+        self.h = h
+        if rc != 0:
+            msg = self.L.sclet_ensemble_last_error(h).decode() if h else ""
+            self.close()
+            raise ScletError(f"sclet_ensemble_create failed ({rc}): {msg}")
+
+    def _ck(self, rc, what):
+        if rc != 0:
+            raise ScletError(f"{what} failed ({rc}): {self.L.sclet_ensemble_last_error(self.h).decode()}")
+
+    def step(self, k: int = 1):
+        self._ck(self.L.sclet_ensemble_step(self.h, k), "ensemble_step")
+
+    def sync(self):
+        self._ck(self.L.sclet_ensemble_sync(self.h), "ensemble_sync")
+
+    def time_steps(self, k: int) -> float:
+        ms = ctypes.c_float()
+        self._ck(self.L.sclet_ensemble_time_steps(self.h, k, ctypes.byref(ms)), "ensemble_time_steps")
+        return ms.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.sclet_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -154,6 +154,17 @@ int sclet_write_vtk_file(const char *path, int istep, int n, int nfields, const 
  * ac_init_phi/ch_init_phi (vars.c:302-359) and elastic_init (elastic.c:607)
  * on device `device`.  Fields start at zero. */
 int sclet_create(const sclet_params *p, int precision, int device, sclet_ctx **out);
+/* No counterpart in the reference (one run per process there): `runs`
+ * independent runs of the same parameters and block size side by side in one
+ * context (the batched ensemble), each with its own state and, when krun is
+ * not NULL, its own value krun[r] of plugin constant 0 (the Landau a2).
+ * Every stage is one launch over all runs.  Run r's fields are the blocks
+ * r F .. r F + F - 1 of the host arrays of sclet_set_fields /
+ * sclet_get_fields, and of sclet_check_soln's output; sclet_field_count gives
+ * runs F.  runs > 1 needs SCLET_MIXED and nch = 0; per-field accessors then
+ * return SCLET_ERR_UNSUPPORTED. */
+int sclet_create_runs(const sclet_params *p, int runs, const double *krun, int precision, int device,
+                      sclet_ctx **out);
 /* dealloc_vars (vars.c:593-732), elastic_finish (elastic.c:276-300) */
 void sclet_destroy(sclet_ctx *ctx);
 /* Last error message of this context (or of the last failed create). */
@@ -162,7 +173,8 @@ const char *sclet_last_error(const sclet_ctx *ctx);
  * basis, as read_matrices does for nx = ny = nz): d (n, unscaled; divided by
  * h^2 here as vars.c:512 does), v and vi row-major n x n. */
 int sclet_set_eigen(sclet_ctx *ctx, const double *d, const double *v, const double *vi);
-/* Block edge n, field count, and the CUDA stream the context runs on. */
+/* Block edge n, field count (of every run), and the CUDA stream the context
+ * runs on. */
 int sclet_block_edge(const sclet_ctx *ctx);
 int sclet_field_count(const sclet_ctx *ctx);
 void *sclet_stream(const sclet_ctx *ctx);
@@ -278,6 +290,32 @@ int sclet_time_steps(sclet_ctx *ctx, int nsteps, float *ms);
  * launches[k] kernel launches.  Up to 8 classes. */
 int sclet_set_profiling(sclet_ctx *ctx, int on);
 int sclet_stage_times(const sclet_ctx *ctx, float *ms, int *launches, int nclasses);
+/* No counterpart in the reference.  sclet_step's work captured once as a
+ * CUDA graph (on the first call; a context that has not stepped yet takes
+ * its first step uncaptured) and replayed nsteps times on the context's
+ * stream: the same launches with the host's launch cost paid once. */
+int sclet_graph_step(sclet_ctx *ctx, int nsteps);
+/* No counterpart in the reference.  Autotuner of the mixed form's launch
+ * shapes: times `trials` steps of each candidate (z-planes per CTA of the
+ * Allen-Cahn right-hand side: 8, 16, 32, 64; then persistent CTAs of the
+ * tensor-core products: all SMs, 3/4, 1/2), keeps the fastest and puts the
+ * state back after every trial, so results do not change.  choice (2 ints,
+ * may be NULL) receives the z-planes and the CTA count (0: all SMs). */
+int sclet_tune(sclet_ctx *ctx, int trials, int *choice);
+/* The batched ensemble (no counterpart in the reference): contexts of
+ * several block sizes (each holding its runs side by side) advanced
+ * together; sclet_ensemble_step captures one step of all of them as one
+ * CUDA graph, one branch per context on the context's stream, and replays
+ * it (contexts that have not stepped yet take one uncaptured step first).
+ * The contexts stay owned by the caller and must outlive the ensemble. */
+typedef struct sclet_ensemble sclet_ensemble;
+int sclet_ensemble_create(sclet_ctx *const *ctxs, int count, sclet_ensemble **out);
+void sclet_ensemble_destroy(sclet_ensemble *e);
+const char *sclet_ensemble_last_error(const sclet_ensemble *e);
+int sclet_ensemble_step(sclet_ensemble *e, int nsteps);
+int sclet_ensemble_sync(sclet_ensemble *e);
+/* nsteps ensemble steps between two CUDA events; elapsed milliseconds. */
+int sclet_ensemble_time_steps(sclet_ensemble *e, int nsteps, float *ms);
 /* Kernel launches issued by this context so far. */
 long long sclet_launch_count(const sclet_ctx *ctx);
 /* Page-locked host buffers for the field blocks (no reference counterpart:
