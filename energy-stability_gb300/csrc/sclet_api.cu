@@ -1334,3 +1334,52 @@ int sclet_tune(sclet_ctx *ctx, int trials, int *choice) {
 }
 
 }  // extern "C"
+
+// ---- FP64 issue rate of the device (the bound of the plain form's stages) ----
+namespace {
+// eight independent FMA chains per thread; the result is stored so the
+// chains are not removed
+__global__ void fp64_fma_kernel(double *out, int iters, double a, double b) {
+  double x[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) x[k] = threadIdx.x * 1e-9 + k;
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int k = 0; k < 8; k++) x[k] = fma(x[k], a, b);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) s += x[k];
+  if (s == 12345.678) out[0] = s;  // never true for these inputs; keeps the work
+}
+}  // namespace
+
+extern "C" int sclet_measure_fp64_rate(int device, double *tflops) {
+  if (!tflops) return SCLET_ERR_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return SCLET_ERR_CUDA;
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return SCLET_ERR_CUDA;
+  double *out = nullptr;
+  if (cudaMalloc(&out, sizeof(double)) != cudaSuccess) return SCLET_ERR_NOMEM;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  const int blocks = sms * 8, threads = 256, iters = 4096;
+  float best = 1e30f;
+  for (int rep = 0; rep < 4; rep++) {
+    cudaEventRecord(a);
+    fp64_fma_kernel<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
+    cudaEventRecord(b);
+    cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    if (rep > 0 && ms < best) best = ms;  // the first launch warms up
+  }
+  cudaError_t e = cudaGetLastError();
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(out);
+  if (e != cudaSuccess) return SCLET_ERR_CUDA;
+  *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
+  return SCLET_OK;
+}

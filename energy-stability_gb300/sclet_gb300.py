@@ -145,6 +145,7 @@ SIGNATURES = {
     "sclet_learned_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                            ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                            ctypes.c_void_p]),
+    "sclet_measure_fp64_rate": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "sclet_graph_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "sclet_tune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "sclet_ensemble_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
@@ -208,6 +209,15 @@ def read_case(case_dir: str, suffix: str) -> Params:
     if rc != 0:
         raise ScletError(f"sclet_read_case({case_dir}, {suffix}) failed with status {rc}")
     return p
+
+
+def fp64_rate(device: int = 0) -> float:
+    """Measured FP64 FMA rate of the device in TFLOP/s (sclet_measure_fp64_rate)."""
+    t = ctypes.c_double()
+    rc = lib().sclet_measure_fp64_rate(device, ctypes.byref(t))
+    if rc != 0:
+        raise ScletError(f"sclet_measure_fp64_rate failed ({rc})")
+    return t.value
 
 
 def default_params() -> Params:

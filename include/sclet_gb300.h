@@ -316,6 +316,10 @@ int sclet_ensemble_step(sclet_ensemble *e, int nsteps);
 int sclet_ensemble_sync(sclet_ensemble *e);
 /* nsteps ensemble steps between two CUDA events; elapsed milliseconds. */
 int sclet_ensemble_time_steps(sclet_ensemble *e, int nsteps, float *ms);
+/* No counterpart in the reference.  The device's FP64 fused multiply-add
+ * rate in TFLOP/s (eight independent chains per thread on every SM, best of
+ * three timed launches): the roofline of the plain form's FP64-bound stages. */
+int sclet_measure_fp64_rate(int device, double *tflops);
 /* Kernel launches issued by this context so far. */
 long long sclet_launch_count(const sclet_ctx *ctx);
 /* Page-locked host buffers for the field blocks (no reference counterpart:
