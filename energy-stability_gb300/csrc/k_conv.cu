@@ -47,7 +47,10 @@ using tc::smem_u32;
 using tc::tmem_ld32;
 
 constexpr int ROWS = 128;                  // cells per tile (MMA M)
-constexpr int STAGES = 8;                  // tap tiles in flight
+// tap tiles in flight: the loads come mostly from L2, and the pipeline is
+// bound by the bytes in flight per SM (eight stages kept the tensor pipe 6%
+// busy), so every stage the shared memory holds beside the weights
+constexpr int STAGES = 20;
 constexpr int ATILE = ROWS * CH * 2;       // 8 KB: 128 cells x 32 channels
 constexpr int WTILE = CH * CH * 2;         // 2 KB: one tap's 32 x 32 weights
 constexpr int NACC = 4;                    // TMEM accumulators of 32 columns
