@@ -1089,8 +1089,28 @@ int sclet_sync(sclet_ctx *ctx) {
   int e = 0;
   CK(cudaMemcpyAsync(&e, ctx->dev_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
-  if (e) return fail(ctx, SCLET_ERR_TIMEOUT, "a bounded device wait gave up (tensor-core pipeline)");
+  if (e) {
+    // reported once: the flag starts clear again for the next work
+    CK(cudaMemsetAsync(ctx->dev_err, 0, sizeof(int), ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return fail(ctx, SCLET_ERR_TIMEOUT, "a bounded device wait gave up (tensor-core pipeline)");
+  }
   return SCLET_OK;
+}
+
+int sclet_selftest_wait_timeout(sclet_ctx *ctx) {
+  CK(cudaSetDevice(ctx->device));
+  if (!mixed(ctx)) return fail(ctx, SCLET_ERR_UNSUPPORTED, "the self-test runs the tensor-core product (mixed form)");
+  int rc = sclet_sync(ctx);
+  if (rc != SCLET_OK) return rc;
+  // one product whose producer issues no loads: the MMA and epilogue warps
+  // wait on barriers nothing arrives on, give up, record the error, free
+  // their tensor memory and return
+  TcArgs g = tc_args(ctx, false, 1, ctx->W1, 0, nullptr, 1);
+  g.in_scale = ctx->scaleP;
+  g.idle = 1;
+  CK(launch_modeprod_tc(ctx->matVi, ctx->P, 1, g, ctx->stream));
+  return sclet_sync(ctx);
 }
 
 int sclet_set_profiling(sclet_ctx *ctx, int on) {

@@ -27,6 +27,7 @@ struct TcArgs {
   int nac, F;
   int *err;                 // set to 1 when a bounded wait gives up
   int max_ctas;             // persistent CTAs (0: as many as can be resident)
+  int idle;                 // 1: the producer issues no loads (the bounded-wait self-test)
 };
 
 int tc_kp(int n);

@@ -145,6 +145,7 @@ SIGNATURES = {
     "sclet_learned_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                            ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                            ctypes.c_void_p]),
+    "sclet_selftest_wait_timeout": (ctypes.c_int, [ctypes.c_void_p]),
     "sclet_measure_fp64_rate": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "sclet_graph_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "sclet_tune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),

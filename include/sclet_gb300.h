@@ -278,6 +278,8 @@ int sclet_get_felas(sclet_ctx *ctx, int m, double *block);
 int sclet_mode_product(sclet_ctx *ctx, int inverse, const double *in, double *out);
 
 /* ---- synchronisation and timing ---------------------------------------- */
+/* Waits for the context's work; SCLET_ERR_TIMEOUT when a bounded device wait
+ * gave up since the last call (reported once, then cleared). */
 int sclet_sync(sclet_ctx *ctx);
 /* Runs `nsteps` steps between two CUDA events on the context's stream and
  * returns the elapsed milliseconds. */
@@ -316,6 +318,14 @@ int sclet_ensemble_step(sclet_ensemble *e, int nsteps);
 int sclet_ensemble_sync(sclet_ensemble *e);
 /* nsteps ensemble steps between two CUDA events; elapsed milliseconds. */
 int sclet_ensemble_time_steps(sclet_ensemble *e, int nsteps, float *ms);
+/* No counterpart in the reference.  Self-test of the bounded device waits
+ * (mixed form): one tensor-core product launch whose producer issues no
+ * loads, so its MMA and epilogue warps wait on barriers that nothing arrives
+ * on until their poll limit (about half a second), then record the error, free
+ * their tensor memory and return.  Returns what sclet_sync reports:
+ * SCLET_ERR_TIMEOUT when the waits gave up as they must; the error is then
+ * cleared and the context stays usable (the state is not touched). */
+int sclet_selftest_wait_timeout(sclet_ctx *ctx);
 /* No counterpart in the reference.  The device's FP64 fused multiply-add
  * rate in TFLOP/s (eight independent chains per thread on every SM, best of
  * three timed launches): the roofline of the plain form's FP64-bound stages. */

@@ -209,3 +209,27 @@ def test_mixed_matches_fp64_reference_formula(sclet_lib):
     errs, eerr = _mixed_vs_fp64(sclet_lib, case, 100)
     assert max(errs) <= 1e-5, errs
     assert eerr <= 1e-6, eerr
+
+
+def test_bounded_wait_gives_up_and_is_reported(sclet_lib):
+    """A tensor-core launch whose barriers receive nothing (no copy is issued)
+    gives up after its poll limit instead of hanging: the status is
+    SCLET_ERR_TIMEOUT, reported once, and the context steps on unchanged."""
+    sg = sclet_lib
+    case = bench.workload(32, seed=23)
+    p = params_for(sg, case)
+    u0 = bench.block_fields(case)
+    s = sg.Solver(p, sg.MIXED)
+    s.set_fields(u0)
+    s.step(1)
+    rc = s.L.sclet_selftest_wait_timeout(s.h)
+    assert rc == 6, (rc, s.L.sclet_last_error(s.h))  # SCLET_ERR_TIMEOUT
+    assert b"bounded" in s.L.sclet_last_error(s.h)
+    assert s.L.sclet_sync(s.h) == 0
+    s.step(3)
+    ref = sg.Solver(p, sg.MIXED)
+    ref.set_fields(u0)
+    ref.step(4)
+    np.testing.assert_array_equal(s.get_fields(), ref.get_fields())
+    s.close()
+    ref.close()
