@@ -510,6 +510,152 @@ __global__ void __launch_bounds__(256, 2) energy_partial_f32(Phys ph, EConst ec,
   block_record_from_warps(mxd, mnd, vol, eac, ech, F, part);
 }
 
+// ---- FP64 states: the same z-marching form in FP64 -------------------------
+//
+// The column tile and the plane walk of energy_partial_f32, with FP64 values
+// and compensated FP64 (TwoSum) running sums.  Two loads per field and cell
+// instead of eight.
+template <typename PL, int NAC, int NCH>
+__global__ void __launch_bounds__(256, 1) energy_partial_f64z(Phys ph, const double *__restrict__ u,
+                                                              const double *__restrict__ elam, int form,
+                                                              double *__restrict__ part) {
+  constexpr int F = NAC + NCH;
+  const int n = ph.n, N = n - 4;
+  const long long n3 = (long long)n * n * n;
+  __shared__ double q6[4][6];  // half epn2 times the symmetrised gradient tensors: xx yy zz xy xz yz
+  if (threadIdx.x < 4 * 6 && threadIdx.y == 0) {
+    const int m = threadIdx.x / 6, c = threadIdx.x % 6;
+    const double *L = elam + 9 * m;
+    const double v = c == 0 ? L[0] : c == 1 ? L[4] : c == 2 ? L[8] : c == 3 ? L[1] + L[3] : c == 4 ? L[2] + L[6] : L[5] + L[7];
+    q6[m][c] = 0.5 * ph.epn2 * v;
+  }
+  __syncthreads();
+  const double i4hx = 0.25 / ph.h[0], i4hy = 0.25 / ph.h[1], i4hz = 0.25 / ph.h[2], half_epn2 = 0.5 * ph.epn2;
+  double Kt[16];
+#pragma unroll
+  for (int k = 0; k < 16; k++) Kt[k] = ph.K[k];
+  const double p2 = 2376.0 / 2372.0 / 2.0, p3 = (7128.0 + 12.0 * 2372.0) / 2372.0 / 3.0,
+               p4 = (4752.0 + 12.0 * 2372.0) / 2372.0 / 4.0;
+  double mx[F], mn[F];
+  KS vsum[F], eac = {0.0, 0.0}, ech = {0.0, 0.0};
+  long long cnt = 0;
+#pragma unroll
+  for (int f = 0; f < F; f++) {
+    mx[f] = -1.0e30;
+    mn[f] = 1.0e30;
+    vsum[f] = KS{0.0, 0.0};
+  }
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int nti = (N + 31) / 32, ntj = (N + 7) / 8, units = energy_units(N);
+  for (int unit = blockIdx.x; unit < units; unit += gridDim.x) {
+    const int ti = unit % nti, tj = (unit / nti) % ntj, zc = unit / (nti * ntj);
+    const int i = 2 + ti * 32 + tx, j = 2 + tj * 8 + ty;
+    const bool own = i <= n - 3 && j <= n - 3, inner = i <= n - 4 && j <= n - 4;
+    const int ic = i < n - 2 ? i : n - 2, jc = j < n - 2 ? j : n - 2;
+    const int k0 = 2 + zc * EZ, k1 = k0 + EZ < n - 2 ? k0 + EZ : n - 2;
+    double a0[F], a1[F], a2[F], a3[F];
+    const long long row0 = ((long long)k0 * n + jc) * n + ic;
+#pragma unroll
+    for (int f = 0; f < F; f++) {
+      const double *q = u + f * n3 + row0;
+      a0[f] = q[0];
+      a2[f] = q[n];
+      a1[f] = __shfl_down_sync(0xffffffffu, a0[f], 1);
+      a3[f] = __shfl_down_sync(0xffffffffu, a2[f], 1);
+      if (tx == 31) {
+        a1[f] = q[1];
+        a3[f] = q[n + 1];
+      }
+    }
+    for (int k = k0; k < k1; k++) {
+      double b0[F], b1[F], b2[F], b3[F];
+      const long long row = ((long long)(k + 1) * n + jc) * n + ic;
+#pragma unroll
+      for (int f = 0; f < F; f++) {
+        const double *q = u + f * n3 + row;
+        b0[f] = q[0];
+        b2[f] = q[n];
+        b1[f] = __shfl_down_sync(0xffffffffu, b0[f], 1);
+        b3[f] = __shfl_down_sync(0xffffffffu, b2[f], 1);
+        if (tx == 31) {
+          b1[f] = q[1];
+          b3[f] = q[n + 1];
+        }
+      }
+      if (own) {
+        cnt++;
+#pragma unroll
+        for (int f = 0; f < F; f++) {
+          mx[f] = fmax(mx[f], a0[f]);
+          mn[f] = fmin(mn[f], a0[f]);
+          ks_add(vsum[f], a0[f]);
+        }
+      }
+      if (inner && k <= n - 4) {
+        double avg[F > 0 ? F : 1];
+        double e_ac = 0.0, e_ch = 0.0, cbar = 0.0;
+#pragma unroll
+        for (int f = 0; f < F; f++) {
+          const double v0 = a0[f], v1 = a1[f], v2 = a2[f], v3 = a3[f], v4 = b0[f], v5 = b1[f], v6 = b2[f],
+                       v7 = b3[f];
+          avg[f] = (v0 + v1 + v2 + v3 + v4 + v5 + v6 + v7) * 0.125;
+          const double ux = ((v1 - v0) + (v3 - v2) + (v5 - v4) + (v7 - v6)) * i4hx;
+          const double uy = ((v2 - v0) + (v3 - v1) + (v6 - v4) + (v7 - v5)) * i4hy;
+          const double uz = ((v4 - v0) + (v5 - v1) + (v6 - v2) + (v7 - v3)) * i4hz;
+          if (f < NAC) {
+            const double *qm = q6[f];
+            e_ac += qm[0] * ux * ux + qm[1] * uy * uy + qm[2] * uz * uz + qm[3] * ux * uy + qm[4] * ux * uz +
+                    qm[5] * uy * uz;
+          } else {
+            const double gr = half_epn2 * (ux * ux + uy * uy + uz * uz);
+            if (form == 0) e_ch += gr;
+            else e_ac += gr;
+            cbar = avg[f];
+          }
+        }
+        if (form == 0) {
+          if (NAC > 0) {
+            double s2 = 0.0, s3 = 0.0;
+#pragma unroll
+            for (int f = 0; f < (NAC < 4 ? NAC : 4); f++) {
+              s2 += avg[f] * avg[f];
+              s3 += avg[f] * avg[f] * avg[f];
+            }
+            e_ac += p2 * s2 - p3 * s3 + p4 * s2 * s2;
+          }
+          if (NCH > 0) e_ch += (cbar * cbar - 1.0) * (cbar * cbar - 1.0) * 0.25;
+        } else {
+          sclet_acv<double> ac[NAC > 0 ? NAC : 1];
+          sclet_chv<double> ch[1];
+#pragma unroll
+          for (int m = 0; m < NAC; m++) ac[m].u = avg[m];
+          ch[0].c = cbar;
+          e_ac += PL::template f_bulk<double>(ac, ch, NAC, NCH, Kt);
+        }
+        ks_add(eac, e_ac);
+        ks_add(ech, e_ch);
+      }
+#pragma unroll
+      for (int f = 0; f < F; f++) {
+        a0[f] = b0[f];
+        a1[f] = b1[f];
+        a2[f] = b2[f];
+        a3[f] = b3[f];
+      }
+    }
+  }
+  double mxd[MAXF], mnd[MAXF];
+  KS vol[MAXF];
+#pragma unroll
+  for (int f = 0; f < MAXF; f++) {
+    mxd[f] = f < F ? mx[f < F ? f : 0] : -1.0e30;
+    mnd[f] = f < F ? mn[f < F ? f : 0] : 1.0e30;
+    vol[f] = f < F ? vsum[f < F ? f : 0] : KS{0.0, 0.0};
+    ks_add(vol[f], (double)cnt);  // sum of (value + 1)
+  }
+  block_record(mxd, mnd, vol, eac, ech, F, part);
+}
+
 // Final reduction over the block records: one warp per quantity (per field
 // max, min, vol; the two energies); each lane folds a fixed strided subset of
 // the records, then a butterfly (deterministic).
@@ -585,7 +731,16 @@ static cudaError_t check_soln_pl(const Phys &ph, const T *u, const double *elam,
       default: launch_f32<PL, 4, 1>(ph, uf, elam, form, partials, npart, s); break;
     }
   } else {
-    energy_partial_kernel<PL, T><<<npart, EB, 0, s>>>(ph, u, elam, form, partials);
+    const double *ud = u;
+    const dim3 g(npart), b(32, 8);
+    switch (ph.nac * 2 + ph.nch) {
+#define SCLET_F64Z(NA, NC) \
+  case NA * 2 + NC: energy_partial_f64z<PL, NA, NC><<<g, b, 0, s>>>(ph, ud, elam, form, partials); break;
+      SCLET_F64Z(0, 1) SCLET_F64Z(1, 0) SCLET_F64Z(1, 1) SCLET_F64Z(2, 0) SCLET_F64Z(2, 1)
+      SCLET_F64Z(3, 0) SCLET_F64Z(3, 1) SCLET_F64Z(4, 0) SCLET_F64Z(4, 1)
+#undef SCLET_F64Z
+      default: energy_partial_kernel<PL, T><<<npart, EB, 0, s>>>(ph, u, elam, form, partials);
+    }
   }
   return cudaGetLastError();
 }
