@@ -290,16 +290,16 @@ def tc_roofline(case, stage_ms, stage_launches, steps):
     """Roofline of the tensor-core mode-n product kernel over `steps` profiled
     steps.  Per tensor-product (n x n matrix times an n^3 tensor): algorithmic
     flops 2 n^4; bytes the kernel must move given its interface: the four BF16
-    slice planes of the input (8 B per element over kp = roundup(n, 8)
-    columns) and the FP32 output (4 B per element); the fused ETD update of one
+    slice planes of the input (8 B per element; the kernel also reads the zero
+    columns up to the next multiple of 32, not counted) and the FP32 output
+    (4 B per element); the fused ETD update of one
     product in nine also reads the other operand (4 B) and the coefficient
     pairs (16 B).  Physical MMA work: eleven BF16 MMAs over 128-row tiles."""
     n, F = case.n, case.nac + case.nch
-    kp = (n + 7) // 8 * 8
     kk = (n + 31) // 32 * 32
     per_step_products = 9 * F
     elems = n ** 3
-    bytes_step = per_step_products * elems * (8.0 * kp / n + 4.0) + F * elems * 20.0
+    bytes_step = per_step_products * elems * (8.0 + 4.0) + F * elems * 20.0
     flops_step = per_step_products * 2.0 * n ** 4
     a_pad = (n + 127) // 128 * 128
     r_pad = (n * n + 127) // 128 * 128

@@ -25,8 +25,11 @@
 // outlier costs precision only within itself.  The scale of an output entry
 // is rank one (matrix row a' times input row r), so accumulation stays exact.
 //
-// Layout: input planes P[t][p][r][k], rows r = 0 .. n*n-1 of kp = roundup(n, 8)
-// BF16 values (one 1-D line along the contracted axis per row).  Output FP32
+// Layout: input planes P[t][p][kb][r][32], k-blocked: rows r = 0 .. n*n-1 are
+// 1-D lines along the contracted axis, k = 32 kb + (k % 32) < kp = roundup(n,
+// 32), zero beyond n; one k-block of 128 consecutive rows is one contiguous
+// 8 KB tile, so every TMA load reads whole 128-byte lines.  Matrix slices
+// likewise [p][kb][a'][32].  Output FP32
 // out[t][a' * n*n + r] for input row r = c * n + b, i.e. contracted index
 // slowest: three products return to x-fastest order.
 //
@@ -126,10 +129,12 @@ __global__ void __launch_bounds__(THREADS, 1)
           if (*(volatile int *)&failed) break;
           uint8_t *st = base + s * STAGE_BYTES;
           mbar_expect_tx(&full_bar[s], STAGE_BYTES);
+          // k-block kb of plane z is the contiguous block z * nkb + kb
           for (int p = 0; p < NPM; p++)
-            tma_load_3d(st + p * PLANE_A, &tmA, kb * BK, ti.a_tile * BM, p, &full_bar[s]);
+            tma_load_3d(st + p * PLANE_A, &tmA, 0, ti.a_tile * BM, p * nkb + kb, &full_bar[s]);
           for (int p = 0; p < NP; p++)
-            tma_load_3d(st + NPM * PLANE_A + p * PLANE_B, &tmB, kb * BK, ti.r_tile * BN, ti.t * NP + p, &full_bar[s]);
+            tma_load_3d(st + NPM * PLANE_A + p * PLANE_B, &tmB, 0, ti.r_tile * BN, (ti.t * NP + p) * nkb + kb,
+                        &full_bar[s]);
         }
         if (*(volatile int *)&failed) break;
       }
@@ -317,85 +322,79 @@ __global__ void __launch_bounds__(THREADS, 1)
 }
 
 
-// FP32 rows of n (x - sub) -> slices, one warp per row: the row's max gives its
-// power-of-two scale S; each slice is exact (the residual is scaled by 2^b and
-// reduced by its nearest integer).
-constexpr int SLICE_MAXC = 17;  // column pairs per lane: rows of up to 32 * 2 * 17 = 1088 values
+// FP32 rows of n (x - sub) -> slices: the row's max gives its power-of-two
+// scale S; each slice is exact (the residual is scaled by 2^b and reduced by
+// its nearest integer).
+constexpr int SLICE_MAXC = 34;  // 32-column chunks per row: rows of up to 32 * 34 = 1088 values
 
-// C = column-pair chunks per lane held in registers (C >= ceil(n / 64)).  A
-// warp takes two adjacent rows at a time (both rows' loads in flight before
-// either is reduced); pairs of columns load as float2 when n is even.
+// A warp takes two adjacent rows, one per half-warp (lane l: row l / 16,
+// columns 2 (l % 16) + 32 c of chunk c, held in registers, C >= ceil(n / 32)).
+// In the k-blocked layout the two rows' k-block c is one contiguous 128-byte
+// run, so every store instruction of the warp fills whole lines.  Columns
+// load as float2 when n is even.
 template <int C>
 __global__ void __launch_bounds__(256) slice_fields_kernel(const float *__restrict__ x, const float *__restrict__ sub,
                                                            float *__restrict__ scale, __nv_bfloat16 *__restrict__ out,
                                                            int n, int kp, int count, int bits) {
   const float step = ldexpf(1.0f, bits);
   const long long rows = (long long)n * n, total_rows = rows * count;
-  const int lane = threadIdx.x & 31;
-  const int chunks = (n + 63) / 64;
+  const int lane = threadIdx.x & 31, h = lane >> 4, kl = 2 * (lane & 15);
+  const int chunks = (n + BK - 1) / BK;
   const bool pairs = (n & 1) == 0;  // every row starts on an 8-byte boundary
   const long long warp0 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   for (long long w0 = 2 * warp0; w0 < total_rows; w0 += 2 * nwarps) {
-    // the two lines in registers (one read each), two columns per lane and chunk
-    float v0[2][C], v1[2][C];
-    float m[2] = {0.0f, 0.0f};
+    const long long wr = w0 + h;
+    const bool live = wr < total_rows;
+    const long long in0 = wr * n;  // rows are contiguous lines of n
+    float v0[C], v1[C];
+    float m = 0.0f;
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
-      const long long wr = w0 + h;
-      const long long in0 = wr * n;  // rows are contiguous lines of n
-#pragma unroll
-      for (int c = 0; c < C; c++) {
-        v0[h][c] = 0.0f;
-        v1[h][c] = 0.0f;
-        const int k = 2 * lane + 64 * c;
-        if (wr < total_rows && c < chunks && k < n) {
-          if (pairs) {
-            float2 a = *reinterpret_cast<const float2 *>(x + in0 + k);
-            if (sub) {
-              const float2 b = *reinterpret_cast<const float2 *>(sub + in0 + k);
-              a.x -= b.x;
-              a.y -= b.y;
-            }
-            v0[h][c] = a.x;
-            v1[h][c] = a.y;
-          } else {
-            v0[h][c] = sub ? x[in0 + k] - sub[in0 + k] : x[in0 + k];
-            if (k + 1 < n) v1[h][c] = sub ? x[in0 + k + 1] - sub[in0 + k + 1] : x[in0 + k + 1];
+    for (int c = 0; c < C; c++) {
+      v0[c] = 0.0f;
+      v1[c] = 0.0f;
+      const int k = kl + BK * c;
+      if (live && c < chunks && k < n) {
+        if (pairs) {
+          float2 a = *reinterpret_cast<const float2 *>(x + in0 + k);
+          if (sub) {
+            const float2 b = *reinterpret_cast<const float2 *>(sub + in0 + k);
+            a.x -= b.x;
+            a.y -= b.y;
           }
+          v0[c] = a.x;
+          v1[c] = a.y;
+        } else {
+          v0[c] = sub ? x[in0 + k] - sub[in0 + k] : x[in0 + k];
+          if (k + 1 < n) v1[c] = sub ? x[in0 + k + 1] - sub[in0 + k + 1] : x[in0 + k + 1];
         }
-        m[h] = fmaxf(m[h], fmaxf(fabsf(v0[h][c]), fabsf(v1[h][c])));
       }
+      m = fmaxf(m, fmaxf(fabsf(v0[c]), fabsf(v1[c])));
     }
+    // the row's max over its half-warp
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      m[0] = fmaxf(m[0], __shfl_xor_sync(0xffffffffu, m[0], off));
-      m[1] = fmaxf(m[1], __shfl_xor_sync(0xffffffffu, m[1], off));
-    }
+    for (int off = 8; off > 0; off >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
+    if (!live) continue;
+    const int t = (int)(wr / rows);
+    const long long row = wr - (long long)t * rows;
+    const float S = pow2_scale(m), inv = 1.0f / S;
+    if (kl == 0) scale[wr] = S;
+    const long long o0 = (long long)t * TC_PLANES * rows * kp + row * BK + kl;
+    // stored as bf16 pairs (the pad columns n .. kp - 1 are never written:
+    // they stay zero from the allocation)
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
-      const long long wr = w0 + h;
-      if (wr >= total_rows) break;
-      const int t = (int)(wr / rows);
-      const long long row = wr - (long long)t * rows;
-      const float S = pow2_scale(m[h]), inv = 1.0f / S;
-      if (lane == 0) scale[wr] = S;
-      const long long o0 = ((long long)t * TC_PLANES * rows + row) * kp;
-      // stored as bf16 pairs (kp is even; a pad column beyond n receives zero
-      // slices)
+    for (int c = 0; c < C; c++) {
+      const int k = kl + BK * c;
+      if (c < chunks && k < n) {
+        float r0 = v0[c] * inv, r1 = v1[c] * inv;
 #pragma unroll
-      for (int c = 0; c < C; c++) {
-        const int k = 2 * lane + 64 * c;
-        if (c < chunks && k < n) {
-          float r0 = v0[h][c] * inv, r1 = v1[h][c] * inv;
-#pragma unroll
-          for (int p = 0; p < TC_PLANES; p++) {
-            const float y0 = r0 * step, y1 = r1 * step;
-            const float d0 = rintf(y0), d1 = rintf(y1);
-            r0 = y0 - d0;
-            r1 = y1 - d1;
-            *reinterpret_cast<__nv_bfloat162 *>(out + o0 + (long long)p * rows * kp + k) = __floats2bfloat162_rn(d0, d1);
-          }
+        for (int p = 0; p < TC_PLANES; p++) {
+          const float y0 = r0 * step, y1 = r1 * step;
+          const float d0 = rintf(y0), d1 = rintf(y1);
+          r0 = y0 - d0;
+          r1 = y1 - d1;
+          *reinterpret_cast<__nv_bfloat162 *>(out + o0 + (long long)p * rows * kp + (long long)c * rows * BK) =
+              __floats2bfloat162_rn(d0, d1);
         }
       }
     }
@@ -432,7 +431,7 @@ __global__ void slice_matrix_kernel(const double *__restrict__ m, __nv_bfloat16 
         v = y - d;
         // the fifth slice enters class 3, one factor 2^b below its own weight
         float q = p < TC_PLANES ? (float)d : (float)(d / step);
-        out[((long long)p * n + r) * kp + c] = __float2bfloat16_rn(q);
+        out[(long long)p * n * kp + (long long)(c / BK) * n * BK + r * BK + c % BK] = __float2bfloat16_rn(q);
       }
     }
   }
@@ -483,7 +482,7 @@ __global__ void coef_kernel(float4 *coef, float2 *coef2, int n, int kind, const 
 
 // ---- host side ------------------------------------------------------------
 
-int tc_kp(int n) { return (n + 7) / 8 * 8; }
+int tc_kp(int n) { return (n + tc::BK - 1) / tc::BK * tc::BK; }
 
 // Slice width: classes 0 and 1 stay exact while K 2^(2b) <= 2^24, K the
 // contraction length rounded up to whole k-blocks.
@@ -500,14 +499,14 @@ cudaError_t tc_slice_matrix(const double *m, __nv_bfloat16 *planes, float *row_s
 
 cudaError_t tc_slice_fields(const float *x, const float *sub, float *scale, __nv_bfloat16 *planes, int n, int count,
                             cudaStream_t s) {
-  if (n > 64 * tc::SLICE_MAXC) return cudaErrorInvalidValue;
+  if (n > tc::BK * tc::SLICE_MAXC) return cudaErrorInvalidValue;
   long long warps = ((long long)n * n * count + 1) / 2;  // two rows per warp
   long long blocks = (warps * 32 + 255) / 256;
   int g = (int)(blocks > 152 * 32 ? 152 * 32 : blocks);
-  const int chunks = (n + 63) / 64, kp = tc_kp(n), bits = tc_slice_bits(n);
-  if (chunks <= 2) tc::slice_fields_kernel<2><<<g, 256, 0, s>>>(x, sub, scale, planes, n, kp, count, bits);
-  else if (chunks <= 4) tc::slice_fields_kernel<4><<<g, 256, 0, s>>>(x, sub, scale, planes, n, kp, count, bits);
+  const int chunks = (n + tc::BK - 1) / tc::BK, kp = tc_kp(n), bits = tc_slice_bits(n);
+  if (chunks <= 4) tc::slice_fields_kernel<4><<<g, 256, 0, s>>>(x, sub, scale, planes, n, kp, count, bits);
   else if (chunks <= 8) tc::slice_fields_kernel<8><<<g, 256, 0, s>>>(x, sub, scale, planes, n, kp, count, bits);
+  else if (chunks <= 17) tc::slice_fields_kernel<17><<<g, 256, 0, s>>>(x, sub, scale, planes, n, kp, count, bits);
   else tc::slice_fields_kernel<tc::SLICE_MAXC><<<g, 256, 0, s>>>(x, sub, scale, planes, n, kp, count, bits);
   launch_counter()++;
   return cudaGetLastError();

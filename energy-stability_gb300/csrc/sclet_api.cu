@@ -477,11 +477,6 @@ int sclet_create_runs(const sclet_params *p, int runs, const double *krun, int p
   }
   if (p->elastic == 1 && p->nac < 1) return bad("ELASTIC = 1 needs Allen-Cahn fields");
   if (precision != SCLET_FP64 && precision != SCLET_MIXED) return bad("precision must be SCLET_FP64 or SCLET_MIXED");
-  if (precision == SCLET_MIXED && tc_kp(p->nx) < 32) {
-    // the tensor-core product loads 32-wide k-slices of each (8-padded) line
-    g_create_error = "the mixed form needs a block edge of at least 25";
-    return SCLET_ERR_UNSUPPORTED;
-  }
   sclet_ctx *ctx = new sclet_ctx();
   ctx->p = *p;
   ctx->precision = precision;

@@ -148,11 +148,13 @@ static inline PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   return fn;
 }
 
+// k-blocked slice planes [depth][kp / BK][rows][BK] as a 3-D tensor {BK, rows,
+// depth * kp / BK}: a box is one k-block of box_rows consecutive rows.
 static inline cudaError_t make_map(CUtensorMap *map, const void *ptr, int kp, long long rows, int depth, int box_rows) {
   auto fn = encode_fn();
   if (!fn) return cudaErrorNotSupported;
-  cuuint64_t dims[3] = {(cuuint64_t)kp, (cuuint64_t)rows, (cuuint64_t)depth};
-  cuuint64_t strides[2] = {(cuuint64_t)kp * 2, (cuuint64_t)kp * 2 * (cuuint64_t)rows};
+  cuuint64_t dims[3] = {(cuuint64_t)tc::BK, (cuuint64_t)rows, (cuuint64_t)depth * (cuuint64_t)(kp / tc::BK)};
+  cuuint64_t strides[2] = {(cuuint64_t)tc::BK * 2, (cuuint64_t)tc::BK * 2 * (cuuint64_t)rows};
   cuuint32_t box[3] = {(cuuint32_t)tc::BK, (cuuint32_t)box_rows, 1};
   cuuint32_t estr[3] = {1, 1, 1};
   CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void *>(ptr), dims, strides, box, estr,
