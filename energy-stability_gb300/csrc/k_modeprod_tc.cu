@@ -33,13 +33,16 @@
 // out[t][a' * n*n + r] for input row r = c * n + b, i.e. contracted index
 // slowest: three products return to x-fastest order.
 //
-// Kernel: persistent CTAs (one per SM) looping over output tiles D[128 a' x
-// 128 r], a'-tiles fastest so that the CTAs working on the a'-tiles of one
-// input tile run side by side and the input slices come from HBM once (the
-// second read hits L2); the matrix slices stay in L2.  Every CTA loads its
-// own operand tiles (no cluster).
-// A = matrix slices (128 a' rows x 32 k, 64-byte swizzle), B = input
-// slices (128 r rows x 32 k), both K-major, in a three-stage mbarrier pipeline
+// Kernel: persistent CTAs (one per SM) looping over output tiles D[128 r x
+// 128 a'] (input rows on the MMA's M side, eigen-modes a' on its N side, so
+// the last a'-tile runs N = its live rows rounded up to 16 rather than a full
+// 128).  A CTA takes whole groups (every a'-tile of one input tile, a'-tiles
+// fastest, groups round robin), so the CTAs stay balanced and the input
+// slices come from HBM once (the group's later a'-tiles read them from L2);
+// the matrix slices stay in L2.  Every CTA loads its own operand tiles (no
+// cluster).
+// A = input slices (128 r rows x 32 k, 64-byte swizzle), B = matrix slices
+// (128 a' rows x 32 k), both K-major, in a three-stage mbarrier pipeline
 // that runs ahead across tiles; a stage is refilled once the MMAs that read
 // it have completed.
 // Warp 0 issues TMA, warp 1 issues MMAs (one elected thread each) and owns the
@@ -68,6 +71,7 @@ namespace sclet {
 
 namespace tc {
 
+template <int EPI, int OUT>
 __global__ void __launch_bounds__(THREADS, 1)
     modeprod_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, TcArgs g) {
   extern __shared__ uint8_t smem_raw[];
@@ -82,9 +86,11 @@ __global__ void __launch_bounds__(THREADS, 1)
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + SMEM_ALIGN - 1) & ~(uintptr_t)(SMEM_ALIGN - 1));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long rows = (long long)g.n * g.n;
-  const int a_tiles = (g.n + BM - 1) / BM;
-  const int r_tiles = (int)((rows + BN - 1) / BN);
-  const int total = a_tiles * r_tiles * g.count;
+  const int a_tiles = (g.n + BN - 1) / BN;
+  const int r_tiles = (int)((rows + BM - 1) / BM);
+  // whole groups (every a'-tile of one input tile) per CTA, round robin
+  const int groups = r_tiles * g.count;
+  const int mine = (int)blockIdx.x < groups ? a_tiles * ((groups - 1 - (int)blockIdx.x) / (int)gridDim.x + 1) : 0;
   const int nkb = g.kblocks;
 
   if (threadIdx.x == 0) {
@@ -94,7 +100,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
     for (int b = 0; b < NBUF; b++) {
       mbar_init(&tfull_bar[b], 1);
-      mbar_init(&tempty_bar[b], 4);  // one arrival per epilogue warp
+      mbar_init(&tempty_bar[b], EPI_WARPS);  // one arrival per epilogue warp
     }
     mbar_init(&done_bar, 1);
     failed = 0;
@@ -114,12 +120,12 @@ __global__ void __launch_bounds__(THREADS, 1)
 
   if (warp == 0) {
     if (lane == 0) {
-      // producer: five A slices and four B slices per stage, k-blocks of all
-      // this CTA's tiles in one stream
+      // producer: four input slices and five matrix slices per stage, the
+      // k-blocks of all this CTA's tiles in one stream
       int it = 0;
       // the self-test leaves every barrier without arrivals (no copy is issued)
-      for (int gam = g.idle ? total : blockIdx.x; gam < total; gam += gridDim.x) {
-        const TileIdx ti = tile_of(gam, a_tiles, r_tiles);
+      for (int u = g.idle ? mine : 0; u < mine; u++) {
+        const TileIdx ti = cta_tile(u, a_tiles, r_tiles, blockIdx.x, gridDim.x);
         for (int kb = 0; kb < nkb; kb++, it++) {
           const int s = it % STAGES;
           if (it >= STAGES && !mbar_wait(&empty_bar[s], ((it / STAGES) & 1) ^ 1)) {
@@ -130,11 +136,10 @@ __global__ void __launch_bounds__(THREADS, 1)
           uint8_t *st = base + s * STAGE_BYTES;
           mbar_expect_tx(&full_bar[s], STAGE_BYTES);
           // k-block kb of plane z is the contiguous block z * nkb + kb
-          for (int p = 0; p < NPM; p++)
-            tma_load_3d(st + p * PLANE_A, &tmA, 0, ti.a_tile * BM, p * nkb + kb, &full_bar[s]);
           for (int p = 0; p < NP; p++)
-            tma_load_3d(st + NPM * PLANE_A + p * PLANE_B, &tmB, 0, ti.r_tile * BN, (ti.t * NP + p) * nkb + kb,
-                        &full_bar[s]);
+            tma_load_3d(st + p * PLANE_A, &tmA, 0, ti.r_tile * BM, (ti.t * NP + p) * nkb + kb, &full_bar[s]);
+          for (int p = 0; p < NPM; p++)
+            tma_load_3d(st + NP * PLANE_A + p * PLANE_B, &tmB, 0, ti.a_tile * BN, p * nkb + kb, &full_bar[s]);
         }
         if (*(volatile int *)&failed) break;
       }
@@ -145,15 +150,18 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      // MMA issuer: 2 k-steps of 16 per stage, eleven terms each; (matrix
-      // slice, input slice, class) grouped by class, small classes first; the
-      // first term of each class at a tile's first k-step starts its accumulator
-      const uint32_t idesc = idesc_bf16(BM, BN);
-      const int pairA[11] = {4, 0, 1, 2, 3, 0, 1, 2, 0, 1, 0};
-      const int pairB[11] = {0, 3, 2, 1, 0, 2, 1, 0, 1, 0, 0};
+      // MMA issuer: 2 k-steps of 16 per stage, eleven terms each; (input
+      // slice, matrix slice, class) grouped by class, small classes first; the
+      // first term of each class at a tile's first k-step starts its
+      // accumulator.  The last a'-tile runs N = its rows rounded up to 16.
+      const int last_cols = g.n - (a_tiles - 1) * BN;
+      const uint32_t idesc_full = idesc_bf16(BM, BN);
+      const uint32_t idesc_last = idesc_bf16(BM, (last_cols + 15) / 16 * 16);
+      const int pairA[11] = {0, 3, 2, 1, 0, 2, 1, 0, 1, 0, 0};  // input slice
+      const int pairB[11] = {4, 0, 1, 2, 3, 0, 1, 2, 0, 1, 0};  // matrix slice
       const int cls[11] = {3, 3, 3, 3, 3, 2, 2, 2, 1, 1, 0};
       int it = 0, j = 0;
-      for (int gam = blockIdx.x; gam < total && !*(volatile int *)&failed; gam += gridDim.x, j++) {
+      for (int u = 0; u < mine && !*(volatile int *)&failed; u++, j++) {
         const int b = j % NBUF;
         // accumulator set b was last used by tile j - NBUF
         if (j >= NBUF && !mbar_wait(&tempty_bar[b], ((j / NBUF) & 1) ^ 1)) {
@@ -162,6 +170,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
         fence_after();
         const uint32_t acc = tmem + (uint32_t)(b * ACC_COLS);
+        const uint32_t idesc = u % a_tiles == a_tiles - 1 ? idesc_last : idesc_full;
         bool ok = true;
         for (int kb = 0; kb < nkb; kb++, it++) {
           const int s = it % STAGES;
@@ -171,7 +180,7 @@ __global__ void __launch_bounds__(THREADS, 1)
           }
           fence_after();
           const uint32_t sa = smem_u32(base + s * STAGE_BYTES);
-          const uint32_t sb = sa + NPM * PLANE_A;
+          const uint32_t sb = sa + NP * PLANE_A;
 #pragma unroll
           for (int ks = 0; ks < BK / 16; ks++) {
             const uint32_t koff = ks * 32;
@@ -198,19 +207,22 @@ __global__ void __launch_bounds__(THREADS, 1)
       if (!mbar_wait(&done_bar, 0)) failed = 1;
     }
   } else {
-    // epilogue warps 2-5: TMEM lane quadrant q = warp % 4 holds a' rows q*32..
-    // Each tile: combine the four classes of all BN columns into registers,
-    // free the accumulators at once (the MMA warp starts the next tile), then
-    // scale, apply the fused update and store while those MMAs run.
-    __shared__ float s_isc[4][BN];  // per warp: the tile's input-row scales
+    // epilogue warps 2-9: TMEM lane quadrant q = warp % 4 holds input rows
+    // q*32 .. q*32+31 of the tile, one per lane; the columns are the tile's
+    // a' (eigen-mode) rows, the first half for warps 2-5, the second for
+    // warps 6-9.  Each tile: combine the four classes of the warp's live
+    // columns into registers, free the accumulators at once (the MMA warp
+    // starts the next tile), then scale, apply the fused update and store
+    // while those MMAs run.  For one a' the 32 lanes hold 32 consecutive
+    // input rows, so every load and store of the warp is one contiguous
+    // 128-byte run (512 bytes for the coefficient tables).
     const int q = warp & 3;
-    const int row = q * 32 + lane;
+    const int c_first = ((warp - 2) >> 2) * CPW;  // the warp's first 32-column chunk
     // class weights 2^-b(w+2); exact integers combined small to large
     const float wt[NACC] = {ldexpf(1.0f, -2 * g.bits), ldexpf(1.0f, -3 * g.bits), ldexpf(1.0f, -4 * g.bits),
                             ldexpf(1.0f, -5 * g.bits)};
-    const bool vec = (rows & 3) == 0;
     int j = 0;
-    for (int gam = blockIdx.x; gam < total; gam += gridDim.x, j++) {
+    for (int u = 0; u < mine; u++, j++) {
       const int b = j % NBUF;
       // one lane waits, the warp follows its verdict (tcgen05.ld below needs
       // the whole warp converged)
@@ -222,94 +234,94 @@ __global__ void __launch_bounds__(THREADS, 1)
         break;
       }
       fence_after();
-      float acc[BN / 32][32];
+      const TileIdx ti = cta_tile(u, a_tiles, r_tiles, blockIdx.x, gridDim.x);
+      const int at0 = ti.a_tile * BN;
+      const int nch = (min(BN, g.n - at0) + 31) / 32;  // 32-column chunks holding live a'
+      const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * ACC_COLS);
+      // per live chunk two classes in flight at a time
+      float acc[CPW][32];
 #pragma unroll
-      for (int c = 0; c < BN / 32; c++) {
-        float w[32];
-        const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * ACC_COLS + c * 32);
-        tmem_ld32(ta + 3 * BN, acc[c]);
+      for (int cl = 0; cl < CPW; cl++) {
+        const int c = c_first + cl;
+        if (c < nch) {
+          uint32_t ra[32], rb[32];
+          tmem_ld32_async(ta + 3 * BN + c * 32, ra);
+          tmem_ld32_async(ta + 2 * BN + c * 32, rb);
+          tmem_wait_ld();
 #pragma unroll
-        for (int jj = 0; jj < 32; jj++) acc[c][jj] *= wt[3];
+          for (int jj = 0; jj < 32; jj++)
+            acc[cl][jj] = fmaf(__uint_as_float(rb[jj]), wt[2], __uint_as_float(ra[jj]) * wt[3]);
+          tmem_ld32_async(ta + 1 * BN + c * 32, ra);
+          tmem_ld32_async(ta + c * 32, rb);
+          tmem_wait_ld();
 #pragma unroll
-        for (int k = 2; k >= 0; k--) {
-          tmem_ld32(ta + k * BN, w);
-#pragma unroll
-          for (int jj = 0; jj < 32; jj++) acc[c][jj] = fmaf(w[jj], wt[k], acc[c][jj]);
+          for (int jj = 0; jj < 32; jj++)
+            acc[cl][jj] = fmaf(__uint_as_float(rb[jj]), wt[0], fmaf(__uint_as_float(ra[jj]), wt[1], acc[cl][jj]));
         }
       }
       fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&tempty_bar[b]);
-      const TileIdx ti = tile_of(gam, a_tiles, r_tiles);
-      const int a = ti.a_tile * BM + row;
-      const int kind = (ti.t % g.F) >= g.nac ? 1 : 0;
+      const long long r = (long long)ti.r_tile * BM + q * 32 + lane;
+      const bool live = r < rows;
+      const bool ch = (ti.t % g.F) >= g.nac;  // field kind: Cahn-Hilliard
+      const float4 *cf = ch ? g.coef[1] : g.coef[0];
+      const float2 *cf2 = ch ? g.coef2[1] : g.coef2[0];
       const long long tb = (long long)ti.t * g.n * rows;
-      const float sa = a < g.n ? g.row_scale[a] : 0.0f;
-      const float *isc = g.in_scale + (long long)ti.t * rows;
-      const long long rt0 = (long long)ti.r_tile * BN;
-      for (int i = lane; i < BN; i += 32) s_isc[q][i] = rt0 + i < rows ? isc[rt0 + i] : 0.0f;
-      __syncwarp();
+      float *outT = g.out + tb;
+      const float si = live ? g.in_scale[(long long)ti.t * rows + r] : 0.0f;
+      // offsets within one tensor stay below n^3 < 2^32 (n <= 1088)
+      const uint32_t urows = (uint32_t)rows;
 #pragma unroll
-      for (int c = 0; c < BN / 32; c++) {
-        if (a < g.n) {
-        const long long r0 = rt0 + c * 32;
-        const long long o0 = (long long)a * rows + r0;  // eigen-mode [k][j][i] of a z-contraction
-        const float *si = &s_isc[q][c * 32];
-        if (vec && r0 + 32 <= rows) {
+      for (int cl = 0; cl < CPW; cl++) {
+        const int c = c_first + cl;
+        if (c < nch) {
+          const int a0 = at0 + c * 32;
+          const int lim = min(32, g.n - a0);  // live a' in the chunk
+          // the chunk's 32 matrix-row scales, one per lane, broadcast below
+          const float rs = lane < lim ? g.row_scale[a0 + lane] : 0.0f;
+          const uint32_t o0 = (uint32_t)a0 * urows + (uint32_t)(live ? r : 0);  // eigen-mode [k][j][i] of a z-contraction
+          // batches of columns: every load of a batch is issued before its
+          // first store (aux and the coefficient tables are read-only here:
+          // the ETD update never runs in place)
+          constexpr int NB = EPI == 0 ? 8 : 4;
 #pragma unroll
-          for (int jj = 0; jj < 32; jj += 4) {
-            float4 y = make_float4(acc[c][jj] * (si[jj] * sa), acc[c][jj + 1] * (si[jj + 1] * sa),
-                                   acc[c][jj + 2] * (si[jj + 2] * sa), acc[c][jj + 3] * (si[jj + 3] * sa));
-            const long long o = o0 + jj;
-            if (g.epi == 1) {
-              const float4 uh = *reinterpret_cast<const float4 *>(g.aux + tb + o);
-              const float4 c0 = g.coef[kind][o], c1 = g.coef[kind][o + 1], c2 = g.coef[kind][o + 2],
-                           c3 = g.coef[kind][o + 3];  // (e_hi, e_lo, phi1_hi, phi1_lo)
-              y.x = fmaf(c0.x, uh.x, fmaf(c0.y, uh.x, fmaf(c0.z, y.x, c0.w * y.x)));
-              y.y = fmaf(c1.x, uh.y, fmaf(c1.y, uh.y, fmaf(c1.z, y.y, c1.w * y.y)));
-              y.z = fmaf(c2.x, uh.z, fmaf(c2.y, uh.z, fmaf(c2.z, y.z, c2.w * y.z)));
-              y.w = fmaf(c3.x, uh.w, fmaf(c3.y, uh.w, fmaf(c3.z, y.w, c3.w * y.w)));
-            } else if (g.epi == 2) {
-              const float2 c0 = g.coef2[kind][o], c1 = g.coef2[kind][o + 1], c2 = g.coef2[kind][o + 2],
-                           c3 = g.coef2[kind][o + 3];  // (phi2_hi, phi2_lo)
-              y.x = fmaf(c0.x, y.x, c0.y * y.x);
-              y.y = fmaf(c1.x, y.y, c1.y * y.y);
-              y.z = fmaf(c2.x, y.z, c2.y * y.z);
-              y.w = fmaf(c3.x, y.w, c3.y * y.w);
-            }
-            float4 *dst = reinterpret_cast<float4 *>(g.out + tb + o);
-            if (g.outmode == 2) {
-              const float4 old = *dst;
-              y.x += old.x;
-              y.y += old.y;
-              y.z += old.z;
-              y.w += old.w;
-            }
-            *dst = y;
-          }
-        } else {
+          for (int j0 = 0; j0 < 32; j0 += NB) {
+            float uh[NB], old[NB];
+            float4 c1[NB];
+            float2 c2[NB];
 #pragma unroll
-          for (int jj = 0; jj < 32; jj++) {
-            const long long r = r0 + jj;
-            if (r < rows) {
-              float y = acc[c][jj] * (si[jj] * sa);
-              const long long o = o0 + jj;
-              if (g.epi == 1) {
-                const float uh = g.aux[tb + o];
-                const float4 cc = g.coef[kind][o];
-                y = fmaf(cc.x, uh, fmaf(cc.y, uh, fmaf(cc.z, y, cc.w * y)));
-              } else if (g.epi == 2) {
-                const float2 cc = g.coef2[kind][o];
-                y = fmaf(cc.x, y, cc.y * y);
+            for (int jj = 0; jj < NB; jj++) {
+              const uint32_t o = o0 + (uint32_t)(j0 + jj) * urows;
+              if (j0 + jj < lim && live) {
+                if (EPI == 1) {
+                  uh[jj] = __ldg(g.aux + tb + o);
+                  c1[jj] = __ldg(cf + o);
+                } else if (EPI == 2) {
+                  c2[jj] = __ldg(cf2 + o);
+                }
+                if (OUT == 2) old[jj] = outT[o];
               }
-              if (g.outmode == 1) g.out[tb + o] = y;
-              else g.out[tb + o] += y;
+            }
+#pragma unroll
+            for (int jj = 0; jj < NB; jj++) {
+              const uint32_t o = o0 + (uint32_t)(j0 + jj) * urows;
+              const float sc = si * __shfl_sync(0xffffffffu, rs, j0 + jj);
+              if (j0 + jj < lim && live) {
+                float y = acc[cl][j0 + jj] * sc;
+                if (EPI == 1) {
+                  const float4 cc = c1[jj];  // (e_hi, e_lo, phi1_hi, phi1_lo)
+                  y = fmaf(cc.x, uh[jj], fmaf(cc.y, uh[jj], fmaf(cc.z, y, cc.w * y)));
+                } else if (EPI == 2) {
+                  y = fmaf(c2[jj].x, y, c2[jj].y * y);  // (phi2_hi, phi2_lo)
+                }
+                if (OUT == 2) y += old[jj];
+                outT[o] = y;
+              }
             }
           }
         }
-        }  // a < n
       }
-      __syncwarp();  // s_isc is rewritten for the next tile
       if (__any_sync(0xffffffffu, *(volatile int *)&failed != 0)) break;
     }
   }
@@ -523,8 +535,24 @@ cudaError_t tc_make_coefs(float4 *coef, float2 *coef2, int n, int kind, const do
   return cudaGetLastError();
 }
 
+// The kernel's instances (fused update, output): (none, store), (none,
+// accumulate), (ETD1, store), (phi2, store) -- the combinations the step uses.
+using TcKernel = void (*)(const CUtensorMap, const CUtensorMap, TcArgs);
+constexpr int TC_INSTANCES = 4;
+static TcKernel tc_instance(int i) {
+  static const TcKernel k[TC_INSTANCES] = {tc::modeprod_tc_kernel<0, 1>, tc::modeprod_tc_kernel<0, 2>,
+                                           tc::modeprod_tc_kernel<1, 1>, tc::modeprod_tc_kernel<2, 1>};
+  return k[i];
+}
+static TcKernel tc_kernel(int epi, int outmode) {
+  if (outmode == 1 && epi >= 0 && epi <= 2) return tc_instance(epi == 0 ? 0 : epi + 1);
+  if (outmode == 2 && epi == 0) return tc_instance(1);
+  return nullptr;
+}
+
 // Per-device launch set-up: the dynamic shared-memory attributes (set per
-// device) and the number of CTAs that can be resident at once.
+// device, for every instance) and the number of CTAs that can be resident at
+// once.
 static int tc_setup(int *ctas) {
   constexpr int MAXDEV = 64;
   static std::mutex mu;
@@ -535,13 +563,15 @@ static int tc_setup(int *ctas) {
   if (dev < 0 || dev >= MAXDEV) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lock(mu);
   if (!resident[dev]) {
-    // all of the unified L1/shared capacity as shared memory
-    e = cudaFuncSetAttribute(tc::modeprod_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(tc::modeprod_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    if (e != cudaSuccess) return e;
+    for (int i = 0; i < TC_INSTANCES; i++) {
+      // all of the unified L1/shared capacity as shared memory
+      e = cudaFuncSetAttribute(tc_instance(i), cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
+      if (e != cudaSuccess) return e;
+      e = cudaFuncSetAttribute(tc_instance(i), cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+      if (e != cudaSuccess) return e;
+    }
     int per_sm = 0, sms = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc::modeprod_tc_kernel, tc::THREADS, tc::SMEM_BYTES);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc_kernel(0, 1), tc::THREADS, tc::SMEM_BYTES);
     if (e != cudaSuccess) return e;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
@@ -557,22 +587,25 @@ cudaError_t launch_modeprod_tc(const __nv_bfloat16 *mat, const __nv_bfloat16 *pl
   int ctas = 0;
   cudaError_t e = (cudaError_t)tc_setup(&ctas);
   if (e != cudaSuccess) return e;
+  const TcKernel kern = tc_kernel(args.epi, args.outmode);
+  if (!kern) return cudaErrorInvalidValue;
   const int n = args.n, kp = tc_kp(n);
   const int bits = tc_slice_bits(n);
   if ((long long)tc::BK * ((n + tc::BK - 1) / tc::BK) > (1LL << (24 - 2 * bits))) return cudaErrorInvalidValue;
+  if ((long long)n * n * n > 0xffffffffLL) return cudaErrorInvalidValue;  // 32-bit offsets within a tensor
   CUtensorMap ma, mb;
-  if ((e = make_map(&ma, mat, kp, n, TC_PLANES_M, tc::BM)) != cudaSuccess) return e;
-  if ((e = make_map(&mb, planes, kp, (long long)n * n, TC_PLANES * count, tc::BN)) != cudaSuccess) return e;
+  if ((e = make_map(&ma, planes, kp, (long long)n * n, TC_PLANES * count, tc::BM)) != cudaSuccess) return e;
+  if ((e = make_map(&mb, mat, kp, n, TC_PLANES_M, tc::BN)) != cudaSuccess) return e;
   TcArgs g = args;
   g.kp = kp;
   g.kblocks = (n + tc::BK - 1) / tc::BK;
   g.bits = bits;
-  const long long tiles = (long long)((n + tc::BM - 1) / tc::BM) * (((long long)n * n + tc::BN - 1) / tc::BN) * count;
-  if (tiles > 0x7fffffffLL) return cudaErrorInvalidValue;
+  const long long groups = (((long long)n * n + tc::BM - 1) / tc::BM) * count;  // input tiles
+  if (groups * ((n + tc::BN - 1) / tc::BN) > 0x7fffffffLL) return cudaErrorInvalidValue;
   // persistent: as many CTAs as can be resident at once (or the tuned count)
   if (args.max_ctas > 0 && args.max_ctas < ctas) ctas = args.max_ctas;
-  const int grid = (int)(tiles < ctas ? tiles : ctas);
-  tc::modeprod_tc_kernel<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(ma, mb, g);
+  const int grid = (int)(groups < ctas ? groups : ctas);
+  kern<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(ma, mb, g);
   launch_counter()++;
   return cudaGetLastError();
 }

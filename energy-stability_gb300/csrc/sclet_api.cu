@@ -885,8 +885,10 @@ static int etd_update_mixed(sclet_ctx *ctx) {
   CK(tc_slice(ctx, ctx->W1, nullptr, 2 * F));
   CK(tc_prod(ctx, false, ctx->P, ctx->scaleP, 2 * F, ctx->W2, 0, nullptr, 1));
   CK(tc_slice(ctx, ctx->W2, nullptr, 2 * F));
-  CK(tc_prod(ctx, false, ctx->P, ctx->scaleP, F, ctx->W1, 0, nullptr, 1));
-  CK(tc_prod(ctx, false, ctx->P + F * ps, ctx->scaleP + F * rows, F, ctx->W1, 1, ctx->W1, 1));
+  // uhat into W2 (free once sliced), so that the fused update reads it from a
+  // buffer it does not write
+  CK(tc_prod(ctx, false, ctx->P, ctx->scaleP, F, ctx->W2, 0, nullptr, 1));
+  CK(tc_prod(ctx, false, ctx->P + F * ps, ctx->scaleP + F * rows, F, ctx->W1, 1, ctx->W2, 1));
   CK(tc_slice(ctx, ctx->W1, nullptr, F));
   CK(tc_prod(ctx, true, ctx->P, ctx->scaleP, F, ctx->W2, 0, nullptr, 1));
   CK(tc_slice(ctx, ctx->W2, nullptr, F));

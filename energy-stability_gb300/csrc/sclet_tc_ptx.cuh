@@ -15,16 +15,18 @@ namespace tc {
 
 
 constexpr int BM = 128, BN = 128, BK = 32, STAGES = 3, NP = TC_PLANES, NPM = TC_PLANES_M;
-constexpr int PLANE_A = BM * BK * 2;  // 8 KB
-constexpr int PLANE_B = BN * BK * 2;  // 8 KB
-constexpr int STAGE_BYTES = NPM * PLANE_A + NP * PLANE_B;
+constexpr int PLANE_A = BM * BK * 2;  // 8 KB: one input slice (M side, 128 input rows)
+constexpr int PLANE_B = BN * BK * 2;  // 8 KB: one matrix slice (N side, 128 a' rows)
+constexpr int STAGE_BYTES = NP * PLANE_A + NPM * PLANE_B;
 constexpr int SMEM_ALIGN = 512;  // period of the 64-byte swizzle pattern
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + SMEM_ALIGN;
 constexpr int NACC = 4;               // weight classes w = 0..3
 constexpr int ACC_COLS = NACC * BN;   // one accumulator set
 constexpr int NBUF = 512 / ACC_COLS;   // accumulator sets in tensor memory (1 or 2)
 constexpr int TMEM_COLS = NBUF * ACC_COLS;
-constexpr int THREADS = 192;          // producer, MMA, four epilogue warps
+constexpr int EPI_WARPS = 8;          // two per TMEM lane quadrant, each half of the columns
+constexpr int CPW = BN / 32 / 2;      // 32-column chunks per epilogue warp
+constexpr int THREADS = 64 + 32 * EPI_WARPS;  // producer, MMA, epilogue warps
 constexpr long long WAIT_LIMIT = 1LL << 22;  // polls (with backoff) before giving up
 static_assert(TMEM_COLS <= 512, "tensor memory holds 512 columns");
 static_assert(SMEM_BYTES <= 227 * 1024, "shared memory per CTA");
@@ -109,6 +111,19 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
   for (int j = 0; j < 32; j++) v[j] = __uint_as_float(r[j]);
 }
 
+// The same load without the wait: the registers are valid after tmem_wait_ld.
+__device__ __forceinline__ void tmem_ld32_async(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
@@ -124,13 +139,17 @@ __device__ __forceinline__ float pow2_scale(float m) {
   return ldexpf(1.0f, e);
 }
 
-// Output tile gam: a'-tiles fastest, then input tiles, then the tensor.
-__device__ __forceinline__ TileIdx tile_of(int gam, int a_tiles, int r_tiles) {
+// The u-th output tile of CTA `cta`: each CTA takes whole groups (every
+// a'-tile of one input tile, a'-tiles fastest), groups dealt round robin.
+// Every group costs the same (the last a'-tile is narrower), so the CTAs stay
+// balanced, and the group's input tile, read once from HBM by its first
+// a'-tile, is read again from L2 by the CTA's next a'-tiles.
+__device__ __forceinline__ TileIdx cta_tile(int u, int a_tiles, int r_tiles, int cta, int grid) {
   TileIdx x;
-  x.a_tile = gam % a_tiles;
-  const int rest = gam / a_tiles;
-  x.r_tile = rest % r_tiles;
-  x.t = rest / r_tiles;
+  const int grp = cta + (u / a_tiles) * grid;
+  x.a_tile = u % a_tiles;
+  x.r_tile = grp % r_tiles;
+  x.t = grp / r_tiles;
   return x;
 }
 
