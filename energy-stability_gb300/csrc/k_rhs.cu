@@ -35,6 +35,7 @@ struct P {
   // anisotropic term folded: kan[m][3 r + c] = epn2 LE (1/2h_r) lam_m[r][c] (1/2h_c),
   // the flux row r differenced along axis r
   T kan[4][9];
+  T mob_m0, mob_dg;     // variable mobility M(eta0) = m0 (1 (1 - eta0) + dg eta0)
 };
 
 template <typename T>
@@ -55,6 +56,8 @@ static P<T> to_p(const Phys &ph) {
     for (int k = 0; k < 9; k++) {
       p.kan[m][k] = (T)(ph.epn2 * ph.LE * i2h[k / 3] * ph.lam[m][k] * i2h[k % 3]);
     }
+  p.mob_m0 = (T)ph.mob_m0;
+  p.mob_dg = (T)ph.mob_dg;
   return p;
 }
 
@@ -304,6 +307,162 @@ __global__ void __launch_bounds__(RX * RY) rhs_ch_lap_kernel(P<T> p0, const T *_
   out[l] = v;
 }
 
+// ---- variable-mobility Cahn-Hilliard ---------------------------------------
+// ch_calc_FU_VariableMobility (source_beta_to_omega/src/mobility.c:838-858),
+// update_M_C (:860-922) run first, on the single conserved field:
+//   f0 = -LCI KCI c + LCI CH_f                              (ch_calc_F0)
+//   t1 = -f0 + KCI c + epn2 c_out / h^2 on faces,  f1 = -C lap0(t1) - C mu_out / h^2
+//                                                           (ch_calc_F1)
+//   t2 = epn2 lap0(c) - f0 + epn2 c_out / h^2 on faces,
+//   f2 = -div0((M - C) grad t2)                             (ch_calc_F2,
+//        ch_divergence_M_gradient :435-722: face flux (m_q + m)(a_q - a)/(2 h^2))
+//   N  = LCI (f1 + f2)
+// with M(eta0) the first concentration's mobility, C its largest value over
+// the block, lap0 / div0 zero outside the block (values and mobility), c_out
+// the periodic image outside a face and mu_out the boundary chemical potential
+// there (ch_mu).  Three launches: the block maxima of M, their maximum C, then
+// t1 and t2, then N.
+
+template <typename T>
+__device__ __forceinline__ T mobility(const P<T> &p, T e) {
+  return p.mob_m0 * ((T)1 * ((T)1 - e) + p.mob_dg * e);
+}
+
+// per run (blockIdx.y): the largest M over the block, per CTA
+template <typename T>
+__global__ void __launch_bounds__(256) mob_max_kernel(P<T> p, const T *__restrict__ u, double *__restrict__ part) {
+  __shared__ double sm[8];
+  const size_t n3 = (size_t)p.n * p.n * p.n;
+  const T *e0 = u + (size_t)blockIdx.y * p.F * n3;  // the run's first order parameter
+  double mx = -1.0e30;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n3; i += (size_t)gridDim.x * blockDim.x)
+    mx = fmax(mx, (double)mobility(p, e0[i]));
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) mx = fmax(mx, sm[w]);
+    part[(size_t)blockIdx.y * MOB_PARTS + blockIdx.x] = mx;
+  }
+}
+
+// C of every run: cmax[run] = max of its MOB_PARTS partial maxima
+__global__ void __launch_bounds__(256) mob_final_kernel(const double *__restrict__ part, double *__restrict__ cmax) {
+  __shared__ double sm[8];
+  double mx = -1.0e30;
+  for (int i = threadIdx.x; i < MOB_PARTS; i += blockDim.x) mx = fmax(mx, part[(size_t)blockIdx.x * MOB_PARTS + i]);
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) mx = fmax(mx, sm[w]);
+    cmax[blockIdx.x] = mx;
+  }
+}
+
+// t1 and t2 of every cell (blockIdx.z = run x z)
+template <typename PL, typename T>
+__global__ void __launch_bounds__(RX * RY) mob_t_kernel(P<T> p0, const T *__restrict__ u, T *__restrict__ tt) {
+  const int n = p0.n;
+  const int run = blockIdx.z / n;
+  const int x = blockIdx.x * RX + threadIdx.x, y = blockIdx.y * RY + threadIdx.y, z = blockIdx.z - run * n;
+  if (x >= n || y >= n) return;
+  const size_t n3 = (size_t)n * n * n, nn = (size_t)n * n;
+  P<T> p = p0;
+  if (p0.krun) p.K[0] = (T)p0.krun[run];
+  u += (size_t)run * p.F * n3;
+  T *t1 = tt + (size_t)run * 2 * n3, *t2 = t1 + n3;
+  const size_t l = (size_t)z * nn + (size_t)y * n + x;
+  const T *cf = u + p.nac * n3;
+  T e[4] = {(T)0, (T)0, (T)0, (T)0};
+#pragma unroll
+  for (int m = 0; m < 4; m++)
+    if (m < p.nac) e[m] = u[m * n3 + l];
+  const T c = cf[l];
+  T f0 = -p.LCI * p.KCI * c;
+  f0 += p.LCI * ch_f<PL>(p, e, c);
+  const T cl = x > 0 ? cf[l - 1] : (T)0, cr = x < n - 1 ? cf[l + 1] : (T)0;
+  const T ct = y > 0 ? cf[l - n] : (T)0, cb = y < n - 1 ? cf[l + n] : (T)0;
+  const T cz = z > 0 ? cf[l - nn] : (T)0, ck = z < n - 1 ? cf[l + nn] : (T)0;
+  T la = (cl + cr - (T)2 * c) * p.ih2x;
+  la += (ct + cb - (T)2 * c) * p.ih2y;
+  la += (cz + ck - (T)2 * c) * p.ih2z;
+  T a = -f0 + p.KCI * c;
+  T b = p.epn2 * la - f0;
+  if (x == 0 || x == n - 1 || y == 0 || y == n - 1 || z == 0 || z == n - 1) {
+    const int iz = img(n, z), iy = img(n, y), ix = img(n, x), lo = img(n, -1), hi = img(n, n);
+    T w;
+    if (x == 0) { w = p.epn2 * cf[L3(n, iz, iy, lo)] * p.ih2x; a += w; b += w; }
+    if (x == n - 1) { w = p.epn2 * cf[L3(n, iz, iy, hi)] * p.ih2x; a += w; b += w; }
+    if (y == 0) { w = p.epn2 * cf[L3(n, iz, lo, ix)] * p.ih2y; a += w; b += w; }
+    if (y == n - 1) { w = p.epn2 * cf[L3(n, iz, hi, ix)] * p.ih2y; a += w; b += w; }
+    if (z == 0) { w = p.epn2 * cf[L3(n, lo, iy, ix)] * p.ih2z; a += w; b += w; }
+    if (z == n - 1) { w = p.epn2 * cf[L3(n, hi, iy, ix)] * p.ih2z; a += w; b += w; }
+  }
+  t1[l] = a;
+  t2[l] = b;
+}
+
+// N = LCI (f1 + f2) of every cell (blockIdx.z = run x z)
+template <typename PL, typename T>
+__global__ void __launch_bounds__(RX * RY) mob_n_kernel(P<T> p0, const T *__restrict__ u, const T *__restrict__ tt,
+                                                        const double *__restrict__ cmax, T *__restrict__ out) {
+  const int n = p0.n;
+  const int run = blockIdx.z / n;
+  const int x = blockIdx.x * RX + threadIdx.x, y = blockIdx.y * RY + threadIdx.y, z = blockIdx.z - run * n;
+  if (x >= n || y >= n) return;
+  const size_t n3 = (size_t)n * n * n, nn = (size_t)n * n;
+  P<T> p = p0;
+  if (p0.krun) p.K[0] = (T)p0.krun[run];
+  u += (size_t)run * p.F * n3;
+  out += (size_t)run * p.F * n3;
+  const T *t1 = tt + (size_t)run * 2 * n3, *t2 = t1 + n3;
+  const T C = (T)cmax[run];
+  const size_t l = (size_t)z * nn + (size_t)y * n + x;
+  // f1 = -C lap0(t1) - C mu_out / h^2
+  const T tc = t1[l];
+  const T al = x > 0 ? t1[l - 1] : (T)0, ar = x < n - 1 ? t1[l + 1] : (T)0;
+  const T at = y > 0 ? t1[l - n] : (T)0, ab = y < n - 1 ? t1[l + n] : (T)0;
+  const T af = z > 0 ? t1[l - nn] : (T)0, ak = z < n - 1 ? t1[l + nn] : (T)0;
+  T la = (al + ar - (T)2 * tc) * p.ih2x;
+  la += (at + ab - (T)2 * tc) * p.ih2y;
+  la += (af + ak - (T)2 * tc) * p.ih2z;
+  T f1 = -C * la;
+  if (x == 0 || x == n - 1 || y == 0 || y == n - 1 || z == 0 || z == n - 1) {
+    const int iz = img(n, z), iy = img(n, y), ix = img(n, x), lo = img(n, -1), hi = img(n, n);
+    if (x == 0) f1 -= C * ch_mu_at<PL>(p, u, iz, iy, lo) * p.ih2x;
+    if (x == n - 1) f1 -= C * ch_mu_at<PL>(p, u, iz, iy, hi) * p.ih2x;
+    if (y == 0) f1 -= C * ch_mu_at<PL>(p, u, iz, lo, ix) * p.ih2y;
+    if (y == n - 1) f1 -= C * ch_mu_at<PL>(p, u, iz, hi, ix) * p.ih2y;
+    if (z == 0) f1 -= C * ch_mu_at<PL>(p, u, lo, iy, ix) * p.ih2z;
+    if (z == n - 1) f1 -= C * ch_mu_at<PL>(p, u, hi, iy, ix) * p.ih2z;
+  }
+  // f2 = -div0((M - C) grad t2), M - C and t2 zero outside the block
+  const T *e0 = u;
+  const T bc = t2[l], mc = mobility(p, e0[l]) - C;
+  auto nb = [&](bool in, size_t q, T &bq, T &mq) {
+    bq = in ? t2[q] : (T)0;
+    mq = in ? mobility(p, e0[q]) - C : (T)0;
+  };
+  T bq, mq, d;
+  const T hx = (T)0.5 * p.ih2x, hy = (T)0.5 * p.ih2y, hz = (T)0.5 * p.ih2z;
+  nb(x > 0, l - 1, bq, mq);
+  d = (mq + mc) * (bq - bc) * hx;
+  nb(x < n - 1, l + 1, bq, mq);
+  d += (mq + mc) * (bq - bc) * hx;
+  nb(y > 0, l - n, bq, mq);
+  d += (mq + mc) * (bq - bc) * hy;
+  nb(y < n - 1, l + n, bq, mq);
+  d += (mq + mc) * (bq - bc) * hy;
+  nb(z > 0, l - nn, bq, mq);
+  d += (mq + mc) * (bq - bc) * hz;
+  nb(z < n - 1, l + nn, bq, mq);
+  d += (mq + mc) * (bq - bc) * hz;
+  out[(size_t)p.nac * n3 + l] = p.LCI * (f1 - d);
+}
+
 template <typename PL, typename T>
 static cudaError_t launch_rhs_pl(const Phys &ph, const T *u, const T *felas, T *out, T *scratch, cudaStream_t s) {
   P<T> p = to_p<T>(ph);
@@ -328,7 +487,16 @@ static cudaError_t launch_rhs_pl(const Phys &ph, const T *u, const T *felas, T *
     if (e != cudaSuccess) return e;
     launch_counter()++;
   }
-  if (PL::max_nch > 0) {
+  if (PL::max_nch > 0 && ph.varmob && ph.nch == 1) {
+    if (!ph.mob_t || !ph.mob_part) return cudaErrorInvalidValue;
+    T *tt = static_cast<T *>(ph.mob_t);
+    double *cmax = ph.mob_part + (size_t)MOB_PARTS * p.runs;
+    mob_max_kernel<T><<<dim3(MOB_PARTS, p.runs), 256, 0, s>>>(p, u, ph.mob_part);
+    mob_final_kernel<<<p.runs, 256, 0, s>>>(ph.mob_part, cmax);
+    mob_t_kernel<PL, T><<<grd, blk, 0, s>>>(p, u, tt);
+    mob_n_kernel<PL, T><<<grd, blk, 0, s>>>(p, u, tt, cmax, out);
+    launch_counter() += 4;
+  } else if (PL::max_nch > 0) {
     for (int m = 0; m < ph.nch; m++) {
       // one conserved field (the plugins' CH_f is defined for c_0 only)
       rhs_ch_t_kernel<PL, T><<<grd, blk, 0, s>>>(p, u, scratch);

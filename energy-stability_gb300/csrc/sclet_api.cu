@@ -69,6 +69,10 @@ struct sclet_ctx {
   float4 *coef[2] = {nullptr, nullptr};   // ETD1 coefficient pairs per field kind
   float2 *coef2[2] = {nullptr, nullptr};  // ETD2 phi2 pairs per field kind
   double *stage64 = nullptr;  // n^3 FP64 staging block for host transfers
+  // variable-mobility CH: two scratch blocks per run in the state's type and
+  // the block maxima of the mobility (Phys::mob_t, Phys::mob_part)
+  void *mob_t = nullptr;
+  double *mob_part = nullptr;
   // pipelined transfers of all fields (sclet_set_fields_async /
   // sclet_get_fields_async): an FP64 staging area per direction, filled and
   // drained by the copy engines on one stream per direction, while the
@@ -418,7 +422,7 @@ void sclet_destroy(sclet_ctx *ctx) {
                   ctx->fstate2, ctx->frhs2, ctx->ffelas, ctx->fscratch, ctx->fshell, ctx->W1, ctx->W2, ctx->P,
                   ctx->scaleP, ctx->rsV, ctx->rsVi, ctx->matV, ctx->matVi, ctx->stage64,
                   ctx->coef[0], ctx->coef[1], ctx->coef2[0], ctx->coef2[1], ctx->massW, ctx->massPart,
-                  ctx->massRes, ctx->in_stage, ctx->out_stage, ctx->krun};
+                  ctx->massRes, ctx->in_stage, ctx->out_stage, ctx->krun, ctx->mob_t, ctx->mob_part};
   for (void *b : bufs) cudaFree(b);
   if (ctx->diag_host) cudaFreeHost(ctx->diag_host);
   for (int a = 0; a < 3; a++) {
@@ -467,8 +471,10 @@ int sclet_create_runs(const sclet_params *p, int runs, const double *krun, int p
   if (p->nx < 8 || p->nx > 1028) return bad("block edge out of range [8, 1028]");
   if (p->nac < 0 || p->nac > 4 || p->nch < 0 || p->nch > 1 || p->nac + p->nch < 1)
     return bad("supported: 0..4 Allen-Cahn fields and 0..1 Cahn-Hilliard field");
-  if (p->variable_mobility != 0) {
-    g_create_error = "VariableMobility = 1 is not supported (constant-mobility CH only)";
+  if (p->variable_mobility != 0 && p->variable_mobility != 1) return bad("VariableMobility must be 0 or 1");
+  if (p->variable_mobility == 1 && (p->nch != 1 || p->nac < 1)) {
+    // update_M_C takes the mobility from the first order parameter
+    g_create_error = "VariableMobility = 1 needs one Cahn-Hilliard field and at least one Allen-Cahn field";
     return SCLET_ERR_UNSUPPORTED;
   }
   if (p->elastic != 0 && p->elastic != 1) {
@@ -600,6 +606,12 @@ int sclet_create_runs(const sclet_params *p, int runs, const double *krun, int p
       CC(cudaMalloc(&ctx->massPart, sizeof(double) * 4 * mass_partials()));
       CC(cudaMalloc(&ctx->massRes, sizeof(double) * 4));
     }
+  }
+  if (p->variable_mobility == 1) {
+    CC(cudaMalloc(&ctx->mob_t, (mixed(ctx) ? sizeof(float) : sizeof(double)) * 2 * runs * ctx->n3));
+    CC(cudaMalloc(&ctx->mob_part, sizeof(double) * (MOB_PARTS + 1) * runs));
+    ph.mob_t = ctx->mob_t;
+    ph.mob_part = ctx->mob_part;
   }
   {
     // energy tensors: the gradient operator of the dynamics

@@ -38,7 +38,18 @@ struct Phys {
   // launch shape chosen by the autotuner (0: the default)
   int rhs_zc;       // z-planes per CTA of the Allen-Cahn right-hand side
   int tc_ctas;      // persistent CTAs of the tensor-core products
+  // variable-mobility Cahn-Hilliard (VariableMobility = 1): M(eta0) =
+  // mob_m0 (1 - eta0 + mob_dg eta0) (mobility_constants); device scratch of
+  // two blocks per run (mob_t, the precision's type) and of the block maxima
+  // of M (mob_part: MOB_PARTS per run, then one C per run)
+  int varmob;
+  double mob_m0, mob_dg;
+  void *mob_t;
+  double *mob_part;
 };
+
+constexpr int MOB_PARTS = 512;  // partial maxima of M per run
+void mobility_constants(double *m0, double *dg);
 
 // Geometry helpers (owned cells are 2 .. n-3 per axis, period N = n - 4).
 __host__ __device__ inline int img(int n, int v) {

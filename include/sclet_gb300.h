@@ -77,7 +77,8 @@ typedef struct sclet_params {
   int elastic;             /* 0 none, 1 elastic force on the AC fields       */
   int anisotropic;         /* 1: explicit div(lambda grad eta) term          */
   double kkx, kky, kkz;
-  int variable_mobility;   /* must be 0 (constant-mobility CH)               */
+  int variable_mobility;   /* 0 constant mobility; 1 variable mobility       */
+                           /* (mobility.c:838-922: nch = 1, nac >= 1)        */
   /* elastic_input.txt (source_beta_to_omega/src/elastic.c:349-439) */
   double elastic_scale;
   double voigt[36];        /* 6x6, order 11,22,33,23,13,12                   */

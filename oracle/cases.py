@@ -165,6 +165,7 @@ class Case:
     c_range: Sequence[float] = (0.48, 0.52)
     suffix: str = "case"
     physics: int = 0                # 0 Landau 2-4-6 plugin, 1 the reference's own formula.c
+    variable_mobility: int = 0      # VariableMobility of the ini (mobility.c:838-922)
 
     @property
     def n(self) -> int:
@@ -197,7 +198,7 @@ def write_case(case: Case, dirpath: str, eigen: bool = True, fields: bool = True
         fp.write(" 1, 0, ./restart/\n 0, 0, 0\n")
         L = case.domain
         fp.write(f" {L!r}, {L!r}, {L!r}\n {case.etd2}\n {case.elastic}\n {case.anisotropic}\n")
-        fp.write(f" {case.kk[0]!r}, {case.kk[1]!r}, {case.kk[2]!r}\n 0\n")
+        fp.write(f" {case.kk[0]!r}, {case.kk[1]!r}, {case.kk[2]!r}\n {case.variable_mobility}\n")
     with open(os.path.join(dirpath, "elastic_input.txt"), "w") as fp:
         fp.write(f"{case.elastic_scale!r}\n\n")
         for row in case.voigt:

@@ -37,6 +37,7 @@ class OrcCfg(ctypes.Structure):
         ("bn", _dp),
         ("elam", ctypes.c_double * 36),
         ("energy_form", ctypes.c_int),
+        ("variable_mobility", ctypes.c_int),
     ]
 
 
@@ -85,6 +86,7 @@ def load_case(case_dir: str, suffix: str, fields=None) -> Dict:
     p["elastic"] = int(nums(lines[13])[0])
     p["anisotropic"] = int(nums(lines[14])[0])
     p["kk"] = nums(lines[15])
+    p["variable_mobility"] = int(nums(lines[16])[0]) if len(lines) > 16 else 0
     n = p["n"]
     big_n = n - 4
     p["h"] = [(hi[d] - lo[d]) / big_n for d in range(3)]
@@ -184,6 +186,7 @@ class Oracle:
         for i, v in enumerate(elam.reshape(-1)):
             c.elam[i] = v
         c.energy_form = energy_form
+        c.variable_mobility = p.get("variable_mobility", 0)
         self.cfg = c
         self.u = np.ascontiguousarray(p["fields"].copy())
         self.felas = np.zeros((max(p["nac"], 1), n, n, n))

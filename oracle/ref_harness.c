@@ -49,6 +49,21 @@ static int g_check = 1;
 void ref_set_check(int on) { g_check = on; }
 double ref_time(void) { return g_tt; }
 
+/* update_M_C (mobility.c:860-922) writes the mobility of three
+ * concentrations (ch[0..2].M and .C) whatever nch is.  With fewer than three
+ * conserved fields the harness gives ch[] three entries (the reference's own
+ * ones first, then two with only an M array), so that the reference's
+ * routine runs within bounds; only ch[0..nch-1] enter the step. */
+static void pad_ch_for_mobility(void) {
+  struct Cahn_Hilliard *p;
+  int m;
+  if (!VariableMobility || nch >= 3) return;
+  p = (struct Cahn_Hilliard *)calloc(3, sizeof *p);
+  memcpy(p, ch, (size_t)nch * sizeof *p);
+  for (m = nch; m < 3; m++) p[m].M = (double *)calloc((size_t)nx * ny * nz, sizeof(double));
+  ch = p;
+}
+
 /* Parses input<suffix>.ini in the working directory (format of ScLETD.c:16-34)
  * and runs the reference's set-up.  Returns 0 on success. */
 int ref_init(const char *suffix) {
@@ -78,6 +93,7 @@ int ref_init(const char *suffix) {
   fclose(file);
   if (ELASTIC != NEITHER_FUNCTION) elastic_input();
   alloc_vars();
+  pad_ch_for_mobility();
   init_vars();
   if (ANISOTROPIC == 1) anisotropic_input();
   define_mpi_type();

@@ -380,6 +380,113 @@ static void ch_boundary_mu(const orc_cfg *c, const double *u, double *mu) {
       }
 }
 
+/* update_M_C (mobility.c:860-922): the mobility of the first concentration
+ * (Cu) from the first order parameter, M = cu0 (1 - cu0) (DA (1 - eta0) +
+ * DG eta0), with DA = 1 and DG the ratio of the two phases' Arrhenius
+ * diffusivities D0 exp(-Q / RT) at T = 823 K (R = 8.314472). */
+void orc_mobility_constants(double *m0, double *dg) {
+  const double rt = 8.314472 * 823.0, cu0 = 0.15;
+  const double da = 4.7e-5 * exp(-2.44e5 / rt);
+  *dg = (4.3e-5 * exp(-2.80e5 / rt)) / da;
+  *m0 = cu0 * (1.0 - cu0);
+}
+
+/* laplace (mobility.c:12-239) on a periodic single rank: the 7-point
+ * Laplacian with values outside the block taken as zero. */
+static void lap_zero_outside(const orc_cfg *c, const double *a, double *la) {
+  int n = c->n, z;
+  size_t nn = (size_t)n * n;
+#pragma omp parallel for
+  for (z = 0; z < n; z++) {
+    int y, x;
+    for (y = 0; y < n; y++)
+      for (x = 0; x < n; x++) {
+        size_t l = IDX(n, z, y, x);
+        double al = x > 0 ? a[l - 1] : 0.0, ar = x < n - 1 ? a[l + 1] : 0.0;
+        double at = y > 0 ? a[l - n] : 0.0, ab = y < n - 1 ? a[l + n] : 0.0;
+        double af = z > 0 ? a[l - nn] : 0.0, ak = z < n - 1 ? a[l + nn] : 0.0;
+        double tmp = 0.0;
+        tmp += (al + ar - 2.0 * a[l]) / c->h[0] / c->h[0];
+        tmp += (at + ab - 2.0 * a[l]) / c->h[1] / c->h[1];
+        tmp += (af + ak - 2.0 * a[l]) / c->h[2] / c->h[2];
+        la[l] = tmp;
+      }
+  }
+}
+
+/* ch_calc_FU_VariableMobility (mobility.c:838-858) of the single conserved
+ * field with update_M_C run first (calc.c:475-481):
+ *   f0 = -LCI KCI c + LCI CH_f                       (ch_calc_F0, SWITCH_CH_FIELD1)
+ *   f1 = -C lap0(-f0 + KCI c + epn2 c_out / h^2) - C mu_out / h^2   (ch_calc_F1)
+ *   f2 = -div0((M - C) grad(epn2 lap0(c) - f0 + epn2 c_out / h^2))  (ch_calc_F2)
+ *   N  = LCI (f1 + f2)
+ * with C the largest M over the block (update_M_C), lap0 and div0 zero
+ * outside the block (ch_divergence_M_gradient, mobility.c:435-722: the
+ * face flux (m_q + m) (a_q - a) / (2 h^2), m_q = a_q = 0 outside), c_out
+ * the periodic image outside each face and mu_out the boundary chemical
+ * potential there (ch_mu). */
+static void ch_rhs_variable_mobility(const orc_cfg *c, const double *u, double *f, double *faces, double *tmp) {
+  int n = c->n, z;
+  size_t n3 = (size_t)n * n * n, nn = (size_t)n * n, l;
+  const double *cm = u + (size_t)c->nac * n3, *e0 = u;
+  double *M = tmp, *f0 = tmp + n3, *t = tmp + 2 * n3, *g = tmp + 3 * n3;
+  double m0, dg, C = -1.0e30;
+  orc_mobility_constants(&m0, &dg);
+  for (l = 0; l < n3; l++) {
+    M[l] = m0 * (1.0 * (1.0 - e0[l]) + dg * e0[l]);
+    C = C > M[l] ? C : M[l];
+  }
+#pragma omp parallel for
+  for (z = 0; z < n; z++) {
+    int y, x, k;
+    for (y = 0; y < n; y++)
+      for (x = 0; x < n; x++) {
+        double e[4];
+        size_t q = IDX(n, z, y, x);
+        for (k = 0; k < c->nac; k++) e[k] = u[(size_t)k * n3 + q];
+        f0[q] = -c->LCI * c->KCI * cm[q];
+        f0[q] += c->LCI * ch_f(c, e, cm[q]);
+      }
+  }
+  orc_boundary_values(n, cm, faces);
+  /* f1 */
+  for (l = 0; l < n3; l++) t[l] = -f0[l] + c->KCI * cm[l];
+  add_faces(n, t, faces, c->epn2, c->h);
+  lap_zero_outside(c, t, f);
+  for (l = 0; l < n3; l++) f[l] = -C * f[l];
+  ch_boundary_mu(c, u, g);
+  add_faces(n, f, g, -C, c->h);
+  /* f2 */
+  lap_zero_outside(c, cm, t);
+  for (l = 0; l < n3; l++) t[l] = c->epn2 * t[l] - f0[l];
+  add_faces(n, t, faces, c->epn2, c->h);
+  for (l = 0; l < n3; l++) M[l] = M[l] - C;
+#pragma omp parallel for
+  for (z = 0; z < n; z++) {
+    int y, x;
+    for (y = 0; y < n; y++)
+      for (x = 0; x < n; x++) {
+        size_t q = IDX(n, z, y, x);
+        const double am = t[q], mm = M[q];
+        const double al = x > 0 ? t[q - 1] : 0.0, ml = x > 0 ? M[q - 1] : 0.0;
+        const double ar = x < n - 1 ? t[q + 1] : 0.0, mr = x < n - 1 ? M[q + 1] : 0.0;
+        const double at = y > 0 ? t[q - n] : 0.0, mt = y > 0 ? M[q - n] : 0.0;
+        const double ab = y < n - 1 ? t[q + n] : 0.0, mb = y < n - 1 ? M[q + n] : 0.0;
+        const double af = z > 0 ? t[q - nn] : 0.0, mf = z > 0 ? M[q - nn] : 0.0;
+        const double ak = z < n - 1 ? t[q + nn] : 0.0, mk = z < n - 1 ? M[q + nn] : 0.0;
+        double d = 0.0;
+        d += (ml + mm) * (al - am) / 2.0 / c->h[0] / c->h[0];
+        d += (mr + mm) * (ar - am) / 2.0 / c->h[0] / c->h[0];
+        d += (mt + mm) * (at - am) / 2.0 / c->h[1] / c->h[1];
+        d += (mb + mm) * (ab - am) / 2.0 / c->h[1] / c->h[1];
+        d += (mf + mm) * (af - am) / 2.0 / c->h[2] / c->h[2];
+        d += (mk + mm) * (ak - am) / 2.0 / c->h[2] / c->h[2];
+        g[q] = -d;
+      }
+  }
+  for (l = 0; l < n3; l++) f[l] = c->LCI * (f[l] + g[l]);
+}
+
 void orc_rhs(const orc_cfg *c, const double *u, const double *felas, double *out) {
   int n = c->n, m, z;
   size_t n3 = (size_t)n * n * n, nn = (size_t)n * n;
@@ -415,8 +522,9 @@ void orc_rhs(const orc_cfg *c, const double *u, const double *felas, double *out
       for (l = 0; l < n3; l++) f[l] -= c->LE * c->elastic_scale * felas[(size_t)m * n3 + l];
     }
   }
+  if (c->variable_mobility && c->nch > 0) ch_rhs_variable_mobility(c, u, out + (size_t)c->nac * n3, faces, tmp);
   /* ch_calc_FU_ConstantMobility (calc.c:70-473). */
-  for (m = 0; m < c->nch; m++) {
+  for (m = 0; m < (c->variable_mobility ? 0 : c->nch); m++) {
     const double *cm = u + (size_t)(c->nac + m) * n3;
     double *f = out + (size_t)(c->nac + m) * n3;
     double *t = tmp;

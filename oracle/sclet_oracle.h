@@ -41,6 +41,9 @@ typedef struct {
    * (0: the reference's hard-coded 2-3-4 form, 1: the 2-4-6 plugin form). */
   double elam[4][3][3];
   int energy_form;
+  /* 1: variable-mobility Cahn-Hilliard right-hand side (VariableMobility of
+   * the ini, ch_calc_FU_VariableMobility, mobility.c:838-858) */
+  int variable_mobility;
 } orc_cfg;
 
 /* Ghost fill of one n^3 block in place (transfer(), trans.c:1939-1996, on a
@@ -66,6 +69,10 @@ void orc_elastic(const orc_cfg *c, const double *eta, double *felas, double *fst
  * ch_calc_FU_ConstantMobility, calc.c:70-473).  u: filled fields
  * ((nac+nch)*n^3), felas as from orc_elastic, out: (nac+nch)*n^3. */
 void orc_rhs(const orc_cfg *c, const double *u, const double *felas, double *out);
+
+/* Constants of update_M_C (mobility.c:860-922) for the first concentration:
+ * M(eta0) = m0 (1 (1 - eta0) + dg eta0). */
+void orc_mobility_constants(double *m0, double *dg);
 
 /* Mode-n product with cyclic rotation: out[b + n*c + n*n*a'] =
  * sum_a M(a', a) * in[a + n*b + n*n*c], M column-major (PUX/PUY/PUZ,

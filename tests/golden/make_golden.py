@@ -63,13 +63,18 @@ def main(only=None):
         with tempfile.TemporaryDirectory() as td:
             c = case_defs.write(name, td)
             lib = LIB_ORIG if c.physics == 1 else LIB
+            # the reference binary itself runs only where its main() is safe:
+            # its variable-mobility path writes three concentrations' mobility
+            # (update_M_C, mobility.c:860-922), so with nch < 3 only the
+            # harness (which gives ch[] three entries) runs it
+            own_check = c.physics == 1 or c.variable_mobility == 1
             rhs = os.path.join(td, "rhs.npz")
             run = os.path.join(td, "run.npz")
             subprocess.run([sys.executable, RUNNER, lib, td, name, "0", rhs, "--rhs"], check=True,
                            capture_output=True)
             subprocess.run([sys.executable, RUNNER, lib, td, name, str(c.steps), run]
-                           + (["--check"] if c.physics == 1 else []), check=True, capture_output=True)
-            if c.physics != 1:
+                           + (["--check"] if own_check else []), check=True, capture_output=True)
+            if not own_check:
                 subprocess.run([BIN, name], cwd=td, check=True, capture_output=True)
             R, S = np.load(rhs), np.load(run)
             out = {}

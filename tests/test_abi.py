@@ -108,3 +108,24 @@ def test_physics_plugin_selection(sclet_lib, tmp_path):
     p2 = sclet_lib.Params()
     assert L.sclet_read_case(str(tmp_path).encode(), b"formula234", ctypes.byref(p2)) == 1  # SCLET_ERR_ARG
     assert c.physics == 1
+
+
+def test_variable_mobility_needs_its_fields(sclet_lib, tmp_path):
+    """VariableMobility = 1 takes the mobility of the one conserved field from
+    the first order parameter (update_M_C, mobility.c:860-922): without a
+    Cahn-Hilliard field or an order parameter the context is refused before
+    any device work; a value other than 0 or 1 is an argument error."""
+    L = sclet_lib.lib()
+    case = cases.Case(big_n=8, nac=1, nch=1, steps=1, variable_mobility=1, suffix="vm")
+    cases.write_case(case, str(tmp_path))
+    p = sclet_lib.read_case(str(tmp_path), "vm")
+    assert p.variable_mobility == 1
+    h = ctypes.c_void_p()
+    p.nch = 0
+    assert L.sclet_create(ctypes.byref(p), sclet_lib.FP64, 0, ctypes.byref(h)) == 4  # SCLET_ERR_UNSUPPORTED
+    assert b"Cahn-Hilliard" in L.sclet_last_error(None)
+    p.nch, p.nac = 1, 0
+    p.elastic = 0
+    assert L.sclet_create(ctypes.byref(p), sclet_lib.FP64, 0, ctypes.byref(h)) == 4
+    p.nac, p.variable_mobility = 1, 2
+    assert L.sclet_create(ctypes.byref(p), sclet_lib.FP64, 0, ctypes.byref(h)) == 1  # SCLET_ERR_ARG

@@ -3,6 +3,7 @@ with FP32 accumulation, FP32 stencils and FFT, FP64 diagnostics.  Checked
 against the plain FP64 form of the same library (itself checked against the
 reference and the oracle): rel L2 <= 1e-5 per field, energy within 1e-6
 relative."""
+import dataclasses
 import tempfile
 
 import numpy as np
@@ -75,6 +76,17 @@ def test_mixed_matches_fp64_beta_omega_64(sclet_lib):
     """64^3 beta->omega physics (4 order parameters, elasticity), 200 steps."""
     case = cases.Case(big_n=64, steps=200, seed=77, suffix="m64")
     errs, eerr = _mixed_vs_fp64(sclet_lib, case, 200)
+    assert max(errs) <= 1e-5, errs
+    assert eerr <= 1e-6, eerr
+
+
+def test_mixed_matches_fp64_variable_mobility(sclet_lib):
+    """Variable-mobility CH coupled to four order parameters (64^3, the
+    mobility following the first order parameter over [0, 0.9], elastic,
+    anisotropic), 200 steps: per field <= 1e-5, energy curve within 1e-6."""
+    case = bench.workload(64, seed=5)
+    case = dataclasses.replace(case, variable_mobility=1, eta_range=(0.0, 0.9), suffix="vm64")
+    errs, eerr = _mixed_vs_fp64(sclet_lib, case, 200, every=50)
     assert max(errs) <= 1e-5, errs
     assert eerr <= 1e-6, eerr
 

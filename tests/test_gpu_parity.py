@@ -104,6 +104,22 @@ def test_all_options_match_oracle(tmp_path, sclet_lib, oracle_lib):
     np.testing.assert_allclose(eg, eo, rtol=1e-10, atol=1e-13)
 
 
+def test_variable_mobility_matches_oracle(tmp_path, sclet_lib, oracle_lib):
+    """Variable-mobility Cahn-Hilliard (VariableMobility = 1, the mobility of
+    the first concentration following the first order parameter, which
+    ranges over [0, 0.9] here) with anisotropy, elasticity and ETD2, 32^3 for
+    20 steps against the oracle (itself pinned to the reference's own
+    update_M_C / ch_calc_FU_VariableMobility by the golden case varmob)."""
+    rng = np.random.default_rng(8)
+    case = cases.Case(big_n=32, nac=4, nch=1, etd2=1, anisotropic=1, kk=(0.5, 0.5, 0.5),
+                      lambdas=[np.diag([0.5, 0.5, 0.3]) + 0.05 * rng.standard_normal((3, 3)) for _ in range(4)],
+                      dt=0.005, epn2=1.0, steps=20, seed=22, eta_range=(0.0, 0.9), variable_mobility=1,
+                      suffix="vmob")
+    errs, eg, eo = _oracle_vs_gpu(tmp_path, sclet_lib, oracle_lib, case, 20)
+    assert max(errs) <= 1e-10, errs
+    np.testing.assert_allclose(eg, eo, rtol=1e-10, atol=1e-13)
+
+
 def test_beta_omega_64_cubed_1000_steps(tmp_path, sclet_lib):
     """The beta->omega plain-ETD workload (64^3, 4 order parameters, Landau
     2-4-6, cubic elasticity, dt = 0.01) for 1000 steps against the
