@@ -37,9 +37,10 @@
 // 128 a'] (input rows on the MMA's M side, eigen-modes a' on its N side, so
 // the last a'-tile runs N = its live rows rounded up to 16 rather than a full
 // 128).  A CTA takes whole groups (every a'-tile of one input tile, a'-tiles
-// fastest, groups round robin), so the CTAs stay balanced and the input
-// slices come from HBM once (the group's later a'-tiles read them from L2);
-// the matrix slices stay in L2.  Every CTA loads its own operand tiles (no
+// fastest, groups round robin, tensor fastest), so the CTAs stay balanced,
+// the input slices come from HBM once (the group's later a'-tiles read them
+// from L2) and the tensors of one input tile share the fused update's
+// coefficient reads through L2; the matrix slices stay in L2.  Every CTA loads its own operand tiles (no
 // cluster).
 // A = input slices (128 r rows x 32 k, 64-byte swizzle), B = matrix slices
 // (128 a' rows x 32 k), both K-major, in a three-stage mbarrier pipeline
@@ -125,7 +126,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       int it = 0;
       // the self-test leaves every barrier without arrivals (no copy is issued)
       for (int u = g.idle ? mine : 0; u < mine; u++) {
-        const TileIdx ti = cta_tile(u, a_tiles, r_tiles, blockIdx.x, gridDim.x);
+        const TileIdx ti = cta_tile(u, a_tiles, g.count, blockIdx.x, gridDim.x);
         for (int kb = 0; kb < nkb; kb++, it++) {
           const int s = it % STAGES;
           if (it >= STAGES && !mbar_wait(&empty_bar[s], ((it / STAGES) & 1) ^ 1)) {
@@ -160,6 +161,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       const int pairA[11] = {0, 3, 2, 1, 0, 2, 1, 0, 1, 0, 0};  // input slice
       const int pairB[11] = {4, 0, 1, 2, 3, 0, 1, 2, 0, 1, 0};  // matrix slice
       const int cls[11] = {3, 3, 3, 3, 3, 2, 2, 2, 1, 1, 0};
+      const bool last_two = g.n - (nkb - 1) * BK > 16;  // the last k-block needs both k-steps
       int it = 0, j = 0;
       for (int u = 0; u < mine && !*(volatile int *)&failed; u++, j++) {
         const int b = j % NBUF;
@@ -183,6 +185,10 @@ __global__ void __launch_bounds__(THREADS, 1)
           const uint32_t sb = sa + NP * PLANE_A;
 #pragma unroll
           for (int ks = 0; ks < BK / 16; ks++) {
+            // the last k-block's second k-step holds only zero columns when
+            // n mod 32 is in 1..16: skipped (adding zero products changes no
+            // accumulator)
+            if (ks > 0 && kb == nkb - 1 && !last_two) continue;
             const uint32_t koff = ks * 32;
             const bool first = (kb == 0 && ks == 0);
 #pragma unroll
@@ -234,7 +240,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         break;
       }
       fence_after();
-      const TileIdx ti = cta_tile(u, a_tiles, r_tiles, blockIdx.x, gridDim.x);
+      const TileIdx ti = cta_tile(u, a_tiles, g.count, blockIdx.x, gridDim.x);
       const int at0 = ti.a_tile * BN;
       const int nch = (min(BN, g.n - at0) + 31) / 32;  // 32-column chunks holding live a'
       const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * ACC_COLS);

@@ -140,16 +140,19 @@ __device__ __forceinline__ float pow2_scale(float m) {
 }
 
 // The u-th output tile of CTA `cta`: each CTA takes whole groups (every
-// a'-tile of one input tile, a'-tiles fastest), groups dealt round robin.
-// Every group costs the same (the last a'-tile is narrower), so the CTAs stay
-// balanced, and the group's input tile, read once from HBM by its first
-// a'-tile, is read again from L2 by the CTA's next a'-tiles.
-__device__ __forceinline__ TileIdx cta_tile(int u, int a_tiles, int r_tiles, int cta, int grid) {
+// a'-tile of one input tile, a'-tiles fastest), groups dealt round robin with
+// the tensor fastest.  Every group costs the same (the last a'-tile is
+// narrower), so the CTAs stay balanced; the group's input tile, read once
+// from HBM by its first a'-tile, is read again from L2 by the CTA's next
+// a'-tiles; and the tensors of one input tile run side by side on
+// neighbouring CTAs, so the fused update's coefficient tables (one per field
+// kind) come from HBM about once per input tile.
+__device__ __forceinline__ TileIdx cta_tile(int u, int a_tiles, int count, int cta, int grid) {
   TileIdx x;
   const int grp = cta + (u / a_tiles) * grid;
   x.a_tile = u % a_tiles;
-  x.r_tile = grp % r_tiles;
-  x.t = grp / r_tiles;
+  x.t = grp % count;
+  x.r_tile = grp / count;
   return x;
 }
 
