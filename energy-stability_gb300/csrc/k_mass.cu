@@ -194,7 +194,8 @@ __global__ void to_pairs_kernel(double *w, long long count) {
 
 }  // namespace
 
-int mass_partials() { return 152 * 4; }
+// sixteen blocks per SM: enough loads in flight to stream the block from HBM
+int mass_partials() { return 152 * 16; }
 
 cudaError_t mass_weight(double *w, double *tmp, const double *g, const double *viT, int n, int which, const EtdCoef &ec,
                         cudaStream_t s) {

@@ -22,6 +22,7 @@
 namespace sclet {
 
 constexpr int ZC = 32;  // default z-planes per CTA of the Allen-Cahn kernel
+constexpr int PZ = 16;  // z-planes per CTA of the one-cell-per-thread CH kernels
 
 template <typename T>
 struct P {
@@ -99,7 +100,7 @@ constexpr int HX = RX + 4, HY = RY + 4;
 constexpr int PLANE = HX * HY;     // one haloed plane
 
 template <typename PL, typename T, int NAC, bool ANISO>
-__global__ void __launch_bounds__(RX * RY) rhs_ac_kernel(P<T> p0, const T *__restrict__ u, const T *__restrict__ felas,
+__global__ void __launch_bounds__(RX * RY, sizeof(T) == 4 ? 3 : 1) rhs_ac_kernel(P<T> p0, const T *__restrict__ u, const T *__restrict__ felas,
                                                          T *__restrict__ out) {
   extern __shared__ unsigned char smem_raw[];
   T *ring = reinterpret_cast<T *>(smem_raw);  // [nac][5][HY][HX]
@@ -223,34 +224,37 @@ __global__ void __launch_bounds__(RX * RY) rhs_ac_kernel(P<T> p0, const T *__res
 template <typename PL, typename T>
 __global__ void __launch_bounds__(RX * RY) rhs_ch_t_kernel(P<T> p0, const T *__restrict__ u, T *__restrict__ t) {
   const int n = p0.n;
-  const int run = blockIdx.z / n;  // blockIdx.z = run x z
-  const int x = blockIdx.x * RX + threadIdx.x, y = blockIdx.y * RY + threadIdx.y, z = blockIdx.z - run * n;
+  const int zch = (n + PZ - 1) / PZ;  // blockIdx.z = run x chunk of PZ planes
+  const int run = blockIdx.z / zch, z0 = (blockIdx.z - run * zch) * PZ, z1 = z0 + PZ < n ? z0 + PZ : n;
+  const int x = blockIdx.x * RX + threadIdx.x, y = blockIdx.y * RY + threadIdx.y;
   if (x >= n || y >= n) return;
   const size_t n3 = (size_t)n * n * n;
   P<T> p = p0;
   if (p0.krun) p.K[0] = (T)p0.krun[run];
   u += (size_t)run * p.F * n3;
   t += (size_t)run * n3;
-  const size_t l = ((size_t)z * n + y) * n + x;
-  const T *cf = u + p.nac * n3;
-  T e[4] = {(T)0, (T)0, (T)0, (T)0};
+  for (int z = z0; z < z1; z++) {
+    const size_t l = ((size_t)z * n + y) * n + x;
+    const T *cf = u + p.nac * n3;
+    T e[4] = {(T)0, (T)0, (T)0, (T)0};
 #pragma unroll
-  for (int m = 0; m < 4; m++)
-    if (m < p.nac) e[m] = u[m * n3 + l];
-  const T c = cf[l];
-  T v = -p.LCI * p.KCI * c;
-  v += p.LCI * ch_f<PL>(p, e, c);
-  if (x == 0 || x == n - 1 || y == 0 || y == n - 1 || z == 0 || z == n - 1) {
-    const int iz = img(n, z), iy = img(n, y), ix = img(n, x), lo = img(n, -1), hi = img(n, n);
-    const T w = p.LCI * p.epn2;
-    if (x == 0) v -= w * cf[L3(n, iz, iy, lo)] * p.ih2x;
-    if (x == n - 1) v -= w * cf[L3(n, iz, iy, hi)] * p.ih2x;
-    if (y == 0) v -= w * cf[L3(n, iz, lo, ix)] * p.ih2y;
-    if (y == n - 1) v -= w * cf[L3(n, iz, hi, ix)] * p.ih2y;
-    if (z == 0) v -= w * cf[L3(n, lo, iy, ix)] * p.ih2z;
-    if (z == n - 1) v -= w * cf[L3(n, hi, iy, ix)] * p.ih2z;
+    for (int m = 0; m < 4; m++)
+      if (m < p.nac) e[m] = u[m * n3 + l];
+    const T c = cf[l];
+    T v = -p.LCI * p.KCI * c;
+    v += p.LCI * ch_f<PL>(p, e, c);
+    if (x == 0 || x == n - 1 || y == 0 || y == n - 1 || z == 0 || z == n - 1) {
+      const int iz = img(n, z), iy = img(n, y), ix = img(n, x), lo = img(n, -1), hi = img(n, n);
+      const T w = p.LCI * p.epn2;
+      if (x == 0) v -= w * cf[L3(n, iz, iy, lo)] * p.ih2x;
+      if (x == n - 1) v -= w * cf[L3(n, iz, iy, hi)] * p.ih2x;
+      if (y == 0) v -= w * cf[L3(n, iz, lo, ix)] * p.ih2y;
+      if (y == n - 1) v -= w * cf[L3(n, iz, hi, ix)] * p.ih2y;
+      if (z == 0) v -= w * cf[L3(n, lo, iy, ix)] * p.ih2z;
+      if (z == n - 1) v -= w * cf[L3(n, hi, iy, ix)] * p.ih2z;
+    }
+    t[l] = v;
   }
-  t[l] = v;
 }
 
 // Boundary chemical potential at periodic image cell (z,y,x) (ch_mu).
@@ -275,8 +279,9 @@ template <typename PL, typename T>
 __global__ void __launch_bounds__(RX * RY) rhs_ch_lap_kernel(P<T> p0, const T *__restrict__ u, const T *__restrict__ t,
                                                              T *__restrict__ out) {
   const int n = p0.n;
-  const int run = blockIdx.z / n;  // blockIdx.z = run x z
-  const int x = blockIdx.x * RX + threadIdx.x, y = blockIdx.y * RY + threadIdx.y, z = blockIdx.z - run * n;
+  const int zch = (n + PZ - 1) / PZ;  // blockIdx.z = run x chunk of PZ planes
+  const int run = blockIdx.z / zch, z0 = (blockIdx.z - run * zch) * PZ, z1 = z0 + PZ < n ? z0 + PZ : n;
+  const int x = blockIdx.x * RX + threadIdx.x, y = blockIdx.y * RY + threadIdx.y;
   if (x >= n || y >= n) return;
   P<T> p = p0;
   if (p0.krun) p.K[0] = (T)p0.krun[run];
@@ -287,24 +292,26 @@ __global__ void __launch_bounds__(RX * RY) rhs_ch_lap_kernel(P<T> p0, const T *_
     out += (size_t)run * p.F * n3;
   }
   const size_t nn = (size_t)n * n;
-  const size_t l = (size_t)z * nn + (size_t)y * n + x;
-  const T tc = t[l];
-  const T fl = x > 0 ? t[l - 1] : (T)0, fr = x < n - 1 ? t[l + 1] : (T)0;
-  const T ft = y > 0 ? t[l - n] : (T)0, fb = y < n - 1 ? t[l + n] : (T)0;
-  const T ff = z > 0 ? t[l - nn] : (T)0, fk = z < n - 1 ? t[l + nn] : (T)0;
-  T v = (fl + fr - (T)2 * tc) * p.ih2x;
-  v += (ft + fb - (T)2 * tc) * p.ih2y;
-  v += (ff + fk - (T)2 * tc) * p.ih2z;
-  if (x == 0 || x == n - 1 || y == 0 || y == n - 1 || z == 0 || z == n - 1) {
-    const int iz = img(n, z), iy = img(n, y), ix = img(n, x), lo = img(n, -1), hi = img(n, n);
-    if (x == 0) v -= ch_mu_at<PL>(p, u, iz, iy, lo) * p.ih2x;
-    if (x == n - 1) v -= ch_mu_at<PL>(p, u, iz, iy, hi) * p.ih2x;
-    if (y == 0) v -= ch_mu_at<PL>(p, u, iz, lo, ix) * p.ih2y;
-    if (y == n - 1) v -= ch_mu_at<PL>(p, u, iz, hi, ix) * p.ih2y;
-    if (z == 0) v -= ch_mu_at<PL>(p, u, lo, iy, ix) * p.ih2z;
-    if (z == n - 1) v -= ch_mu_at<PL>(p, u, hi, iy, ix) * p.ih2z;
+  for (int z = z0; z < z1; z++) {
+    const size_t l = (size_t)z * nn + (size_t)y * n + x;
+    const T tc = t[l];
+    const T fl = x > 0 ? t[l - 1] : (T)0, fr = x < n - 1 ? t[l + 1] : (T)0;
+    const T ft = y > 0 ? t[l - n] : (T)0, fb = y < n - 1 ? t[l + n] : (T)0;
+    const T ff = z > 0 ? t[l - nn] : (T)0, fk = z < n - 1 ? t[l + nn] : (T)0;
+    T v = (fl + fr - (T)2 * tc) * p.ih2x;
+    v += (ft + fb - (T)2 * tc) * p.ih2y;
+    v += (ff + fk - (T)2 * tc) * p.ih2z;
+    if (x == 0 || x == n - 1 || y == 0 || y == n - 1 || z == 0 || z == n - 1) {
+      const int iz = img(n, z), iy = img(n, y), ix = img(n, x), lo = img(n, -1), hi = img(n, n);
+      if (x == 0) v -= ch_mu_at<PL>(p, u, iz, iy, lo) * p.ih2x;
+      if (x == n - 1) v -= ch_mu_at<PL>(p, u, iz, iy, hi) * p.ih2x;
+      if (y == 0) v -= ch_mu_at<PL>(p, u, iz, lo, ix) * p.ih2y;
+      if (y == n - 1) v -= ch_mu_at<PL>(p, u, iz, hi, ix) * p.ih2y;
+      if (z == 0) v -= ch_mu_at<PL>(p, u, lo, iy, ix) * p.ih2z;
+      if (z == n - 1) v -= ch_mu_at<PL>(p, u, hi, iy, ix) * p.ih2z;
+    }
+    out[l] = v;
   }
-  out[l] = v;
 }
 
 // ---- variable-mobility Cahn-Hilliard ---------------------------------------
@@ -366,43 +373,46 @@ __global__ void __launch_bounds__(256) mob_final_kernel(const double *__restrict
 template <typename PL, typename T>
 __global__ void __launch_bounds__(RX * RY) mob_t_kernel(P<T> p0, const T *__restrict__ u, T *__restrict__ tt) {
   const int n = p0.n;
-  const int run = blockIdx.z / n;
-  const int x = blockIdx.x * RX + threadIdx.x, y = blockIdx.y * RY + threadIdx.y, z = blockIdx.z - run * n;
+  const int zch = (n + PZ - 1) / PZ;  // blockIdx.z = run x chunk of PZ planes
+  const int run = blockIdx.z / zch, z0 = (blockIdx.z - run * zch) * PZ, z1 = z0 + PZ < n ? z0 + PZ : n;
+  const int x = blockIdx.x * RX + threadIdx.x, y = blockIdx.y * RY + threadIdx.y;
   if (x >= n || y >= n) return;
   const size_t n3 = (size_t)n * n * n, nn = (size_t)n * n;
   P<T> p = p0;
   if (p0.krun) p.K[0] = (T)p0.krun[run];
   u += (size_t)run * p.F * n3;
   T *t1 = tt + (size_t)run * 2 * n3, *t2 = t1 + n3;
-  const size_t l = (size_t)z * nn + (size_t)y * n + x;
-  const T *cf = u + p.nac * n3;
-  T e[4] = {(T)0, (T)0, (T)0, (T)0};
+  for (int z = z0; z < z1; z++) {
+    const size_t l = (size_t)z * nn + (size_t)y * n + x;
+    const T *cf = u + p.nac * n3;
+    T e[4] = {(T)0, (T)0, (T)0, (T)0};
 #pragma unroll
-  for (int m = 0; m < 4; m++)
-    if (m < p.nac) e[m] = u[m * n3 + l];
-  const T c = cf[l];
-  T f0 = -p.LCI * p.KCI * c;
-  f0 += p.LCI * ch_f<PL>(p, e, c);
-  const T cl = x > 0 ? cf[l - 1] : (T)0, cr = x < n - 1 ? cf[l + 1] : (T)0;
-  const T ct = y > 0 ? cf[l - n] : (T)0, cb = y < n - 1 ? cf[l + n] : (T)0;
-  const T cz = z > 0 ? cf[l - nn] : (T)0, ck = z < n - 1 ? cf[l + nn] : (T)0;
-  T la = (cl + cr - (T)2 * c) * p.ih2x;
-  la += (ct + cb - (T)2 * c) * p.ih2y;
-  la += (cz + ck - (T)2 * c) * p.ih2z;
-  T a = -f0 + p.KCI * c;
-  T b = p.epn2 * la - f0;
-  if (x == 0 || x == n - 1 || y == 0 || y == n - 1 || z == 0 || z == n - 1) {
-    const int iz = img(n, z), iy = img(n, y), ix = img(n, x), lo = img(n, -1), hi = img(n, n);
-    T w;
-    if (x == 0) { w = p.epn2 * cf[L3(n, iz, iy, lo)] * p.ih2x; a += w; b += w; }
-    if (x == n - 1) { w = p.epn2 * cf[L3(n, iz, iy, hi)] * p.ih2x; a += w; b += w; }
-    if (y == 0) { w = p.epn2 * cf[L3(n, iz, lo, ix)] * p.ih2y; a += w; b += w; }
-    if (y == n - 1) { w = p.epn2 * cf[L3(n, iz, hi, ix)] * p.ih2y; a += w; b += w; }
-    if (z == 0) { w = p.epn2 * cf[L3(n, lo, iy, ix)] * p.ih2z; a += w; b += w; }
-    if (z == n - 1) { w = p.epn2 * cf[L3(n, hi, iy, ix)] * p.ih2z; a += w; b += w; }
+    for (int m = 0; m < 4; m++)
+      if (m < p.nac) e[m] = u[m * n3 + l];
+    const T c = cf[l];
+    T f0 = -p.LCI * p.KCI * c;
+    f0 += p.LCI * ch_f<PL>(p, e, c);
+    const T cl = x > 0 ? cf[l - 1] : (T)0, cr = x < n - 1 ? cf[l + 1] : (T)0;
+    const T ct = y > 0 ? cf[l - n] : (T)0, cb = y < n - 1 ? cf[l + n] : (T)0;
+    const T cz = z > 0 ? cf[l - nn] : (T)0, ck = z < n - 1 ? cf[l + nn] : (T)0;
+    T la = (cl + cr - (T)2 * c) * p.ih2x;
+    la += (ct + cb - (T)2 * c) * p.ih2y;
+    la += (cz + ck - (T)2 * c) * p.ih2z;
+    T a = -f0 + p.KCI * c;
+    T b = p.epn2 * la - f0;
+    if (x == 0 || x == n - 1 || y == 0 || y == n - 1 || z == 0 || z == n - 1) {
+      const int iz = img(n, z), iy = img(n, y), ix = img(n, x), lo = img(n, -1), hi = img(n, n);
+      T w;
+      if (x == 0) { w = p.epn2 * cf[L3(n, iz, iy, lo)] * p.ih2x; a += w; b += w; }
+      if (x == n - 1) { w = p.epn2 * cf[L3(n, iz, iy, hi)] * p.ih2x; a += w; b += w; }
+      if (y == 0) { w = p.epn2 * cf[L3(n, iz, lo, ix)] * p.ih2y; a += w; b += w; }
+      if (y == n - 1) { w = p.epn2 * cf[L3(n, iz, hi, ix)] * p.ih2y; a += w; b += w; }
+      if (z == 0) { w = p.epn2 * cf[L3(n, lo, iy, ix)] * p.ih2z; a += w; b += w; }
+      if (z == n - 1) { w = p.epn2 * cf[L3(n, hi, iy, ix)] * p.ih2z; a += w; b += w; }
+    }
+    t1[l] = a;
+    t2[l] = b;
   }
-  t1[l] = a;
-  t2[l] = b;
 }
 
 // N = LCI (f1 + f2) of every cell (blockIdx.z = run x z)
@@ -410,8 +420,9 @@ template <typename PL, typename T>
 __global__ void __launch_bounds__(RX * RY) mob_n_kernel(P<T> p0, const T *__restrict__ u, const T *__restrict__ tt,
                                                         const double *__restrict__ cmax, T *__restrict__ out) {
   const int n = p0.n;
-  const int run = blockIdx.z / n;
-  const int x = blockIdx.x * RX + threadIdx.x, y = blockIdx.y * RY + threadIdx.y, z = blockIdx.z - run * n;
+  const int zch = (n + PZ - 1) / PZ;  // blockIdx.z = run x chunk of PZ planes
+  const int run = blockIdx.z / zch, z0 = (blockIdx.z - run * zch) * PZ, z1 = z0 + PZ < n ? z0 + PZ : n;
+  const int x = blockIdx.x * RX + threadIdx.x, y = blockIdx.y * RY + threadIdx.y;
   if (x >= n || y >= n) return;
   const size_t n3 = (size_t)n * n * n, nn = (size_t)n * n;
   P<T> p = p0;
@@ -420,54 +431,56 @@ __global__ void __launch_bounds__(RX * RY) mob_n_kernel(P<T> p0, const T *__rest
   out += (size_t)run * p.F * n3;
   const T *t1 = tt + (size_t)run * 2 * n3, *t2 = t1 + n3;
   const T C = (T)cmax[run];
-  const size_t l = (size_t)z * nn + (size_t)y * n + x;
-  // f1 = -C lap0(t1) - C mu_out / h^2
-  const T tc = t1[l];
-  const T al = x > 0 ? t1[l - 1] : (T)0, ar = x < n - 1 ? t1[l + 1] : (T)0;
-  const T at = y > 0 ? t1[l - n] : (T)0, ab = y < n - 1 ? t1[l + n] : (T)0;
-  const T af = z > 0 ? t1[l - nn] : (T)0, ak = z < n - 1 ? t1[l + nn] : (T)0;
-  T la = (al + ar - (T)2 * tc) * p.ih2x;
-  la += (at + ab - (T)2 * tc) * p.ih2y;
-  la += (af + ak - (T)2 * tc) * p.ih2z;
-  T f1 = -C * la;
-  if (x == 0 || x == n - 1 || y == 0 || y == n - 1 || z == 0 || z == n - 1) {
-    const int iz = img(n, z), iy = img(n, y), ix = img(n, x), lo = img(n, -1), hi = img(n, n);
-    if (x == 0) f1 -= C * ch_mu_at<PL>(p, u, iz, iy, lo) * p.ih2x;
-    if (x == n - 1) f1 -= C * ch_mu_at<PL>(p, u, iz, iy, hi) * p.ih2x;
-    if (y == 0) f1 -= C * ch_mu_at<PL>(p, u, iz, lo, ix) * p.ih2y;
-    if (y == n - 1) f1 -= C * ch_mu_at<PL>(p, u, iz, hi, ix) * p.ih2y;
-    if (z == 0) f1 -= C * ch_mu_at<PL>(p, u, lo, iy, ix) * p.ih2z;
-    if (z == n - 1) f1 -= C * ch_mu_at<PL>(p, u, hi, iy, ix) * p.ih2z;
+  for (int z = z0; z < z1; z++) {
+    const size_t l = (size_t)z * nn + (size_t)y * n + x;
+    // f1 = -C lap0(t1) - C mu_out / h^2
+    const T tc = t1[l];
+    const T al = x > 0 ? t1[l - 1] : (T)0, ar = x < n - 1 ? t1[l + 1] : (T)0;
+    const T at = y > 0 ? t1[l - n] : (T)0, ab = y < n - 1 ? t1[l + n] : (T)0;
+    const T af = z > 0 ? t1[l - nn] : (T)0, ak = z < n - 1 ? t1[l + nn] : (T)0;
+    T la = (al + ar - (T)2 * tc) * p.ih2x;
+    la += (at + ab - (T)2 * tc) * p.ih2y;
+    la += (af + ak - (T)2 * tc) * p.ih2z;
+    T f1 = -C * la;
+    if (x == 0 || x == n - 1 || y == 0 || y == n - 1 || z == 0 || z == n - 1) {
+      const int iz = img(n, z), iy = img(n, y), ix = img(n, x), lo = img(n, -1), hi = img(n, n);
+      if (x == 0) f1 -= C * ch_mu_at<PL>(p, u, iz, iy, lo) * p.ih2x;
+      if (x == n - 1) f1 -= C * ch_mu_at<PL>(p, u, iz, iy, hi) * p.ih2x;
+      if (y == 0) f1 -= C * ch_mu_at<PL>(p, u, iz, lo, ix) * p.ih2y;
+      if (y == n - 1) f1 -= C * ch_mu_at<PL>(p, u, iz, hi, ix) * p.ih2y;
+      if (z == 0) f1 -= C * ch_mu_at<PL>(p, u, lo, iy, ix) * p.ih2z;
+      if (z == n - 1) f1 -= C * ch_mu_at<PL>(p, u, hi, iy, ix) * p.ih2z;
+    }
+    // f2 = -div0((M - C) grad t2), M - C and t2 zero outside the block
+    const T *e0 = u;
+    const T bc = t2[l], mc = mobility(p, e0[l]) - C;
+    auto nb = [&](bool in, size_t q, T &bq, T &mq) {
+      bq = in ? t2[q] : (T)0;
+      mq = in ? mobility(p, e0[q]) - C : (T)0;
+    };
+    T bq, mq, d;
+    const T hx = (T)0.5 * p.ih2x, hy = (T)0.5 * p.ih2y, hz = (T)0.5 * p.ih2z;
+    nb(x > 0, l - 1, bq, mq);
+    d = (mq + mc) * (bq - bc) * hx;
+    nb(x < n - 1, l + 1, bq, mq);
+    d += (mq + mc) * (bq - bc) * hx;
+    nb(y > 0, l - n, bq, mq);
+    d += (mq + mc) * (bq - bc) * hy;
+    nb(y < n - 1, l + n, bq, mq);
+    d += (mq + mc) * (bq - bc) * hy;
+    nb(z > 0, l - nn, bq, mq);
+    d += (mq + mc) * (bq - bc) * hz;
+    nb(z < n - 1, l + nn, bq, mq);
+    d += (mq + mc) * (bq - bc) * hz;
+    out[(size_t)p.nac * n3 + l] = p.LCI * (f1 - d);
   }
-  // f2 = -div0((M - C) grad t2), M - C and t2 zero outside the block
-  const T *e0 = u;
-  const T bc = t2[l], mc = mobility(p, e0[l]) - C;
-  auto nb = [&](bool in, size_t q, T &bq, T &mq) {
-    bq = in ? t2[q] : (T)0;
-    mq = in ? mobility(p, e0[q]) - C : (T)0;
-  };
-  T bq, mq, d;
-  const T hx = (T)0.5 * p.ih2x, hy = (T)0.5 * p.ih2y, hz = (T)0.5 * p.ih2z;
-  nb(x > 0, l - 1, bq, mq);
-  d = (mq + mc) * (bq - bc) * hx;
-  nb(x < n - 1, l + 1, bq, mq);
-  d += (mq + mc) * (bq - bc) * hx;
-  nb(y > 0, l - n, bq, mq);
-  d += (mq + mc) * (bq - bc) * hy;
-  nb(y < n - 1, l + n, bq, mq);
-  d += (mq + mc) * (bq - bc) * hy;
-  nb(z > 0, l - nn, bq, mq);
-  d += (mq + mc) * (bq - bc) * hz;
-  nb(z < n - 1, l + nn, bq, mq);
-  d += (mq + mc) * (bq - bc) * hz;
-  out[(size_t)p.nac * n3 + l] = p.LCI * (f1 - d);
 }
 
 template <typename PL, typename T>
 static cudaError_t launch_rhs_pl(const Phys &ph, const T *u, const T *felas, T *out, T *scratch, cudaStream_t s) {
   P<T> p = to_p<T>(ph);
   long long n3 = (long long)ph.n * ph.n * ph.n;
-  const dim3 blk(RX, RY), grd((ph.n + RX - 1) / RX, (ph.n + RY - 1) / RY, ph.n * p.runs);
+  const dim3 blk(RX, RY), grd((ph.n + RX - 1) / RX, (ph.n + RY - 1) / RY, ((ph.n + PZ - 1) / PZ) * p.runs);
   if (ph.nac > 0) {
     const size_t smem = sizeof(T) * ph.nac * 5 * PLANE;
     const dim3 gac((ph.n + RX - 1) / RX, (ph.n + RY - 1) / RY, ((ph.n + p.zc - 1) / p.zc) * p.runs);
