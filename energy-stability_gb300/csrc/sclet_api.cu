@@ -154,22 +154,44 @@ __global__ void f32_to_f64(const float *__restrict__ a, double *__restrict__ b, 
 }
 
 // all F fields between the FP64 host layout and the state: FP32 states hold
-// the conserved fields (f >= nac) relative to shift; grid y = field
+// the conserved fields (f >= nac) relative to shift; grid y = field.  Four
+// values per thread and pass (16-byte FP32 and two 16-byte FP64 accesses)
+// where every field block starts on a 32-byte boundary (n^3 % 4 == 0).
 __global__ void fields_to_state(const double *__restrict__ a, float *__restrict__ b, long long n3, int nac,
                                 double shift, int F) {
   const double sh = (int)blockIdx.y % F >= nac ? shift : 0.0;
   const double *s = a + blockIdx.y * n3;
   float *d = b + blockIdx.y * n3;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3; i += (long long)gridDim.x * blockDim.x)
-    d[i] = (float)(s[i] - sh);
+  const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x, st = (long long)gridDim.x * blockDim.x;
+  long long done = 0;
+  if (n3 % 4 == 0) {
+    const double4_32a *s4 = reinterpret_cast<const double4_32a *>(s);
+    float4 *d4 = reinterpret_cast<float4 *>(d);
+    for (long long i = t0; i < n3 / 4; i += st) {
+      const double4_32a v = s4[i];
+      d4[i] = make_float4((float)(v.x - sh), (float)(v.y - sh), (float)(v.z - sh), (float)(v.w - sh));
+    }
+    done = n3;
+  }
+  for (long long i = done + t0; i < n3; i += st) d[i] = (float)(s[i] - sh);
 }
 __global__ void fields_from_state(const float *__restrict__ a, double *__restrict__ b, long long n3, int nac,
                                   double shift, int F) {
   const double sh = (int)blockIdx.y % F >= nac ? shift : 0.0;
   const float *s = a + blockIdx.y * n3;
   double *d = b + blockIdx.y * n3;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3; i += (long long)gridDim.x * blockDim.x)
-    d[i] = (double)s[i] + sh;
+  const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x, st = (long long)gridDim.x * blockDim.x;
+  long long done = 0;
+  if (n3 % 4 == 0) {
+    const float4 *s4 = reinterpret_cast<const float4 *>(s);
+    double4_32a *d4 = reinterpret_cast<double4_32a *>(d);
+    for (long long i = t0; i < n3 / 4; i += st) {
+      const float4 v = s4[i];
+      d4[i] = make_double4_32a((double)v.x + sh, (double)v.y + sh, (double)v.z + sh, (double)v.w + sh);
+    }
+    done = n3;
+  }
+  for (long long i = done + t0; i < n3; i += st) d[i] = (double)s[i] + sh;
 }
 
 int grid_of(long long total) {
