@@ -1,24 +1,28 @@
 // Kernels of the learned coarse-step corrector: a periodic 3x3x3 convolution
 // network on BF16 activations with FP32 accumulation.
 //
-// Activation layout: channels last, 32 BF16 channels per cell (64 bytes),
-// one haloed block of Np^3 cells per sample (Np = N + 2: the N^3 periodic
-// grid plus one periodic image layer per side), samples stacked in z:
-// cell(b, zh, yh, xh) = ((b Np + zh) Np + yh) Np + xh.
+// Activation layout (sclet_conv.cuh, conv_at): chunk-planar.  A sample is
+// Np = N + 2 haloed planes (the N^3 periodic grid plus one periodic image
+// layer per side); a plane holds 4 chunks of 8 channels, each chunk the
+// plane's Np^2 cells (slot = yh Np + xh, 16 bytes each) padded to a multiple
+// of 8 slots.
 //
 // conv_tc_kernel is an implicit GEMM on the 5th-generation tensor cores:
 //   D[cell][co] = sum_{tap, ci} A[cell + off(tap)][ci] * W[tap][co][ci]
 // with M = 128 cells, N = 32 output channels and K = 27 taps x 32 input
-// channels.  A tile is 128 consecutive "slots" of one haloed plane (slot =
-// yh Np + xh); for every tap the 128 input rows are again consecutive cells
-// (shifted by dz Np^2 + dy Np + dx), so each tap is one TMA box of 128 x 64 B,
-// whatever N is.  Slots in the x- or y-halo produce outputs that are dropped.
-// The weights (27 x 32 x 32 BF16, 54 KB) stay in shared memory.  Warp 0
-// issues TMA, warp 1 issues the MMAs (54 per tile: two K = 16 steps per tap)
-// into one of four 32-column TMEM accumulators, warps 2-5 drain them and run
-// the fused epilogue (bias, ReLU, residual, ReLU-mask, FP32 planar output).
-// The same kernel computes the data gradient of a convolution with the
-// weights flipped and transposed (the adjoint of a periodic convolution).
+// channels.  A tile is 128 consecutive slots of one haloed plane.  For every
+// plane dz of the stencil and every chunk, the rows all nine (dy, dx) taps
+// read are one contiguous run of 128 + 2 Np + 2 slots: the producer loads
+// those twelve runs (whole 128-byte lines, one TMA box each) and every tap's
+// operand is a descriptor into them (no-swizzle K-major layout: rows 16 bytes
+// apart, the chunks of a K step a box apart), offset by dy Np + dx rows.
+// Slots in the x- or y-halo produce outputs that are dropped.  The weights
+// (27 x 32 x 32 BF16, 54 KB) stay in shared memory.  Warp 0 issues TMA, warp 1
+// issues the MMAs (54 per tile: two K = 16 steps per tap) into one of four
+// 32-column TMEM accumulators, warps 2-5 drain them and run the fused
+// epilogue (bias, ReLU, residual, ReLU-mask, FP32 planar output).  The same
+// kernel computes the data gradient of a convolution with the weights
+// flipped and transposed (the adjoint of a periodic convolution).
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
@@ -47,17 +51,41 @@ using tc::smem_u32;
 using tc::tmem_ld32;
 
 constexpr int ROWS = 128;                  // cells per tile (MMA M)
-// tap tiles in flight: the loads come mostly from L2, and the pipeline is
-// bound by the bytes in flight per SM (eight stages kept the tensor pipe 6%
-// busy), so every stage the shared memory holds beside the weights
-constexpr int STAGES = 20;
-constexpr int ATILE = ROWS * CH * 2;       // 8 KB: 128 cells x 32 channels
+constexpr int MAX_STAGES = 3;              // tiles of input runs in flight
 constexpr int WTILE = CH * CH * 2;         // 2 KB: one tap's 32 x 32 weights
 constexpr int NACC = 4;                    // TMEM accumulators of 32 columns
 constexpr int TMEM_COLS = NACC * CH;       // 128
 constexpr int THREADS = 192;
-constexpr int SMEM_BYTES = TAPS * WTILE + STAGES * ATILE + 1024;
-static_assert(SMEM_BYTES <= 227 * 1024, "shared memory per CTA");
+constexpr int SMEM_LIMIT = 226 * 1024;  // dynamic shared memory: 227 KB per CTA less the static part
+
+// Per-launch geometry: each of the twelve runs of a tile is one box of
+// box_rows lines of 128 bytes (8 slots), enough for the run's 128 + 2 Np + 2
+// slots from any slot offset within the first line.
+struct Geom {
+  int box_rows, box_bytes, stage_bytes, stages, smem;
+};
+static Geom geom_of(int N) {
+  Geom g;
+  const int R = ROWS + 2 * (N + 2) + 2;
+  g.box_rows = (R + 7 + 7) / 8;
+  g.box_bytes = g.box_rows * 128;
+  g.stage_bytes = 12 * g.box_bytes;
+  g.stages = (SMEM_LIMIT - 1024 - TAPS * WTILE) / g.stage_bytes;
+  if (g.stages > MAX_STAGES) g.stages = MAX_STAGES;
+  g.smem = TAPS * WTILE + (g.stages > 0 ? g.stages : 1) * g.stage_bytes + 1024;
+  return g;
+}
+
+// Shared-memory matrix descriptor, K-major without swizzle: 8-row core
+// matrices 128 bytes apart (rows 16 bytes apart), K chunks lbo bytes apart.
+__device__ __forceinline__ uint64_t smem_desc_plain(uint32_t addr, uint32_t lbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;  // leading byte offset: next K chunk
+  d |= (uint64_t)(128 >> 4) << 32;              // stride byte offset: next 8 rows
+  d |= (uint64_t)1 << 46;                       // descriptor version
+  return d;                                     // layout type 0: no swizzle
+}
 
 __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar) {
   asm volatile(
@@ -86,10 +114,11 @@ __device__ __forceinline__ float bf(uint32_t w, int hi) {
 }
 
 __global__ void __launch_bounds__(THREADS, 1)
-    conv_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmW, ConvArgs g) {
+    conv_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmW, ConvArgs g,
+                   int box_bytes, int stages) {
   extern __shared__ uint8_t smem_raw[];
-  __shared__ __align__(8) uint64_t full_bar[STAGES];
-  __shared__ __align__(8) uint64_t empty_bar[STAGES];
+  __shared__ __align__(8) uint64_t full_bar[MAX_STAGES];
+  __shared__ __align__(8) uint64_t empty_bar[MAX_STAGES];
   __shared__ __align__(8) uint64_t tfull_bar[NACC];
   __shared__ __align__(8) uint64_t tempty_bar[NACC];
   __shared__ __align__(8) uint64_t w_bar;
@@ -100,16 +129,16 @@ __global__ void __launch_bounds__(THREADS, 1)
 
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint8_t *wsm = base;                    // 27 tap tiles of weights
-  uint8_t *asm_ = base + TAPS * WTILE;    // STAGES input tiles
+  uint8_t *asm_ = base + TAPS * WTILE;    // stages x 12 input runs
+  const int stage_bytes = 12 * box_bytes;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int N = g.N, Np = N + 2;
   const int per_plane = (N * Np + ROWS - 1) / ROWS;
   const int total = g.batch * N * per_plane;
-  const long long plane = (long long)Np * Np;
 
   if (threadIdx.x < CH) s_bias[threadIdx.x] = g.bias ? g.bias[threadIdx.x] : 0.0f;
   if (threadIdx.x == 0) {
-    for (int s = 0; s < STAGES; s++) {
+    for (int s = 0; s < MAX_STAGES; s++) {
       mbar_init(&full_bar[s], 1);
       mbar_init(&empty_bar[s], 1);
     }
@@ -139,23 +168,24 @@ __global__ void __launch_bounds__(THREADS, 1)
       mbar_expect_tx(&w_bar, TAPS * WTILE);
       for (int t = 0; t < TAPS; t++) tma_load_2d(wsm + t * WTILE, &tmW, 0, t * CH, &w_bar);
       int it = 0;
-      for (int tile = blockIdx.x; tile < total && !*(volatile int *)&failed; tile += gridDim.x) {
+      for (int tile = blockIdx.x; tile < total && !*(volatile int *)&failed; tile += gridDim.x, it++) {
         const Tile ti = tile_of(tile, N, Np, per_plane);
-        const long long pbase = ((long long)ti.b * Np + ti.zh) * plane + ti.s0;
-        for (int tap = 0; tap < TAPS; tap++, it++) {
-          const int s = it % STAGES;
-          if (it >= STAGES && !mbar_wait(&empty_bar[s], ((it / STAGES) & 1) ^ 1)) {
-            failed = 1;
-            break;
-          }
-          const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
-          const long long row = pbase + dz * plane + dy * Np + dx;
-          mbar_expect_tx(&full_bar[s], ATILE);
-          tma_load_2d(asm_ + s * ATILE, &tmA, 0, (int)row, &full_bar[s]);
+        const int s = it % stages;
+        if (it >= stages && !mbar_wait(&empty_bar[s], ((it / stages) & 1) ^ 1)) {
+          failed = 1;
+          break;
         }
+        // plane zh + dz - 1, chunk k: the run from slot s0 - Np - 1 (>= -1;
+        // a line before the buffer or past its end reads as zeros)
+        mbar_expect_tx(&full_bar[s], stage_bytes);
+        for (int dz = 0; dz < 3; dz++)
+          for (int k = 0; k < 4; k++) {
+            const long long flat = conv_at(N, ti.b, ti.zh + dz - 1, k, (long long)ti.s0 - Np - 1);
+            tma_load_2d(asm_ + s * stage_bytes + (dz * 4 + k) * box_bytes, &tmA, 0, (int)(flat >> 3), &full_bar[s]);
+          }
       }
       if (*(volatile int *)&failed) {
-        for (int i = it - STAGES < 0 ? 0 : it - STAGES; i < it; i++) mbar_wait(&full_bar[i % STAGES], (i / STAGES) & 1);
+        for (int i = it - stages < 0 ? 0 : it - stages; i < it; i++) mbar_wait(&full_bar[i % stages], (i / stages) & 1);
       }
       mbar_wait(&w_bar, 0);
     }
@@ -165,35 +195,40 @@ __global__ void __launch_bounds__(THREADS, 1)
       bool ok = mbar_wait(&w_bar, 0);
       if (!ok) failed = 1;
       fence_after();
-      int it = 0, j = 0;
+      int it = 0;
       const uint32_t w0 = smem_u32(wsm), a0 = smem_u32(asm_);
-      for (int tile = blockIdx.x; ok && tile < total && !*(volatile int *)&failed; tile += gridDim.x, j++) {
-        const int b = j % NACC;
-        if (j >= NACC && !mbar_wait(&tempty_bar[b], ((j / NACC) & 1) ^ 1)) {
+      for (int tile = blockIdx.x; ok && tile < total && !*(volatile int *)&failed; tile += gridDim.x, it++) {
+        const int b = it % NACC;
+        if (it >= NACC && !mbar_wait(&tempty_bar[b], ((it / NACC) & 1) ^ 1)) {
+          failed = 1;
+          break;
+        }
+        const int s = it % stages;
+        if (!mbar_wait(&full_bar[s], (it / stages) & 1)) {
           failed = 1;
           break;
         }
         fence_after();
         const uint32_t acc = tmem + (uint32_t)(b * CH);
-        for (int tap = 0; tap < TAPS; tap++, it++) {
-          const int s = it % STAGES;
-          if (!mbar_wait(&full_bar[s], (it / STAGES) & 1)) {
-            ok = false;
-            break;
-          }
-          fence_after();
+        const Tile ti = tile_of(tile, N, Np, per_plane);
+        const int shift = (int)(((long long)ti.s0 - Np - 1) & 7);  // the run's first slot within its first line
+        // descriptors of the stage's first run and of the first weight tile;
+        // a tap adds its run and row offsets (16-byte units) to the address
+        // field, which stays below 2^14 inside the shared memory
+        const uint64_t dab = smem_desc_plain(a0 + (uint32_t)(s * stage_bytes + shift * 16), box_bytes);
+        const uint64_t dwb = smem_desc(w0);
+        const uint32_t run16 = (uint32_t)box_bytes >> 4;
+#pragma unroll
+        for (int tap = 0; tap < TAPS; tap++) {
+          const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;  // each 0..2
 #pragma unroll
           for (int ks = 0; ks < 2; ks++) {
-            const uint64_t da = smem_desc(a0 + s * ATILE + ks * 32);
-            const uint64_t dw = smem_desc(w0 + tap * WTILE + ks * 32);
+            const uint64_t da = dab + (uint64_t)((uint32_t)(dz * 4 + 2 * ks) * run16 + (uint32_t)(dy * Np + dx));
+            const uint64_t dw = dwb + (uint64_t)((tap * WTILE + ks * 32) >> 4);
             mma_bf16(acc, da, dw, idesc, (tap == 0 && ks == 0) ? 0u : 1u);
           }
-          mma_commit(&empty_bar[s]);
         }
-        if (!ok) {
-          failed = 1;
-          break;
-        }
+        mma_commit(&empty_bar[s]);
         mma_commit(&tfull_bar[b]);
       }
       mma_commit(&done_bar);
@@ -222,7 +257,7 @@ __global__ void __launch_bounds__(THREADS, 1)
       const int s = ti.s0 + row;
       const int yh = s / Np, xh = s - yh * Np;
       if (yh >= 1 && yh <= N && xh >= 1 && xh <= N) {
-        const long long cell = ((long long)ti.b * Np + ti.zh) * plane + s;
+        const long long cell0 = conv_at(N, ti.b, ti.zh, 0, s), cstride = conv_chunk_slots(N);  // chunk k: cell0 + k cstride
         if (g.mode == CONV_OUT_F32) {
           // FP32 planar output of the first `cout` channels (owned cells)
           const long long n3 = (long long)N * N * N;
@@ -240,10 +275,10 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
             for (int c = 0; c < CH; c++) v[c] = acc[c] + s_bias[c];
           } else {
-            const uint4 *src = reinterpret_cast<const uint4 *>(g.aux + cell * CH);
+            const uint4 *src = reinterpret_cast<const uint4 *>(g.aux);
 #pragma unroll
             for (int k = 0; k < 4; k++) {
-              const uint4 w = src[k];
+              const uint4 w = src[cell0 + k * cstride];
               const uint32_t ww[4] = {w.x, w.y, w.z, w.w};
 #pragma unroll
               for (int h = 0; h < 8; h++) {
@@ -253,7 +288,7 @@ __global__ void __launch_bounds__(THREADS, 1)
               }
             }
           }
-          uint4 *dst = reinterpret_cast<uint4 *>(g.out + cell * CH);
+          uint4 *dst = reinterpret_cast<uint4 *>(g.out);
 #pragma unroll
           for (int k = 0; k < 4; k++) {
             uint32_t w[4];
@@ -262,7 +297,7 @@ __global__ void __launch_bounds__(THREADS, 1)
               const __nv_bfloat162 p = __floats2bfloat162_rn(v[k * 8 + 2 * h], v[k * 8 + 2 * h + 1]);
               w[h] = *reinterpret_cast<const uint32_t *>(&p);
             }
-            dst[k] = make_uint4(w[0], w[1], w[2], w[3]);
+            dst[cell0 + k * cstride] = make_uint4(w[0], w[1], w[2], w[3]);
           }
         }
       }
@@ -293,6 +328,22 @@ static cudaError_t make_map_rows(CUtensorMap *map, const void *ptr, long long ro
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
+// 2-D BF16 tensor map over an activation buffer as lines of 128 bytes (8 slots
+// of 16 bytes), no swizzle, boxes of box_rows lines; lines outside the buffer
+// read as zeros.
+static cudaError_t make_map_lines(CUtensorMap *map, const void *ptr, long long lines, int box_rows) {
+  auto fn = encode_fn();
+  if (!fn) return cudaErrorNotSupported;
+  cuuint64_t dims[2] = {64, (cuuint64_t)lines};
+  cuuint64_t strides[1] = {128};
+  cuuint32_t box[2] = {64, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(ptr), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
 // per device: the shared-memory attribute and the resident CTA count
 static cudaError_t conv_setup(int *ctas) {
   constexpr int MAXDEV = 64;
@@ -304,10 +355,10 @@ static cudaError_t conv_setup(int *ctas) {
   if (dev < 0 || dev >= MAXDEV) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lock(mu);
   if (!resident[dev]) {
-    e = cudaFuncSetAttribute(conv_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    e = cudaFuncSetAttribute(conv_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_LIMIT);
     if (e != cudaSuccess) return e;
     int per_sm = 0, sms = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, conv_tc_kernel, THREADS, SMEM_BYTES);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, conv_tc_kernel, THREADS, SMEM_LIMIT);
     if (e != cudaSuccess) return e;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
@@ -326,15 +377,17 @@ cudaError_t launch_conv(const __nv_bfloat16 *in, const __nv_bfloat16 *w, const C
   if (e != cudaSuccess) return e;
   const int N = args.N, Np = N + 2;
   if (N < 2 || args.batch < 1) return cudaErrorInvalidValue;
-  const long long cells = (long long)args.batch * Np * Np * Np;
-  if (cells >= 0x7fffffffLL) return cudaErrorInvalidValue;
+  const conv::Geom gm = conv::geom_of(N);
+  if (gm.stages < 1 || gm.box_rows > 256) return cudaErrorInvalidValue;  // N too large for one tile's runs
+  const long long lines = conv_units(N, args.batch) / 8;
+  if (lines >= 0x7fffffffLL) return cudaErrorInvalidValue;
   CUtensorMap ma, mw;
-  if ((e = conv::make_map_rows(&ma, in, cells, conv::ROWS)) != cudaSuccess) return e;
+  if ((e = conv::make_map_lines(&ma, in, lines, gm.box_rows)) != cudaSuccess) return e;
   if ((e = conv::make_map_rows(&mw, w, (long long)TAPS * CH, CH)) != cudaSuccess) return e;
   const long long per_plane = ((long long)N * Np + conv::ROWS - 1) / conv::ROWS;
   const long long tiles = (long long)args.batch * N * per_plane;
   const int grid = (int)(tiles < ctas ? tiles : ctas);
-  conv::conv_tc_kernel<<<grid, conv::THREADS, conv::SMEM_BYTES, s>>>(ma, mw, args);
+  conv::conv_tc_kernel<<<grid, conv::THREADS, gm.smem, s>>>(ma, mw, args, gm.box_bytes, gm.stages);
   launch_counter()++;
   return cudaGetLastError();
 }

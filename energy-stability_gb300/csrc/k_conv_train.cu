@@ -1,7 +1,8 @@
 // Element-wise and reduction kernels of the corrector network: periodic halo,
 // packing FP32 fields into haloed BF16 activations, the weight gradient of a
 // 3x3x3 convolution (FP32 accumulation), the BF16 weight copies, Adam and the
-// training residual.  Layouts as in k_conv.cu.
+// training residual.  Activations in the chunk-planar layout of
+// sclet_conv.cuh (conv_at).
 #include <cuda_bf16.h>
 #include <stdint.h>
 
@@ -46,10 +47,9 @@ __global__ void halo_kernel(__nv_bfloat16 *a, int N, int batch) {
       y = 1 + (int)(r % N);
       x = r < N ? 0 : Np - 1;
     }
-    const long long bb = (long long)b * Np * plane;
-    const long long dst = bb + ((long long)z * Np + y) * Np + x;
-    const long long src = bb + ((long long)wrap_h(z, N) * Np + wrap_h(y, N)) * Np + wrap_h(x, N);
-    reinterpret_cast<uint4 *>(a)[dst * 4 + k] = reinterpret_cast<const uint4 *>(a)[src * 4 + k];
+    const long long dst = conv_at(N, b, z, k, (long long)y * Np + x);
+    const long long src = conv_at(N, b, wrap_h(z, N), k, (long long)wrap_h(y, N) * Np + wrap_h(x, N));
+    reinterpret_cast<uint4 *>(a)[dst] = reinterpret_cast<const uint4 *>(a)[src];
   }
 }
 
@@ -75,9 +75,10 @@ __global__ void pack_kernel(const float *__restrict__ in, int cin, float scale, 
       const __nv_bfloat162 p = __floats2bfloat162_rn(v0, v1);
       w[c / 2] = *reinterpret_cast<const uint32_t *>(&p);
     }
-    uint4 *dst = reinterpret_cast<uint4 *>(a) + i * 4;
+    uint4 *dst = reinterpret_cast<uint4 *>(a);
+    const long long c0 = conv_at(N, b, z, 0, (long long)y * Np + x), cs = conv_chunk_slots(N);
 #pragma unroll
-    for (int k = 0; k < 4; k++) dst[k] = make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
+    for (int k = 0; k < 4; k++) dst[c0 + k * cs] = make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
   }
 }
 
@@ -94,8 +95,7 @@ __global__ void __launch_bounds__(64) wgrad_kernel(const __nv_bfloat16 *__restri
   const int tap = blockIdx.y;
   const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
   const int Np = N + 2;
-  const long long plane = (long long)Np * Np, n3 = (long long)N * N * N;
-  const long long off = dz * plane + dy * Np + dx;
+  const long long n3 = (long long)N * N * N;
   const long long total = n3 * batch;
   const int tid = threadIdx.x;
   const int co0 = (tid >> 3) * 4, ci0 = (tid & 7) * 4;
@@ -116,9 +116,8 @@ __global__ void __launch_bounds__(64) wgrad_kernel(const __nv_bfloat16 *__restri
         const int z = (int)(rr / ((long long)N * N));
         rr -= (long long)z * N * N;
         const int y = (int)(rr / N), x = (int)(rr - (long long)y * N);
-        const long long cell = (((long long)b * Np + z + 1) * Np + y + 1) * Np + x + 1;
-        gv = reinterpret_cast<const uint4 *>(g)[cell * 4 + k];
-        xv = reinterpret_cast<const uint4 *>(in)[(cell + off) * 4 + k];
+        gv = reinterpret_cast<const uint4 *>(g)[conv_at(N, b, z + 1, k, (long long)(y + 1) * Np + x + 1)];
+        xv = reinterpret_cast<const uint4 *>(in)[conv_at(N, b, z + 1 + dz, k, (long long)(y + 1 + dy) * Np + x + 1 + dx)];
       }
       const uint32_t gw[4] = {gv.x, gv.y, gv.z, gv.w}, xw[4] = {xv.x, xv.y, xv.z, xv.w};
 #pragma unroll
@@ -250,7 +249,7 @@ cudaError_t launch_conv_pack_grad(const float *g, int cout, float scale, int N, 
 }
 
 cudaError_t launch_conv_relu_mask(__nv_bfloat16 *g, const __nv_bfloat16 *act, int N, int batch, cudaStream_t s) {
-  const long long chunks = (long long)(N + 2) * (N + 2) * (N + 2) * batch * 4;
+  const long long chunks = conv_units(N, batch);
   relu_mask_kernel<<<grid_for(chunks, 256), 256, 0, s>>>(reinterpret_cast<uint4 *>(g),
                                                           reinterpret_cast<const uint4 *>(act), chunks);
   launch_counter()++;

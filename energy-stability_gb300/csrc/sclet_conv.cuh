@@ -9,6 +9,23 @@ namespace sclet {
 constexpr int CH = 32;    // channels of every activation (inputs and outputs zero padded)
 constexpr int TAPS = 27;  // 3 x 3 x 3 taps, t = (dz + 1) 9 + (dy + 1) 3 + (dx + 1)
 
+// Activation layout, chunk-planar: a sample is Np = N + 2 haloed planes (zh),
+// each plane 4 chunks of 8 channels (16 bytes per cell), each chunk the plane's
+// Np^2 cells (slot = yh Np + xh) padded to a multiple of 8 slots (so every
+// chunk starts on a 128-byte boundary).  Positions below are in 16-byte units.
+__host__ __device__ inline long long conv_chunk_slots(int N) {
+  const long long s = (long long)(N + 2) * (N + 2);
+  return (s + 7) / 8 * 8;
+}
+// chunk k (channels 8k .. 8k+7) of cell (zh, slot) of sample b
+__host__ __device__ inline long long conv_at(int N, int b, int zh, int k, long long slot) {
+  return (((long long)b * (N + 2) + zh) * 4 + k) * conv_chunk_slots(N) + slot;
+}
+// 16-byte units of `batch` samples
+__host__ __device__ inline long long conv_units(int N, int batch) {
+  return (long long)batch * (N + 2) * 4 * conv_chunk_slots(N);
+}
+
 // Epilogue of conv_tc_kernel (acc = the convolution, b = bias, a = aux at the cell):
 enum ConvMode {
   CONV_RELU = 0,      // out = max(acc + b, 0)                       (BF16)
@@ -30,7 +47,7 @@ struct ConvArgs {
   int *err;                  // set to 1 when a bounded wait gives up
 };
 
-// in: batch haloed blocks of (N + 2)^3 cells x CH BF16; w: TAPS x CH (co) x CH
+// in: batch haloed samples in the chunk-planar layout; w: TAPS x CH (co) x CH
 // (ci) BF16, ci fastest.
 cudaError_t launch_conv(const __nv_bfloat16 *in, const __nv_bfloat16 *w, const ConvArgs &args, cudaStream_t s);
 

@@ -91,8 +91,9 @@ void free_acts(sclet_net *net) {
 int ensure_acts(sclet_net *net, int N, int batch) {
   if (N == net->N && batch <= net->batch) return SCLET_OK;
   free_acts(net);
-  const long long Np = N + 2;
-  const long long elems = Np * Np * Np * batch * CH;
+  // chunk-planar activations (8 BF16 channels per 16-byte unit); zeroed once,
+  // so the padding slots of every chunk read as zeros
+  const long long elems = conv_units(N, batch) * 8;
   const size_t bytes = sizeof(__nv_bfloat16) * elems;
   NK(cudaMalloc(&net->x, bytes));
   for (auto &a : net->h) NK(cudaMalloc(&a, bytes));
@@ -101,6 +102,10 @@ int ensure_acts(sclet_net *net, int N, int batch) {
   NK(cudaMalloc(&net->ga, bytes));
   NK(cudaMalloc(&net->gh[0], bytes));
   NK(cudaMalloc(&net->gh[1], bytes));
+  for (__nv_bfloat16 *a : {net->x, net->gy, net->ga, net->gh[0], net->gh[1]})
+    NK(cudaMemsetAsync(a, 0, bytes, net->stream));
+  for (auto &a : net->h) NK(cudaMemsetAsync(a, 0, bytes, net->stream));
+  for (auto &a : net->r) NK(cudaMemsetAsync(a, 0, bytes, net->stream));
   const size_t outb = sizeof(float) * (size_t)SCLET_NET_OUT * N * N * N * batch;
   NK(cudaMalloc(&net->pred, outb));
   NK(cudaMalloc(&net->resid, outb));
