@@ -28,6 +28,7 @@
 #include <cudaTypedefs.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <mutex>
 
 #include "sclet_internal.cuh"
@@ -58,22 +59,33 @@ constexpr int TMEM_COLS = NACC * CH;       // 128
 constexpr int THREADS = 192;
 constexpr int SMEM_LIMIT = 226 * 1024;  // dynamic shared memory: 227 KB per CTA less the static part
 
-// Per-launch geometry: each of the twelve runs of a tile is one box of
-// box_rows lines of 128 bytes (8 slots), enough for the run's 128 + 2 Np + 2
-// slots from any slot offset within the first line.
+// Per-launch geometry.  ny = 1: per stencil plane and channel chunk one run
+// of 128 + 2 Np + 2 slots serves all nine in-plane taps (twelve runs a tile);
+// ny = 3: one run of 130 slots per stencil row dy (thirty-six runs a tile,
+// fewer bytes once Np exceeds about 148).  A run is one box of box_rows lines
+// of 128 bytes (8 slots), enough from any slot offset within the first line.
 struct Geom {
-  int box_rows, box_bytes, stage_bytes, stages, smem;
+  int ny, box_rows, box_bytes, stage_bytes, stages, smem;
 };
-static Geom geom_of(int N) {
+static Geom geom_for(int N, int ny) {
   Geom g;
-  const int R = ROWS + 2 * (N + 2) + 2;
+  g.ny = ny;
+  const int R = ny == 1 ? ROWS + 2 * (N + 2) + 2 : ROWS + 2;
   g.box_rows = (R + 7 + 7) / 8;
   g.box_bytes = g.box_rows * 128;
-  g.stage_bytes = 12 * g.box_bytes;
+  g.stage_bytes = 12 * ny * g.box_bytes;
   g.stages = (SMEM_LIMIT - 1024 - TAPS * WTILE) / g.stage_bytes;
   if (g.stages > MAX_STAGES) g.stages = MAX_STAGES;
   g.smem = TAPS * WTILE + (g.stages > 0 ? g.stages : 1) * g.stage_bytes + 1024;
   return g;
+}
+std::atomic<int> g_runs_per_plane{0};  // 0: by N; 1 or 3: forced (sclet_net_set_conv_runs)
+static Geom geom_of(int N) {
+  const Geom a = geom_for(N, 1), b = geom_for(N, 3);
+  const int forced = g_runs_per_plane.load();
+  if (forced == 1 && a.stages >= 1) return a;
+  if (forced == 3) return b;
+  return a.stages >= 1 && a.stage_bytes <= b.stage_bytes ? a : b;
 }
 
 // Shared-memory matrix descriptor, K-major without swizzle: 8-row core
@@ -115,7 +127,7 @@ __device__ __forceinline__ float bf(uint32_t w, int hi) {
 
 __global__ void __launch_bounds__(THREADS, 1)
     conv_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmW, ConvArgs g,
-                   int box_bytes, int stages) {
+                   int box_bytes, int stages, int ny) {
   extern __shared__ uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t full_bar[MAX_STAGES];
   __shared__ __align__(8) uint64_t empty_bar[MAX_STAGES];
@@ -129,8 +141,8 @@ __global__ void __launch_bounds__(THREADS, 1)
 
   uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint8_t *wsm = base;                    // 27 tap tiles of weights
-  uint8_t *asm_ = base + TAPS * WTILE;    // stages x 12 input runs
-  const int stage_bytes = 12 * box_bytes;
+  uint8_t *asm_ = base + TAPS * WTILE;    // stages x 12 ny input runs
+  const int stage_bytes = 12 * ny * box_bytes;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int N = g.N, Np = N + 2;
   const int per_plane = (N * Np + ROWS - 1) / ROWS;
@@ -175,14 +187,18 @@ __global__ void __launch_bounds__(THREADS, 1)
           failed = 1;
           break;
         }
-        // plane zh + dz - 1, chunk k: the run from slot s0 - Np - 1 (>= -1;
-        // a line before the buffer or past its end reads as zeros)
+        // plane zh + dz - 1, chunk k: the run from slot s0 - Np - 1 (ny = 1)
+        // or s0 + (dy - 1) Np - 1 (ny = 3), >= -1; a line before the buffer
+        // or past its end reads as zeros
         mbar_expect_tx(&full_bar[s], stage_bytes);
         for (int dz = 0; dz < 3; dz++)
-          for (int k = 0; k < 4; k++) {
-            const long long flat = conv_at(N, ti.b, ti.zh + dz - 1, k, (long long)ti.s0 - Np - 1);
-            tma_load_2d(asm_ + s * stage_bytes + (dz * 4 + k) * box_bytes, &tmA, 0, (int)(flat >> 3), &full_bar[s]);
-          }
+          for (int r = 0; r < ny; r++)
+            for (int k = 0; k < 4; k++) {
+              const long long first = (long long)ti.s0 + (ny == 1 ? -Np : (r - 1) * Np) - 1;
+              const long long flat = conv_at(N, ti.b, ti.zh + dz - 1, k, first);
+              tma_load_2d(asm_ + s * stage_bytes + ((dz * ny + r) * 4 + k) * box_bytes, &tmA, 0, (int)(flat >> 3),
+                          &full_bar[s]);
+            }
       }
       if (*(volatile int *)&failed) {
         for (int i = it - stages < 0 ? 0 : it - stages; i < it; i++) mbar_wait(&full_bar[i % stages], (i / stages) & 1);
@@ -211,11 +227,19 @@ __global__ void __launch_bounds__(THREADS, 1)
         fence_after();
         const uint32_t acc = tmem + (uint32_t)(b * CH);
         const Tile ti = tile_of(tile, N, Np, per_plane);
-        const int shift = (int)(((long long)ti.s0 - Np - 1) & 7);  // the run's first slot within its first line
+        // per stencil row dy: the run holding it (its offset in runs from the
+        // plane's first) and the row of the tap dx = -1 within that run
+        uint32_t rrun[3], rrow[3];
+#pragma unroll
+        for (int dy = 0; dy < 3; dy++) {
+          const long long first = (long long)ti.s0 + (ny == 1 ? -Np : (dy - 1) * Np) - 1;
+          rrun[dy] = ny == 1 ? 0u : (uint32_t)(dy * 4);
+          rrow[dy] = (uint32_t)(first & 7) + (ny == 1 ? (uint32_t)(dy * Np) : 0u);
+        }
         // descriptors of the stage's first run and of the first weight tile;
         // a tap adds its run and row offsets (16-byte units) to the address
         // field, which stays below 2^14 inside the shared memory
-        const uint64_t dab = smem_desc_plain(a0 + (uint32_t)(s * stage_bytes + shift * 16), box_bytes);
+        const uint64_t dab = smem_desc_plain(a0 + (uint32_t)(s * stage_bytes), box_bytes);
         const uint64_t dwb = smem_desc(w0);
         const uint32_t run16 = (uint32_t)box_bytes >> 4;
 #pragma unroll
@@ -223,7 +247,8 @@ __global__ void __launch_bounds__(THREADS, 1)
           const int dz = tap / 9, dy = (tap / 3) % 3, dx = tap % 3;  // each 0..2
 #pragma unroll
           for (int ks = 0; ks < 2; ks++) {
-            const uint64_t da = dab + (uint64_t)((uint32_t)(dz * 4 + 2 * ks) * run16 + (uint32_t)(dy * Np + dx));
+            const uint64_t da =
+                dab + (uint64_t)(((uint32_t)(dz * ny * 4 + 2 * ks) + rrun[dy]) * run16 + rrow[dy] + (uint32_t)dx);
             const uint64_t dw = dwb + (uint64_t)((tap * WTILE + ks * 32) >> 4);
             mma_bf16(acc, da, dw, idesc, (tap == 0 && ks == 0) ? 0u : 1u);
           }
@@ -371,6 +396,11 @@ static cudaError_t conv_setup(int *ctas) {
 
 }  // namespace conv
 
+int conv_set_runs(int runs_per_plane) {
+  if (runs_per_plane != 0 && runs_per_plane != 1 && runs_per_plane != 3) return -1;
+  return conv::g_runs_per_plane.exchange(runs_per_plane);
+}
+
 cudaError_t launch_conv(const __nv_bfloat16 *in, const __nv_bfloat16 *w, const ConvArgs &args, cudaStream_t s) {
   int ctas = 0;
   cudaError_t e = conv::conv_setup(&ctas);
@@ -378,7 +408,7 @@ cudaError_t launch_conv(const __nv_bfloat16 *in, const __nv_bfloat16 *w, const C
   const int N = args.N, Np = N + 2;
   if (N < 2 || args.batch < 1) return cudaErrorInvalidValue;
   const conv::Geom gm = conv::geom_of(N);
-  if (gm.stages < 1 || gm.box_rows > 256) return cudaErrorInvalidValue;  // N too large for one tile's runs
+  if (gm.stages < 1 || gm.box_rows > 256) return cudaErrorInvalidValue;
   const long long lines = conv_units(N, args.batch) / 8;
   if (lines >= 0x7fffffffLL) return cudaErrorInvalidValue;
   CUtensorMap ma, mw;
@@ -387,7 +417,7 @@ cudaError_t launch_conv(const __nv_bfloat16 *in, const __nv_bfloat16 *w, const C
   const long long per_plane = ((long long)N * Np + conv::ROWS - 1) / conv::ROWS;
   const long long tiles = (long long)args.batch * N * per_plane;
   const int grid = (int)(tiles < ctas ? tiles : ctas);
-  conv::conv_tc_kernel<<<grid, conv::THREADS, gm.smem, s>>>(ma, mw, args, gm.box_bytes, gm.stages);
+  conv::conv_tc_kernel<<<grid, conv::THREADS, gm.smem, s>>>(ma, mw, args, gm.box_bytes, gm.stages, gm.ny);
   launch_counter()++;
   return cudaGetLastError();
 }

@@ -50,6 +50,9 @@ struct ConvArgs {
 // in: batch haloed samples in the chunk-planar layout; w: TAPS x CH (co) x CH
 // (ci) BF16, ci fastest.
 cudaError_t launch_conv(const __nv_bfloat16 *in, const __nv_bfloat16 *w, const ConvArgs &args, cudaStream_t s);
+// Input runs per tile of launch_conv (sclet_net_set_conv_runs); returns the
+// previous setting, -1 for an invalid one.
+int conv_set_runs(int runs_per_plane);
 
 // Periodic halo of batch haloed blocks, in place.
 cudaError_t launch_conv_halo(__nv_bfloat16 *a, int N, int batch, cudaStream_t s);

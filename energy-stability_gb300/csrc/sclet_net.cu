@@ -354,6 +354,8 @@ int sclet_net_train_step(sclet_net *net, int N, int batch, const float *in, cons
   return SCLET_OK;
 }
 
+int sclet_net_set_conv_runs(int runs_per_plane) { return conv_set_runs(runs_per_plane); }
+
 }  // extern "C"
 
 namespace sclet {

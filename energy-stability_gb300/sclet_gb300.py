@@ -138,6 +138,7 @@ SIGNATURES = {
     "sclet_net_forward": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                           ctypes.c_void_p]),
     "sclet_net_sync": (ctypes.c_int, [ctypes.c_void_p]),
+    "sclet_net_set_conv_runs": (ctypes.c_int, [ctypes.c_int]),
     "sclet_net_gradient": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                            ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]),
     "sclet_net_train_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,

@@ -405,6 +405,12 @@ int sclet_net_gradient(sclet_net *net, int N, int batch, const float *in, const 
 /* sclet_net_gradient followed by one Adam step (beta 0.9 / 0.999). */
 int sclet_net_train_step(sclet_net *net, int N, int batch, const float *in, const float *target, float lr,
                          double *loss);
+/* Input runs of the convolution kernel per 128-cell tile, process-wide: 0
+ * chooses by N (the default), 1 one run per stencil plane and channel chunk,
+ * 3 one run per stencil row.  Both tilings compute the same sums in the same
+ * order; the setting is there to test that.  Returns the previous setting,
+ * or -1 for a value other than 0, 1, 3. */
+int sclet_net_set_conv_runs(int runs_per_plane);
 
 /* Coarse steps judged by the plain-ETD checks.  coarse and fine are two
  * contexts of the same run on one device, coarse.dt = ratio * fine.dt.  Each

@@ -44,6 +44,34 @@ def test_forward_matches_oracle(N, B, learned):
     net.close()
 
 
+def test_conv_tilings_agree(learned, sclet_lib):
+    """The convolution kernel's two tilings (one input run per stencil plane
+    and channel chunk, as small grids use; one per stencil row, as grids of
+    N >= 146 use) give the same forward pass bit for bit, at 24^3 and at a
+    grid where the planes' slot counts are not multiples of 8."""
+    torch = _torch()
+    L = sclet_lib.lib()
+    p = co.random_params(9).astype(np.float32)
+    for N, B in ((24, 2), (13, 1)):
+        rng = np.random.default_rng(N)
+        inp = torch.from_numpy((rng.random((B, co.NIN, N, N, N)) - 0.5).astype(np.float32)).cuda()
+        outs = []
+        try:
+            for runs in (1, 3):
+                assert L.sclet_net_set_conv_runs(runs) in (0, 1, 3)
+                net = learned.Net(seed=1, out_scale=0.5)
+                net.set_params(p)
+                y = torch.empty((B, co.NOUT, N, N, N), dtype=torch.float32, device="cuda")
+                net.forward(inp, y)
+                outs.append(y.cpu().numpy())
+                net.close()
+        finally:
+            L.sclet_net_set_conv_runs(0)
+        np.testing.assert_array_equal(outs[0], outs[1], err_msg=f"N={N}")
+        assert np.isfinite(outs[0]).all() and np.abs(outs[0]).max() > 0
+    assert L.sclet_net_set_conv_runs(2) == -1
+
+
 def test_gradients_match_oracle(learned):
     torch = _torch()
     rng = np.random.default_rng(3)
