@@ -30,13 +30,16 @@ struct TcArgs {
   int idle;                 // 1: the producer issues no loads (the bounded-wait self-test)
 };
 
+// kp = n rounded up to whole k-blocks of 32: the slice planes are k-blocked,
+// [p][kp / 32][rows][32], columns n .. kp - 1 zero
 int tc_kp(int n);
 int tc_slice_bits(int n);
-// Row-major FP64 n x n matrix -> TC_PLANES_M slice planes [p][n][kp] (zero padded
-// columns) and the power-of-two scale of each row.
+// Row-major FP64 n x n matrix -> TC_PLANES_M k-blocked slice planes
+// [p][kp / 32][n][32] (zero padded columns) and the power-of-two scale of each row.
 cudaError_t tc_slice_matrix(const double *m, __nv_bfloat16 *planes, float *row_scale, int n, cudaStream_t s);
-// FP32 blocks (x - sub; sub may be null), rows of n -> slice planes
-// [count][p][n*n][kp] with the power-of-two scale of each row in scale[count][n*n].
+// FP32 blocks (x - sub; sub may be null), rows of n -> k-blocked slice planes
+// [count][p][kp / 32][n*n][32] with the power-of-two scale of each row in
+// scale[count][n*n]; the pad columns are never written (zero from allocation).
 cudaError_t tc_slice_fields(const float *x, const float *sub, float *scale, __nv_bfloat16 *planes, int n, int count,
                             cudaStream_t s);
 // ETD coefficient tables of one field kind (see TcArgs::coef)
