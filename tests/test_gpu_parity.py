@@ -154,3 +154,33 @@ def test_beta_omega_64_cubed_1000_steps(tmp_path, sclet_lib):
     np.testing.assert_allclose(ours, g["diag"], rtol=1e-10, atol=1e-13)
     free = np.array(free)
     assert np.all(np.diff(free) <= 1e-12 * np.abs(free[:-1])), "free energy increased"
+
+
+@pytest.mark.parametrize("precision_name", ["FP64", "MIXED"])
+def test_nan_in_the_state_is_reported(precision_name, tmp_path, sclet_lib):
+    """A NaN planted in one owned cell on the host: the diagnostics report
+    SCLET_ERR_NONFINITE (an error code, no exit and no device fault), before
+    and after a step that spreads it, and the device stays usable: a new
+    context on it steps and checks normally."""
+    sg = sclet_lib
+    case = cases.Case(big_n=24, nac=4, nch=1, steps=2, seed=3, suffix="nan")
+    d = str(tmp_path)
+    cases.write_case(case, d)
+    p = sg.read_case(d, case.suffix)
+    s = sg.Solver(p, getattr(sg, precision_name))
+    u0 = np.zeros((s.F, case.n, case.n, case.n))
+    u0[:, 2:-2, 2:-2, 2:-2] = 0.01
+    u0[s.nac:] += 0.5
+    bad = u0.copy()
+    bad[1, 7, 8, 9] = np.nan
+    s.set_fields(bad)
+    for _ in range(2):
+        with pytest.raises(sg.ScletError, match=r"\(7\)"):
+            s.check_soln(1)
+        s.step(1)
+    s.close()
+    s = sg.Solver(p, getattr(sg, precision_name))
+    s.set_fields(u0)
+    s.step(1)
+    assert np.isfinite(s.check_soln(1)).all()
+    s.close()
