@@ -237,7 +237,6 @@ int sclet_net_create(int device, unsigned long long seed, float out_scale, sclet
   sclet_net *net = new sclet_net();
   net->device = device;
   net->out_scale = out_scale;
-  int rc = SCLET_OK;
   auto undo = [&](int code) {
     *out = net;  // the caller reads the message, then destroys
     return code;
@@ -270,7 +269,6 @@ int sclet_net_create(int device, unsigned long long seed, float out_scale, sclet
   init_params(h, seed);
   NC(cudaMemcpy(net->p, h.data(), pb, cudaMemcpyHostToDevice));
 #undef NC
-  (void)rc;
   *out = net;
   return SCLET_OK;
 }
